@@ -1,0 +1,180 @@
+/*
+ * lofgb.h — C ABI of liblofgb.so, the GB300 (sm_103a) kernels behind the
+ * LoFloat emulation ops.
+ *
+ * Every entry point:
+ *   - takes plain device pointers, element counts and a cudaStream_t passed as
+ *     `void*` (NULL = legacy default stream); no torch types cross this line;
+ *   - launches asynchronously on that stream and never synchronises the device;
+ *   - returns LOFGB_OK (0) or a negative LOFGB_ERR_* code, never exits/aborts;
+ *     lofgb_strerror() turns a code into text, lofgb_last_error_detail() gives
+ *     the message of the last failing call on the calling host thread;
+ *   - writes out-of-place; `in == out` (fully aliased) is allowed for the
+ *     elementwise and MX entry points;
+ *   - leaves all memory to the caller (inputs borrowed, outputs preallocated).
+ *
+ * Each declaration names the reference interface it replaces
+ * (SudhanvaKulkarni123/LoFloat, path:line).
+ */
+#ifndef LOFGB_H
+#define LOFGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- enums: integer values follow the reference's X-macro order ---------
+ * src/fp_tools.hpp:13-28 (rounding_modes), :30-32 (signednesses),
+ * :34-36 (inf_behaviors), :44-46 (nan_behaviors). The Python enums of the
+ * reference binding (src/LoPy_bind.cpp:284-313) expose the same integers. */
+enum lofgb_rounding_mode {
+    LOFGB_RNE = 0,              /* RoundToNearestEven */
+    LOFGB_RTZ = 1,              /* RoundTowardsZero */
+    LOFGB_RAFZ = 2,             /* RoundAwayFromZero */
+    LOFGB_SR_A = 3,             /* StochasticRoundingA */
+    LOFGB_RNO = 4,              /* RoundToNearestOdd */
+    LOFGB_RD = 5,               /* RoundDown */
+    LOFGB_RU = 6,               /* RoundUp */
+    LOFGB_RTA = 7,              /* RoundTiesToAway */
+    LOFGB_SR_B = 8,             /* StochasticRoundingB */
+    LOFGB_SR_C = 9,             /* StochasticRoundingC */
+    LOFGB_TRUE_SR = 10,         /* True_StochasticRounding */
+    LOFGB_PROB = 11,            /* ProbabilisticRounding */
+    LOFGB_RTO = 12,             /* RoundToOdd */
+    LOFGB_RTTZ = 13,            /* RoundTiesTowardsZero */
+    LOFGB_SR_D = 14,            /* StochasticRoundingD */
+    LOFGB_NUM_MODES = 15
+};
+enum lofgb_inf_behavior { LOFGB_INF_EXTENDED = 0, LOFGB_INF_SATURATING = 1 };
+enum lofgb_nan_behavior { LOFGB_NAN_3109 = 0, LOFGB_NAN_754 = 1 };
+enum lofgb_signedness { LOFGB_SIGNED = 0, LOFGB_UNSIGNED = 1 };
+
+/* Runtime float format. Mirrors the fields of FloatingPointParams that the
+ * rounding path reads (src/fp_tools.hpp:187-252) and of the Python
+ * FloatFormatDescriptor (src/LoPy_bind.cpp:45-68). The inf/NaN checker
+ * functors are not carried: virtual_round never calls them
+ * (src/lo_float.h:2843-2939). */
+typedef struct lofgb_format {
+    int32_t bitwidth;       /* total bits incl. sign (if signed)            */
+    int32_t mantissa_bits;  /* fraction bits                                 */
+    int32_t bias;           /* exponent bias                                 */
+    uint8_t inf_behavior;   /* lofgb_inf_behavior                            */
+    uint8_t nan_behavior;   /* lofgb_nan_behavior (carried, not used)        */
+    uint8_t signedness;     /* lofgb_signedness                              */
+    uint8_t reserved;       /* must be 0                                     */
+} lofgb_format;
+
+/* ---- status codes -------------------------------------------------------- */
+enum lofgb_status {
+    LOFGB_OK = 0,
+    LOFGB_ERR_NULL = -1,          /* NULL pointer where data is required     */
+    LOFGB_ERR_SIZE = -2,          /* negative / inconsistent sizes            */
+    LOFGB_ERR_FORMAT = -3,        /* format fields out of supported range     */
+    LOFGB_ERR_MODE = -4,          /* unknown rounding mode / bad stoch_len    */
+    LOFGB_ERR_BLOCK = -5,         /* unsupported MX block size                */
+    LOFGB_ERR_ALIAS = -6,         /* partially overlapping in/out             */
+    LOFGB_ERR_UNSUPPORTED = -7,   /* valid request the kernel does not cover  */
+    LOFGB_ERR_CUDA = -8,          /* CUDA runtime error (see detail string)   */
+    LOFGB_ERR_WORKSPACE = -9,     /* caller workspace too small               */
+    LOFGB_ERR_TIMEOUT = -10       /* a bounded device-side wait expired       */
+};
+
+const char* lofgb_strerror(int status);
+/* Message of the last failing call made by this host thread ("" if none). */
+const char* lofgb_last_error_detail(void);
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+int lofgb_version(void);
+
+/* ---- (a) virtual rounding to a runtime format ----------------------------
+ * Replaces the CUDA branch of virtual_round_params (src/LoPy_bind.cpp:122-139)
+ * → round_fp_params / round_fp_params_kernel (src/Lof_kernel.cu:49-60), scalar
+ * semantics lo_float::virtual_round(x, FloatingPointParams, ProjSpec)
+ * (src/lo_float.h:2843-2939, public wrapper :4271-4274).
+ * out[i] = virtual_round(scale * in[i], fmt, {mode, OvfInf, stoch_len}).
+ * `scale` is applied in the source type, as the reference kernel does
+ * (src/Lof_kernel.cu:52); scale == 1 skips the multiply.
+ * Stochastic modes draw R = SplitMix64(seed, offset + i) per element i.
+ * f16 data is IEEE binary16 bit patterns (uint16_t). */
+int lofgb_round_f32(const float* in, float* out, int64_t n, const lofgb_format* fmt,
+                    int mode, int stoch_len, float scale, uint64_t seed,
+                    uint64_t offset, void* stream);
+int lofgb_round_f64(const double* in, double* out, int64_t n, const lofgb_format* fmt,
+                    int mode, int stoch_len, double scale, uint64_t seed,
+                    uint64_t offset, void* stream);
+int lofgb_round_f16(const uint16_t* in, uint16_t* out, int64_t n, const lofgb_format* fmt,
+                    int mode, int stoch_len, float scale, uint64_t seed,
+                    uint64_t offset, void* stream);
+
+/* ---- (a') mantissa-only rounding -----------------------------------------
+ * Replaces virtual_round_mantissa (src/LoPy_bind.cpp:80-120) → round_mantissa /
+ * round_mantissa_kernel (src/Lof_kernel.cu:37-48), scalar semantics
+ * lo_float::virtual_round(x, int ToMantissaBits, ProjSpec)
+ * (src/lo_float.h:2715-2756, wrapper :4258-4261). */
+int lofgb_round_mantissa_f32(const float* in, float* out, int64_t n, int mantissa_bits,
+                             int mode, int stoch_len, float scale, uint64_t seed,
+                             uint64_t offset, void* stream);
+int lofgb_round_mantissa_f64(const double* in, double* out, int64_t n, int mantissa_bits,
+                             int mode, int stoch_len, double scale, uint64_t seed,
+                             uint64_t offset, void* stream);
+int lofgb_round_mantissa_f16(const uint16_t* in, uint16_t* out, int64_t n,
+                             int mantissa_bits, int mode, int stoch_len, float scale,
+                             uint64_t seed, uint64_t offset, void* stream);
+
+/* ---- (b) MX block rounding -----------------------------------------------
+ * Replaces virtual_mx_round (src/LoPy_bind.cpp:165-217) → run_virtual_mx_round
+ * (src/Lof_kernel.cu:70-94) → virtual_mx_round<float,256,MX,NX>
+ * (src/mx_round.cuh:27-214). Contiguous blocks of `block_size` elements; the
+ * trailing partial block is masked. block_size ∈ {8,16,32,64,128,256}
+ * (the reference launcher accepts 16..256). Element SR draws use counter
+ * offset + i; scale rounding never uses stochastic bits (stoch_len 0, as
+ * src/mx_round.cuh:58-65). */
+int lofgb_mx_round_f32(const float* in, float* out, int64_t n, int block_size,
+                       const lofgb_format* elem_fmt, const lofgb_format* scale_fmt,
+                       int mode, int scale_mode, int stoch_len, uint64_t seed,
+                       uint64_t offset, void* stream);
+
+/* ---- (c) emulated-accumulation GEMM --------------------------------------
+ * Replaces LoF_gemm (src/Lof_kernel.cu:96-154) → lo_float::Gemm::run_scaled
+ * (src/cutlass_gemms.cuh:1777-1787) with the OpLoFMultiplyAdd leaf
+ * (src/cutlass_gemms.cuh:97-168).
+ *
+ * D[i,j] = alpha * acc_K(i,j), acc_0 = +0,
+ * acc_{k+1} = RNE_m(rto_fma(A[i,k], B[k,j], acc_k))  for k = 0..K-1 in order.
+ * A is M×K (trans_a = 0: row-major with leading dim lda ≥ K; trans_a = 1:
+ * stored K×M row-major, lda ≥ M). B is K×N (trans_b = 0: row-major, ldb ≥ N;
+ * trans_b = 1: stored N×K, ldb ≥ K). D is M×N row-major, ldd ≥ N.
+ * The reference leaf ignores the rounding mode and always uses RNE
+ * (src/cutlass_gemms.cuh:122); `mode` must be LOFGB_RNE.
+ * alpha: the caller passes 1/(scale_a*scale_b) (1 if the product is 0), as
+ * run_scaled computes it (src/cutlass_gemms.cuh:1784-1786).
+ *
+ * variant LOFGB_GEMM_PLAIN: CUDA cores, bit-exact, needs no workspace.
+ * variant LOFGB_GEMM_TC: tcgen05 tensor cores; each k-chunk of `chunk`
+ * (multiple of 16) is summed in FP32 in TMEM and then rounded into the
+ * emulated accumulator: acc = RNE_m(rto(acc + chunk_sum)). Operands are split
+ * into BF16 hi+lo pairs (3 MMAs per k-step; the lo·lo term is dropped). Not
+ * bit-exact; error is stated against lofgb_gemm_f64_ref. Needs `workspace` of
+ * lofgb_gemm_tc_workspace_size(M,N,K) bytes (256-byte aligned). */
+enum lofgb_gemm_variant { LOFGB_GEMM_PLAIN = 0, LOFGB_GEMM_TC = 1 };
+
+int lofgb_gemm_f32(const float* A, int64_t lda, int trans_a, const float* B, int64_t ldb,
+                   int trans_b, float* D, int64_t ldd, int M, int N, int K,
+                   int accum_mant_bits, int mode, float alpha, int variant, int chunk,
+                   void* workspace, size_t workspace_bytes, void* stream);
+size_t lofgb_gemm_tc_workspace_size(int M, int N, int K);
+
+/* FP64 GPU oracle GEMM used only to state the error of the tensor-core form:
+ * D[i,j] = sum_k (double)A[i,k]*(double)B[k,j] in FP64, same layouts as above.
+ * No counterpart in the reference (its harness compares against cuBLAS SGEMM,
+ * test/gemm_test.cu:114). */
+int lofgb_gemm_f64_ref(const float* A, int64_t lda, int trans_a, const float* B,
+                       int64_t ldb, int trans_b, double* D, int64_t ldd, int M, int N,
+                       int K, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LOFGB_H */

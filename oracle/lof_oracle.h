@@ -1,0 +1,112 @@
+/*
+ * lof_oracle.h — TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of the reference's rounding, MX and emulated-accumulation
+ * GEMM arithmetic (SudhanvaKulkarni123/LoFloat). It is the checker for the
+ * CUDA kernels in liblofgb.so and the CPU baseline timed by bench.py. Only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it;
+ * the product path never calls it.
+ *
+ * Pinning: tests/golden/ holds vectors produced by the reference's own scalar
+ * functions (src/lo_float.h compiled from the reference sources by
+ * oracle/ref_shim.cpp); tests/test_oracle_golden.py checks this oracle
+ * against them bit for bit.
+ */
+#ifndef LOF_ORACLE_H
+#define LOF_ORACLE_H
+#include <stdint.h>
+#include "../include/lofgb.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* SplitMix64 (Steele, Lea, Flood 2014) as a counter-based generator: the
+ * idx-th output of a SplitMix64 stream whose state starts at `seed`. */
+uint64_t orc_rng(uint64_t seed, uint64_t idx);
+
+/* Scalar cores. `rbits` is the random word for stochastic modes; `usamp` is
+ * the uniform [0,1) sample used by True_StochasticRounding (pass a negative
+ * value to derive it from rbits as (rbits >> 11) * 2^-53). */
+float orc_vr_f32(float x, const lofgb_format* f, int mode, int len, uint64_t rbits,
+                 double usamp);
+double orc_vr_f64(double x, const lofgb_format* f, int mode, int len, uint64_t rbits,
+                  double usamp);
+uint16_t orc_vr_f16(uint16_t x, const lofgb_format* f, int mode, int len,
+                    uint64_t rbits, double usamp);
+float orc_vm_f32(float x, int mbits, int mode, int len, uint64_t rbits, double usamp);
+double orc_vm_f64(double x, int mbits, int mode, int len, uint64_t rbits, double usamp);
+uint16_t orc_vm_f16(uint16_t x, int mbits, int mode, int len, uint64_t rbits,
+                    double usamp);
+
+/* Array forms with the library's (seed, offset) RNG contract. Return 0 or a
+ * LOFGB_ERR_* code (same validation as the library). nthreads <= 0 → all. */
+int orc_round_f32(const float* in, float* out, int64_t n, const lofgb_format* f,
+                  int mode, int len, float scale, uint64_t seed, uint64_t offset,
+                  int nthreads);
+int orc_round_f64(const double* in, double* out, int64_t n, const lofgb_format* f,
+                  int mode, int len, double scale, uint64_t seed, uint64_t offset,
+                  int nthreads);
+int orc_round_f16(const uint16_t* in, uint16_t* out, int64_t n, const lofgb_format* f,
+                  int mode, int len, float scale, uint64_t seed, uint64_t offset,
+                  int nthreads);
+int orc_round_mantissa_f32(const float* in, float* out, int64_t n, int mbits, int mode,
+                           int len, float scale, uint64_t seed, uint64_t offset,
+                           int nthreads);
+int orc_round_mantissa_f64(const double* in, double* out, int64_t n, int mbits,
+                           int mode, int len, double scale, uint64_t seed,
+                           uint64_t offset, int nthreads);
+int orc_round_mantissa_f16(const uint16_t* in, uint16_t* out, int64_t n, int mbits,
+                           int mode, int len, float scale, uint64_t seed,
+                           uint64_t offset, int nthreads);
+
+/* Array forms with explicit per-element random words (golden pinning). */
+int orc_round_f32_bits(const float* in, float* out, int64_t n, const lofgb_format* f,
+                       int mode, int len, const uint64_t* rbits, const double* usamp);
+int orc_round_f64_bits(const double* in, double* out, int64_t n, const lofgb_format* f,
+                       int mode, int len, const uint64_t* rbits, const double* usamp);
+int orc_round_f16_bits(const uint16_t* in, uint16_t* out, int64_t n,
+                       const lofgb_format* f, int mode, int len, const uint64_t* rbits,
+                       const double* usamp);
+int orc_round_mantissa_f32_bits(const float* in, float* out, int64_t n, int mbits,
+                                int mode, int len, const uint64_t* rbits,
+                                const double* usamp);
+int orc_round_mantissa_f64_bits(const double* in, double* out, int64_t n, int mbits,
+                                int mode, int len, const uint64_t* rbits,
+                                const double* usamp);
+int orc_round_mantissa_f16_bits(const uint16_t* in, uint16_t* out, int64_t n, int mbits,
+                                int mode, int len, const uint64_t* rbits,
+                                const double* usamp);
+
+/* MX block rounding. scale_formula 0 = GPU form amax*(1/pmn)
+ * (src/mx_round.cuh:59), 1 = CPU form amax/pmn (src/LoPy_bind.cpp:208). */
+int orc_mx_round_f32(const float* in, float* out, int64_t n, int block,
+                     const lofgb_format* ef, const lofgb_format* sf, int mode,
+                     int scale_mode, int len, uint64_t seed, uint64_t offset,
+                     int scale_formula, int nthreads);
+
+/* Emulated-accumulation GEMM, sequential k, device round-to-odd FMA.
+ * Same layout arguments as lofgb_gemm_f32. */
+int orc_gemm_f32(const float* A, int64_t lda, int trans_a, const float* B, int64_t ldb,
+                 int trans_b, float* D, int64_t ldd, int M, int N, int K, int mbits,
+                 float alpha, int nthreads);
+/* Only rows [row0, row0+rows) of D are computed (bounded CPU samples). */
+int orc_gemm_f32_rows(const float* A, int64_t lda, int trans_a, const float* B,
+                      int64_t ldb, int trans_b, float* D, int64_t ldd, int M, int N,
+                      int K, int mbits, float alpha, int row0, int rows, int nthreads);
+/* The device leaf's round-to-odd FMA (src/cutlass_gemms.cuh:73-88). */
+float orc_rto_fma(float a, float b, float c);
+/* Chunked accumulation model of the tensor-core form with exact chunk sums:
+ * acc = RNE_m(rto(acc + RN_fp32(sum of chunk products in FP64))). Used only to
+ * sanity-check the error statistics on the CPU. */
+int orc_gemm_chunked_f32(const float* A, int64_t lda, int trans_a, const float* B,
+                         int64_t ldb, int trans_b, float* D, int64_t ldd, int M, int N,
+                         int K, int mbits, int chunk, float alpha, int nthreads);
+
+int orc_validate_format(const lofgb_format* f, int src_mant_bits);
+int orc_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,193 @@
+"""ctypes front-end of the CPU oracle — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import
+this module. It loads ``oracle/_build/liblof_oracle.so`` (built by
+``oracle/build_oracle.py``) and, when present, the reference shim
+``oracle/_ref/libref_shim.so``. Arrays are numpy; f16 data travels as uint16
+bit patterns.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle as _bo
+
+_lib = None
+_ref = None
+
+
+class Format(C.Structure):
+    """Same layout as ``lofgb_format`` in include/lofgb.h."""
+    _fields_ = [("bitwidth", C.c_int32), ("mantissa_bits", C.c_int32), ("bias", C.c_int32),
+                ("inf_behavior", C.c_uint8), ("nan_behavior", C.c_uint8),
+                ("signedness", C.c_uint8), ("reserved", C.c_uint8)]
+
+
+def fmt(bitwidth, mantissa_bits, bias, saturating=True, signed=True, nan_754=False) -> Format:
+    return Format(bitwidth, mantissa_bits, bias, 1 if saturating else 0, 1 if nan_754 else 0,
+                  0 if signed else 1, 0)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _bo.build_oracle()
+        L = C.CDLL(path)
+        vp, i64, i32, u64, f32, f64 = C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_float, C.c_double
+        P = C.POINTER(Format)
+        L.orc_rng.restype = u64
+        L.orc_rng.argtypes = [u64, u64]
+        for name, sc in (("orc_round_f32", f32), ("orc_round_f64", f64), ("orc_round_f16", f32)):
+            getattr(L, name).argtypes = [vp, vp, i64, P, i32, i32, sc, u64, u64, i32]
+        for name, sc in (("orc_round_mantissa_f32", f32), ("orc_round_mantissa_f64", f64),
+                         ("orc_round_mantissa_f16", f32)):
+            getattr(L, name).argtypes = [vp, vp, i64, i32, i32, i32, sc, u64, u64, i32]
+        for name in ("orc_round_f32_bits", "orc_round_f64_bits", "orc_round_f16_bits"):
+            getattr(L, name).argtypes = [vp, vp, i64, P, i32, i32, vp, vp]
+        for name in ("orc_round_mantissa_f32_bits", "orc_round_mantissa_f64_bits",
+                     "orc_round_mantissa_f16_bits"):
+            getattr(L, name).argtypes = [vp, vp, i64, i32, i32, i32, vp, vp]
+        L.orc_mx_round_f32.argtypes = [vp, vp, i64, i32, P, P, i32, i32, i32, u64, u64, i32, i32]
+        L.orc_gemm_f32.argtypes = [vp, i64, i32, vp, i64, i32, vp, i64, i32, i32, i32, i32, f32, i32]
+        L.orc_gemm_f32_rows.argtypes = [vp, i64, i32, vp, i64, i32, vp, i64, i32, i32, i32, i32,
+                                        f32, i32, i32, i32]
+        L.orc_gemm_chunked_f32.argtypes = [vp, i64, i32, vp, i64, i32, vp, i64, i32, i32, i32, i32,
+                                           i32, f32, i32]
+        L.orc_rto_fma.restype = f32
+        L.orc_rto_fma.argtypes = [f32, f32, f32]
+        L.orc_max_threads.restype = i32
+        L.orc_validate_format.argtypes = [P, i32]
+        _lib = L
+    return _lib
+
+
+def ref():
+    """The reference shim, or None when it is not built (no reference checkout)."""
+    global _ref
+    if _ref is None:
+        path = _bo.build_ref() if os.path.exists(_bo.reference_src_dir()) else (
+            _bo.REF_SO if os.path.exists(_bo.REF_SO) else None)
+        if path is None:
+            return None
+        R = C.CDLL(path)
+        vp, i64, i32, f32 = C.c_void_p, C.c_int64, C.c_int, C.c_float
+        for name in ("ref_round_f32", "ref_round_f64"):
+            getattr(R, name).argtypes = [vp, vp, i64, i32, i32, i32, i32, i32, i32, i32, i32, vp, vp, vp]
+        for name in ("ref_round_mantissa_f32", "ref_round_mantissa_f64", "ref_round_mantissa_f16"):
+            getattr(R, name).argtypes = [vp, vp, i64, i32, i32, i32, vp, vp, vp]
+        R.ref_mx_round_f32.argtypes = [vp, vp, i64, i32] + [i32] * 13
+        R.ref_gemm_f32.argtypes = [vp, vp, vp, i32, i32, i32, i32, f32]
+        _ref = R
+    return _ref
+
+
+def _check(st):
+    if st != 0:
+        raise ValueError(f"oracle status {st}")
+
+
+_DT = {np.dtype(np.float32): "f32", np.dtype(np.float64): "f64", np.dtype(np.uint16): "f16"}
+
+
+def rng(seed: int, idx: int) -> int:
+    return lib().orc_rng(seed, idx)
+
+
+def round(x: np.ndarray, f: Format, mode: int, stoch_len: int = 0, scale: float = 1.0,
+          seed: int = 0, offset: int = 0, nthreads: int = 0) -> np.ndarray:
+    x = np.ascontiguousarray(x)
+    out = np.empty_like(x)
+    t = _DT[x.dtype]
+    _check(getattr(lib(), f"orc_round_{t}")(_p(x), _p(out), x.size, C.byref(f), mode, stoch_len,
+                                            scale, seed, offset, nthreads))
+    return out
+
+
+def round_mantissa(x: np.ndarray, mbits: int, mode: int, stoch_len: int = 0, scale: float = 1.0,
+                   seed: int = 0, offset: int = 0, nthreads: int = 0) -> np.ndarray:
+    x = np.ascontiguousarray(x)
+    out = np.empty_like(x)
+    t = _DT[x.dtype]
+    _check(getattr(lib(), f"orc_round_mantissa_{t}")(_p(x), _p(out), x.size, mbits, mode,
+                                                     stoch_len, scale, seed, offset, nthreads))
+    return out
+
+
+def round_bits(x, f: Format | None, mode: int, stoch_len: int, rbits=None, usamp=None,
+               mbits: int | None = None) -> np.ndarray:
+    """Round with explicit per-element random words (golden pinning)."""
+    x = np.ascontiguousarray(x)
+    out = np.empty_like(x)
+    t = _DT[x.dtype]
+    rb = None if rbits is None else np.ascontiguousarray(rbits, dtype=np.uint64)
+    us = None if usamp is None else np.ascontiguousarray(usamp, dtype=np.float64)
+    if f is not None:
+        st = getattr(lib(), f"orc_round_{t}_bits")(_p(x), _p(out), x.size, C.byref(f), mode,
+                                                   stoch_len, _p(rb), _p(us))
+    else:
+        st = getattr(lib(), f"orc_round_mantissa_{t}_bits")(_p(x), _p(out), x.size, mbits, mode,
+                                                            stoch_len, _p(rb), _p(us))
+    _check(st)
+    return out
+
+
+def mx_round(x: np.ndarray, block: int, ef: Format, sf: Format, mode: int = 0,
+             scale_mode: int = 0, stoch_len: int = 0, seed: int = 0, offset: int = 0,
+             scale_formula: int = 0, nthreads: int = 0) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty_like(x)
+    _check(lib().orc_mx_round_f32(_p(x), _p(out), x.size, block, C.byref(ef), C.byref(sf), mode,
+                                  scale_mode, stoch_len, seed, offset, scale_formula, nthreads))
+    return out
+
+
+def _gemm_args(A, B, trans_a, trans_b):
+    A = np.ascontiguousarray(A, dtype=np.float32)
+    B = np.ascontiguousarray(B, dtype=np.float32)
+    M, K = (A.shape[1], A.shape[0]) if trans_a else A.shape
+    Kb, N = (B.shape[1], B.shape[0]) if trans_b else B.shape
+    assert K == Kb, "inner dimensions differ"
+    return A, B, M, N, K
+
+
+def gemm(A, B, mbits: int, alpha: float = 1.0, trans_a: int = 0, trans_b: int = 0,
+         nthreads: int = 0) -> np.ndarray:
+    """Bit-exact sequential-k emulated GEMM (A M×K or K×M when trans_a)."""
+    A, B, M, N, K = _gemm_args(A, B, trans_a, trans_b)
+    D = np.empty((M, N), np.float32)
+    _check(lib().orc_gemm_f32(_p(A), A.shape[1], trans_a, _p(B), B.shape[1], trans_b, _p(D), N,
+                              M, N, K, mbits, alpha, nthreads))
+    return D
+
+
+def gemm_rows(A, B, mbits: int, row0: int, rows: int, alpha: float = 1.0, trans_a: int = 0,
+              trans_b: int = 0, nthreads: int = 0) -> np.ndarray:
+    A, B, M, N, K = _gemm_args(A, B, trans_a, trans_b)
+    D = np.zeros((M, N), np.float32)
+    _check(lib().orc_gemm_f32_rows(_p(A), A.shape[1], trans_a, _p(B), B.shape[1], trans_b,
+                                   _p(D), N, M, N, K, mbits, alpha, row0, rows, nthreads))
+    return D[row0:row0 + rows]
+
+
+def gemm_chunked(A, B, mbits: int, chunk: int, alpha: float = 1.0, trans_a: int = 0,
+                 trans_b: int = 0, nthreads: int = 0) -> np.ndarray:
+    A, B, M, N, K = _gemm_args(A, B, trans_a, trans_b)
+    D = np.empty((M, N), np.float32)
+    _check(lib().orc_gemm_chunked_f32(_p(A), A.shape[1], trans_a, _p(B), B.shape[1], trans_b,
+                                      _p(D), N, M, N, K, mbits, chunk, alpha, nthreads))
+    return D
+
+
+def rto_fma(a: float, b: float, c: float) -> float:
+    return lib().orc_rto_fma(a, b, c)
+
+
+def max_threads() -> int:
+    return lib().orc_max_threads()
