@@ -1,0 +1,415 @@
+"""Benchmark of the LoFloat emulation hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Headline (one step): MX block rounding of an 8192x8192 FP32 matrix (N(0,1)
+with 1% outliers scaled by 2^12, seed 2), blocks of 32 along rows with an E8M0
+scale, to E2M1, E4M3 and E5M2 in turn under RNE — 3 launches, 8 algorithmic
+bytes per element each. `value` is GB/s with inputs resident in HBM (the
+256 MiB input is larger than L2, so no flush is needed between steps);
+`e2e` is the same metric through the public API with host buffers (pinned
+input copied in, each result copied out, every step).
+
+The line also carries the other workloads as secondary numbers: plain
+rounding of 2^24 FP32 to E4M3 (RNE and SR-A), and the 4096^3 emulated GEMM
+(CUDA-core bit-exact form and tensor-core chunked form with its FP64-oracle
+error).
+
+--impl reference times the reference algorithm on the host cores (the C
+oracle, a restatement of the reference's scalar code, with all threads) on a
+bounded sample of the same workload.
+
+With N > 1 (torchrun) every rank runs an independent replica of the workload
+on its own GPU (weak scaling, no data-path collective); timing is the max
+over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MX_ROWS = MX_COLS = 8192
+MX_BLOCK = 32
+MX_BYTES = MX_ROWS * MX_COLS * 8  # per format: 4 B read + 4 B write per element
+ELEM_FORMATS = {"e2m1": (4, 1, 1), "e4m3": (8, 3, 7), "e5m2": (8, 2, 15)}
+C1_N = 1 << 24
+GEMM_N = 4096
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-secondary", action="store_true", help="headline workload only")
+    return ap.parse_args()
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def profile_traffic(name: str):
+    """dram bytes per launch recorded from an ncu capture in profiles/."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(path) as fh:
+            m = re.search(r"dram_bytes_per_launch\s*=\s*([0-9.eE+]+)", fh.read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"lofgb_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                f = [v.strip() for v in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def config2_input(torch, dev):
+    g = torch.Generator().manual_seed(2)
+    x = torch.randn(MX_ROWS * MX_COLS, generator=g, dtype=torch.float32)
+    mask = torch.rand(MX_ROWS * MX_COLS, generator=g) < 0.01
+    x[mask] *= 4096.0
+    return x.reshape(MX_ROWS, MX_COLS)
+
+
+def fmt_desc(lg, bw, m, bias, sat=True, signed=True):
+    return lg.FloatFormatDescriptor(bw, m, bias,
+                                    lg.InfBehavior.Saturating if sat else lg.InfBehavior.Extended,
+                                    lg.NaNBehavior._754,
+                                    lg.Signedness.Signed if signed else lg.Signedness.Unsigned,
+                                    lg.formats.P3109_InfChecker(bw), lg.formats.P3109_NaNChecker(bw))
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the reference algorithm on the host cores
+# ---------------------------------------------------------------------------
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import torch  # noqa: F401  (same environment as our arm)
+
+    from oracle import oracle as O
+    threads = O.max_threads()
+    x = config2_input(torch, None).reshape(-1).numpy()
+    sample = x[: 1 << 24]  # a quarter of the matrix per format per step
+    sf = O.fmt(8, 0, 127, saturating=False, signed=False)
+    efs = [O.fmt(*v) for v in ELEM_FORMATS.values()]
+
+    def step():
+        for ef in efs:
+            O.mx_round(sample, MX_BLOCK, ef, sf, nthreads=threads)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    gbs = args.steps * len(efs) * sample.size * 8 / dt / 1e9
+    line = {"impl": "reference", "metric": "MX block rounding throughput (8 B/elem)", "value": gbs,
+            "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "MX round 8192x8192 f32, block 32, E2M1/E4M3/E5M2 + E8M0, RNE",
+                       "sample": "first 2^24 elements per format per step"},
+            "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
+                             "sample": "MX rounding of 2^24 of the 2^26 config elements, 3 formats"},
+            "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def cpu_baseline_sample():
+    """The oracle on a bounded sample of the headline workload (all threads)."""
+    import torch
+
+    from oracle import oracle as O
+    threads = O.max_threads()
+    x = config2_input(torch, None).reshape(-1).numpy()[: 1 << 22]
+    sf = O.fmt(8, 0, 127, saturating=False, signed=False)
+    efs = [O.fmt(*v) for v in ELEM_FORMATS.values()]
+    O.mx_round(x, MX_BLOCK, efs[1], sf, nthreads=threads)
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        for ef in efs:
+            O.mx_round(x, MX_BLOCK, ef, sf, nthreads=threads)
+        reps += 1
+        if time.perf_counter() - t0 > 10.0:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": reps * len(efs) * x.size * 8 / dt / 1e9, "unit": "GB/s", "cores": threads,
+            "kind": "port",
+            "sample": f"MX rounding of 2^22 of the 2^26 config elements, 3 formats x {reps} reps"}
+
+
+def time_events(torch, fn, reps, stream):
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    for i in range(reps):
+        starts[i].record(stream)
+        fn()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+
+def secondary(torch, lg, dev, peaks):
+    """Plain rounding (config-1 workload) and the 4096^3 emulated GEMMs."""
+    out = {}
+    stream = torch.cuda.current_stream(dev)
+    g = torch.Generator().manual_seed(0)
+    x = (torch.randn(C1_N, generator=g) * torch.exp2(torch.randint(-20, 21, (C1_N,), generator=g).float()))
+    xg = x.to(dev)
+    yg = torch.empty_like(xg)
+    e4m3 = fmt_desc(lg, 8, 3, 7)
+    for name, mode, ln in (("rne", 0, 0), ("sr_a", 3, 8)):
+        fn = lambda: lg.virtual_round(xg, e4m3, round_mode=mode, stoch_len=ln, seed=1, offset=0, out=yg)  # noqa: E731
+        for _ in range(5):
+            fn()
+        ms = time_events(torch, fn, 20, stream)
+        gbs = C1_N * 8 / (statistics.median(ms) * 1e-3) / 1e9
+        out[f"round_2^24_e4m3_{name}_GBs"] = round(gbs, 1)
+        out[f"round_2^24_e4m3_{name}_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)
+    # GEMM 4096^3, MX-E4M3 operands along K, 10-bit accumulator
+    g = torch.Generator().manual_seed(3)
+    A = torch.randn(GEMM_N, GEMM_N, generator=g).to(dev)
+    Bt = torch.randn(GEMM_N, GEMM_N, generator=g).to(dev)
+    e8 = lg.create_e8m0_params()
+    Aq = lg.virtual_mx_round(A, 32, e4m3, e8)
+    Btq = lg.virtual_mx_round(Bt, 32, e4m3, e8)  # rows of B^T = columns of B: blocks along K
+    flops = 2.0 * GEMM_N ** 3
+    D = torch.empty(GEMM_N, GEMM_N, device=dev)
+    fn = lambda: lg.gemm(Aq, Btq, 10, trans_b=True, out=D)  # noqa: E731
+    fn()
+    ms = time_events(torch, fn, 3, stream)
+    plain = flops / (statistics.median(ms) * 1e-3) / 1e12
+    out["gemm_4096_plain_TFLOPs"] = round(plain, 3)
+    out["gemm_4096_plain_ms"] = round(statistics.median(ms), 3)
+    try:
+        Dt = torch.empty_like(D)
+        fn = lambda: lg.gemm(Aq, Btq, 10, trans_b=True, variant="tc", chunk=32, out=Dt)  # noqa: E731
+        fn()
+        ms = time_events(torch, fn, 5, stream)
+        tc = flops / (statistics.median(ms) * 1e-3) / 1e12
+        ref = lg.gemm_f64_reference(Aq, Btq, trans_b=True)
+        den = ref.abs().clamp_min(1e-30)
+        rel_tc = (Dt.double() - ref).abs() / den
+        rel_pl = (D.double() - ref).abs() / den
+        big = ref.abs() > 1e-2 * ref.abs().mean()
+        out.update({
+            "gemm_4096_tc_TFLOPs": round(tc, 2), "gemm_4096_tc_ms": round(statistics.median(ms), 3),
+            "gemm_tc_over_plain": round(tc / plain, 2),
+            "gemm_tc_frac_bf16_peak": round(tc / peaks["bf16_tflops"], 4),
+            "gemm_tc_err_vs_fp64": {"max_rel": float(rel_tc[big].max()), "mean_rel": float(rel_tc[big].mean())},
+            "gemm_plain_err_vs_fp64": {"max_rel": float(rel_pl[big].max()), "mean_rel": float(rel_pl[big].mean())},
+            "gemm_err_note": "relative error over outputs with |ref| > 1% of mean |ref|",
+        })
+    except Exception as e:  # tensor-core form unavailable: report why
+        out["gemm_tc_unavailable"] = str(e)[:200]
+    return out
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    import lofloat_gb300 as lg
+    from lofloat_gb300 import _native
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    peaks, peak_src = measured_peaks()
+    x_host = config2_input(torch, None)
+    x = x_host.to(dev)
+    y = torch.empty_like(x)
+    e8 = lg.create_e8m0_params()
+    efs = [fmt_desc(lg, *v) for v in ELEM_FORMATS.values()]
+    stream = torch.cuda.current_stream(dev)
+    _native.lib()
+
+    launch_ms = []
+
+    def step(record=False):
+        for ef in efs:
+            if record:
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+                lg.virtual_mx_round(x, MX_BLOCK, ef, e8, out=y)
+                e.record(stream)
+                launch_ms.append((s, e))
+            else:
+                lg.virtual_mx_round(x, MX_BLOCK, ef, e8, out=y)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        step(record=True)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    elapsed = t0.elapsed_time(t1) / 1e3
+    per_launch = statistics.mean(s.elapsed_time(e) for s, e in launch_ms) / 1e3
+
+    # end to end through the public API with host buffers
+    xh = x_host.pin_memory()
+    yh = [torch.empty_like(xh).pin_memory() for _ in efs]
+
+    def e2e_step():
+        xd = xh.to(dev, non_blocking=True)
+        for i, ef in enumerate(efs):
+            yd = lg.virtual_mx_round(xd, MX_BLOCK, ef, e8)
+            yh[i].copy_(yd, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_steps = max(3, min(args.steps, 10))
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = e0.elapsed_time(e1) / 1e3
+    clk = clocks.stop()
+
+    if dist:
+        t = torch.tensor([elapsed, e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed, e2e_s = float(t[0]), float(t[1])
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    step_bytes = len(efs) * MX_BYTES
+    value = world * args.steps * step_bytes / elapsed / 1e9
+    achieved = MX_BYTES / per_launch / 1e9
+    traffic = profile_traffic("mx_kernel_8192x8192.md")
+    line = {
+        "metric": "MX block rounding throughput (8 B/elem); secondary: emulated-accum GEMM TFLOP/s",
+        "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": round(elapsed / args.steps * 1e3, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded N(0,1), 1% outliers x2^12)",
+        "config": {"workload": "MX round 8192x8192 f32, block 32 along rows, E8M0 scale, "
+                               "E2M1/E4M3/E5M2 in turn, RNE",
+                   "l2": "input 256 MiB > 129 MB L2; no flush", "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+                     "traffic": traffic, "peak_source": f"{peak_src} hbm_gbs",
+                     "kernel": "mx_kernel<32,RNE,RNE>", "algorithmic_bytes_per_launch": MX_BYTES},
+        "e2e": {"value": round(world * e2e_steps * step_bytes / e2e_s / 1e9, 2), "unit": "GB/s",
+                "h2d_bytes_per_step": MX_ROWS * MX_COLS * 4,
+                "d2h_bytes_per_step": len(efs) * MX_ROWS * MX_COLS * 4,
+                "api": "lofloat_gb300.virtual_mx_round (C ABI lofgb_mx_round_f32)"},
+        "gpu_launches": args.steps * len(efs),
+        "clocks": clk,
+    }
+    if not args.no_secondary:
+        line["secondary"] = secondary(torch, lg, dev, peaks)
+    if world == 1:
+        line["cpu_baseline"] = cpu_baseline_sample()
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

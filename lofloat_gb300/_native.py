@@ -1,0 +1,85 @@
+"""ctypes loader for liblofgb.so (the C ABI declared in include/lofgb.h).
+
+The library is built in-tree by lofloat_gb300/build.py. There is no fallback:
+if the library cannot be built or loaded, every op raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+
+class LofgbFormat(C.Structure):
+    """``lofgb_format`` (include/lofgb.h)."""
+    _fields_ = [("bitwidth", C.c_int32), ("mantissa_bits", C.c_int32), ("bias", C.c_int32),
+                ("inf_behavior", C.c_uint8), ("nan_behavior", C.c_uint8),
+                ("signedness", C.c_uint8), ("reserved", C.c_uint8)]
+
+
+# (name, restype, argtypes) for every entry point of include/lofgb.h
+_vp, _i64, _i32, _u64, _f32, _f64, _sz = (C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_float,
+                                          C.c_double, C.c_size_t)
+_FP = C.POINTER(LofgbFormat)
+SIGNATURES = [
+    ("lofgb_strerror", C.c_char_p, [_i32]),
+    ("lofgb_last_error_detail", C.c_char_p, []),
+    ("lofgb_version", _i32, []),
+    ("lofgb_round_f32", _i32, [_vp, _vp, _i64, _FP, _i32, _i32, _f32, _u64, _u64, _vp]),
+    ("lofgb_round_f64", _i32, [_vp, _vp, _i64, _FP, _i32, _i32, _f64, _u64, _u64, _vp]),
+    ("lofgb_round_f16", _i32, [_vp, _vp, _i64, _FP, _i32, _i32, _f32, _u64, _u64, _vp]),
+    ("lofgb_round_mantissa_f32", _i32, [_vp, _vp, _i64, _i32, _i32, _i32, _f32, _u64, _u64, _vp]),
+    ("lofgb_round_mantissa_f64", _i32, [_vp, _vp, _i64, _i32, _i32, _i32, _f64, _u64, _u64, _vp]),
+    ("lofgb_round_mantissa_f16", _i32, [_vp, _vp, _i64, _i32, _i32, _i32, _f32, _u64, _u64, _vp]),
+    ("lofgb_mx_round_f32", _i32, [_vp, _vp, _i64, _i32, _FP, _FP, _i32, _i32, _i32, _u64, _u64,
+                                  _vp]),
+    ("lofgb_gemm_f32", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32,
+                              _i32, _i32, _f32, _i32, _i32, _vp, _sz, _vp]),
+    ("lofgb_gemm_tc_workspace_size", _sz, [_i32, _i32, _i32]),
+    ("lofgb_gemm_f64_ref", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32,
+                                  _vp]),
+]
+
+
+class LofgbError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        lib_ = _lib
+        msg = lib_.lofgb_strerror(status).decode() if lib_ else str(status)
+        detail = lib_.lofgb_last_error_detail().decode() if lib_ else ""
+        super().__init__(f"{where}: {msg}" + (f" ({detail})" if detail else ""))
+        self.status = status
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Build (if stale) and load liblofgb.so."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            L = C.CDLL(path)
+            for name, res, args in SIGNATURES:
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def check(status: int, where: str) -> None:
+    if status != 0:
+        raise LofgbError(status, where)
+
+
+def exported_symbols() -> list[str]:
+    return [name for name, _, _ in SIGNATURES]

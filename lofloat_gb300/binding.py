@@ -1,0 +1,325 @@
+"""Python surface of the GB300 kernels, mirroring the reference's compiled
+module ``LoFloat.LoFloat`` (src/LoPy_bind.cpp:281-394): the enums,
+``FloatFormatDescriptor``, ``virtual_round`` (mantissa and format overloads),
+``virtual_mx_round`` and ``lof_gemm``. Every op runs through liblofgb.so on
+the tensor's device, on torch's current stream, out of place.
+
+Differences from the reference, all deliberate:
+  * CPU tensors raise (the reference's CUDA build returns an uninitialised
+    tensor for them, src/LoPy_bind.cpp:80-97, 140-154);
+  * non-contiguous inputs are made contiguous first (the reference reads
+    data_ptr() of whatever layout it is given);
+  * stochastic modes draw from a counter-based generator keyed by
+    (seed, offset) — ``set_seed`` plays the role of lo_float::set_seed
+    (src/lo_float.h:58-62) and every stochastic call advances the offset by
+    the number of elements it rounds.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import threading
+
+import numpy as np
+import torch
+
+from . import _native
+from ._native import LofgbFormat, check
+
+
+class Signedness(enum.IntEnum):
+    Signed = 0
+    Unsigned = 1
+
+
+class InfBehavior(enum.IntEnum):
+    Extended = 0
+    Saturating = 1
+
+
+class NaNBehavior(enum.IntEnum):
+    _3109 = 0
+    _754 = 1
+
+
+class RoundingMode(enum.IntEnum):
+    """Integer values follow src/fp_tools.hpp:13-28."""
+    RoundToNearestEven = 0
+    RoundTowardsZero = 1
+    RoundAwayFromZero = 2
+    StochasticRoundingA = 3
+    RoundToNearestOdd = 4
+    RoundDown = 5
+    RoundUp = 6
+    RoundTiesToAway = 7
+    StochasticRoundingB = 8
+    StochasticRoundingC = 9
+    True_StochasticRounding = 10
+    ProbabilisticRounding = 11
+    RoundToOdd = 12
+    RoundTiesTowardsZero = 13
+    StochasticRoundingD = 14
+
+
+STOCHASTIC_MODES = {3, 8, 9, 10, 11, 14}
+
+# expose enum members at module level like pybind's export_values()
+for _e in (Signedness, InfBehavior, RoundingMode, NaNBehavior):
+    for _m in _e:
+        globals().setdefault(_m.name, _m)
+
+
+class FloatFormatDescriptor:
+    """Runtime float format (src/LoPy_bind.cpp:45-68, bound at :315-327).
+
+    The inf/NaN checkers are validated like the reference does (callable, with
+    minNegInf/minPosInf, and qNanBitPattern or sNanBitPattern) and kept for
+    callers that read them; the rounding path does not use them.
+    """
+
+    __slots__ = ("_total_bits", "_mantissa_bits", "_bias", "_inf", "_nan", "_sign",
+                 "_is_inf", "_is_nan", "_c")
+
+    def __init__(self, total_bits, mantissa_bits, bias, inf_behavior, nan_behavior, signedness,
+                 is_inf_checker, is_nan_checker):
+        if not callable(is_inf_checker):
+            raise ValueError("inf_checker must be callable")
+        if not hasattr(is_inf_checker, "minNegInf"):
+            raise ValueError("inf_checker must have minNegInf()")
+        if not hasattr(is_inf_checker, "minPosInf"):
+            raise ValueError("inf_checker must have minPosInf()")
+        if not callable(is_nan_checker):
+            raise ValueError("nan_checker must be callable")
+        if not (hasattr(is_nan_checker, "qNanBitPattern") or hasattr(is_nan_checker, "sNanBitPattern")):
+            raise ValueError("nan_checker must have qNanBitPattern() or sNanBitPattern()")
+        self._total_bits = int(total_bits)
+        self._mantissa_bits = int(mantissa_bits)
+        self._bias = int(bias)
+        self._inf = InfBehavior(int(inf_behavior))
+        self._nan = NaNBehavior(int(nan_behavior))
+        self._sign = Signedness(int(signedness))
+        self._is_inf = is_inf_checker
+        self._is_nan = is_nan_checker
+        self._c = LofgbFormat(self._total_bits, self._mantissa_bits, self._bias, int(self._inf),
+                              int(self._nan), int(self._sign), 0)
+
+    total_bits = property(lambda s: s._total_bits)
+    mantissa_bits = property(lambda s: s._mantissa_bits)
+    bias = property(lambda s: s._bias)
+    inf_behavior = property(lambda s: s._inf)
+    nan_behavior = property(lambda s: s._nan)
+    signedness = property(lambda s: s._sign)
+    is_inf_checker = property(lambda s: s._is_inf)
+    is_nan_checker = property(lambda s: s._is_nan)
+
+    @property
+    def c_format(self) -> LofgbFormat:
+        return self._c
+
+    def __repr__(self):
+        return (f"FloatFormatDescriptor(total_bits={self._total_bits}, mantissa_bits="
+                f"{self._mantissa_bits}, bias={self._bias}, {self._inf.name}, {self._sign.name})")
+
+
+# ---- stochastic-rounding generator state -----------------------------------
+_rng_lock = threading.Lock()
+_rng_state = {"seed": 12345, "offset": 0}
+
+
+def set_seed(seed: int) -> None:
+    """Seed the counter-based generator used by the stochastic modes."""
+    with _rng_lock:
+        _rng_state["seed"] = int(seed) & ((1 << 64) - 1)
+        _rng_state["offset"] = 0
+
+
+def get_rng_state() -> tuple[int, int]:
+    with _rng_lock:
+        return _rng_state["seed"], _rng_state["offset"]
+
+
+def set_rng_state(seed: int, offset: int) -> None:
+    with _rng_lock:
+        _rng_state["seed"] = int(seed) & ((1 << 64) - 1)
+        _rng_state["offset"] = int(offset)
+
+
+def _take_counters(mode: int, n: int) -> tuple[int, int]:
+    with _rng_lock:
+        seed, off = _rng_state["seed"], _rng_state["offset"]
+        if int(mode) in STOCHASTIC_MODES:
+            _rng_state["offset"] = off + int(n)
+        return seed, off
+
+
+def _stream(t: torch.Tensor):
+    return C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+
+
+def _require_cuda(t: torch.Tensor, what: str) -> None:
+    if not t.is_cuda:
+        raise RuntimeError(f"{what}: liblofgb runs on CUDA tensors only (got {t.device})")
+
+
+_ROUND_FNS = {torch.float32: ("lofgb_round_f32", "lofgb_round_mantissa_f32"),
+              torch.float64: ("lofgb_round_f64", "lofgb_round_mantissa_f64"),
+              torch.float16: ("lofgb_round_f16", "lofgb_round_mantissa_f16")}
+
+
+def virtual_round(input: torch.Tensor, params, round_mode=RoundingMode.RoundToNearestEven,
+                  stoch_len: int = 0, scale: float = 1.0, *, out: torch.Tensor | None = None,
+                  seed: int | None = None, offset: int | None = None) -> torch.Tensor:
+    """round(scale * input) to `params` (a FloatFormatDescriptor) or to an
+    int number of mantissa bits — the two overloads of
+    src/LoPy_bind.cpp:329-339. Returns a new tensor (or fills `out`)."""
+    _require_cuda(input, "virtual_round")
+    if input.dtype not in _ROUND_FNS:
+        raise RuntimeError(f"virtual_round: unsupported dtype {input.dtype} "
+                           "(float16, float32, float64)")
+    x = input.contiguous()
+    y = torch.empty_like(x) if out is None else out
+    if y.shape != x.shape or y.dtype != x.dtype or not y.is_contiguous() or y.device != x.device:
+        raise RuntimeError("virtual_round: out must be a contiguous tensor like input")
+    n = x.numel()
+    mode = int(round_mode)
+    if seed is None:
+        s, o = _take_counters(mode, n)
+    else:
+        s, o = int(seed), int(offset or 0)
+    L = _native.lib()
+    with torch.cuda.device(x.device):
+        st = _stream(x)
+        if isinstance(params, FloatFormatDescriptor):
+            fn = getattr(L, _ROUND_FNS[x.dtype][0])
+            check(fn(x.data_ptr(), y.data_ptr(), n, C.byref(params.c_format), mode, int(stoch_len),
+                     float(scale), s, o, st), "virtual_round")
+        elif isinstance(params, (int, np.integer)) and not isinstance(params, bool):
+            fn = getattr(L, _ROUND_FNS[x.dtype][1])
+            check(fn(x.data_ptr(), y.data_ptr(), n, int(params), mode, int(stoch_len), float(scale),
+                     s, o, st), "virtual_round")
+        else:
+            raise TypeError("virtual_round: params must be a FloatFormatDescriptor or an int "
+                            "number of mantissa bits")
+    return y
+
+
+def virtual_mx_round(input: torch.Tensor, block_size: int, element_format: FloatFormatDescriptor,
+                     scale_format: FloatFormatDescriptor,
+                     round_mode=RoundingMode.RoundToNearestEven,
+                     scale_round_mode=RoundingMode.RoundToNearestEven, stoch_len: int = 0, *,
+                     out: torch.Tensor | None = None, seed: int | None = None,
+                     offset: int | None = None) -> torch.Tensor:
+    """MX block fake-quantisation (src/LoPy_bind.cpp:165-217): contiguous blocks
+    of `block_size`, one shared scale per block in `scale_format`, elements
+    rounded into `element_format` and rescaled. float32 only."""
+    if input.dtype != torch.float32:
+        raise RuntimeError("virtual_mx_round: float32 tensors only")
+    if int(block_size) <= 0:
+        raise RuntimeError("virtual_mx_round: block_size must be positive")
+    _require_cuda(input, "virtual_mx_round")
+    x = input.contiguous()
+    y = torch.empty_like(x) if out is None else out
+    if y.shape != x.shape or y.dtype != x.dtype or not y.is_contiguous() or y.device != x.device:
+        raise RuntimeError("virtual_mx_round: out must be a contiguous float32 tensor like input")
+    n = x.numel()
+    mode = int(round_mode)
+    if seed is None:
+        s, o = _take_counters(mode, n)
+    else:
+        s, o = int(seed), int(offset or 0)
+    with torch.cuda.device(x.device):
+        check(_native.lib().lofgb_mx_round_f32(
+            x.data_ptr(), y.data_ptr(), n, int(block_size), C.byref(element_format.c_format),
+            C.byref(scale_format.c_format), mode, int(scale_round_mode), int(stoch_len), s, o,
+            _stream(x)), "virtual_mx_round")
+    return y.view_as(input)
+
+
+def gemm_alpha(scale_a: float, scale_b: float) -> float:
+    """alpha = 1/(scale_a*scale_b) in float32, 1 when the product is 0
+    (src/cutlass_gemms.cuh:1784-1786, scales narrowed to float at
+    src/Lof_kernel.cu:140-141)."""
+    sa, sb = np.float32(scale_a), np.float32(scale_b)
+    denom = np.float32(sa * sb)
+    return 1.0 if denom == 0 else float(np.float32(1.0) / denom)
+
+
+_ws_cache: dict = {}
+
+
+def _tc_workspace(device: torch.device, M: int, N: int, K: int) -> torch.Tensor:
+    need = int(_native.lib().lofgb_gemm_tc_workspace_size(M, N, K))
+    key = device
+    buf = _ws_cache.get(key)
+    if buf is None or buf.numel() < need:
+        buf = torch.empty(max(need, 256), dtype=torch.uint8, device=device)
+        _ws_cache[key] = buf
+    return buf
+
+
+def gemm(A: torch.Tensor, B: torch.Tensor, accum_mant_bits: int, *, trans_a: bool = False,
+         trans_b: bool = False, alpha: float = 1.0, variant: str = "plain", chunk: int = 32,
+         out: torch.Tensor | None = None) -> torch.Tensor:
+    """Emulated-accumulation GEMM with explicit layouts.
+
+    A is (M, K), or (K, M) when trans_a; B is (K, N), or (N, K) when trans_b;
+    both contiguous float32 CUDA tensors. variant "plain" is bit-exact to the
+    reference leaf; "tc" is the tcgen05 chunked form."""
+    for t, nm in ((A, "A"), (B, "B")):
+        if t.dim() != 2:
+            raise RuntimeError(f"lof_gemm: {nm} must be 2-D")
+        if t.dtype != torch.float32:
+            raise RuntimeError("lof_gemm: only float32 inputs are supported")
+        _require_cuda(t, "lof_gemm")
+    A = A.contiguous()
+    B = B.contiguous()
+    M, K = (A.shape[1], A.shape[0]) if trans_a else (A.shape[0], A.shape[1])
+    Kb, N = (B.shape[1], B.shape[0]) if trans_b else (B.shape[0], B.shape[1])
+    if K != Kb:
+        raise RuntimeError(f"LoF_gemm: A.cols ({K}) != B.rows ({Kb})")
+    D = torch.empty((M, N), dtype=torch.float32, device=A.device) if out is None else out
+    if D.shape != (M, N) or not D.is_contiguous() or D.dtype != torch.float32:
+        raise RuntimeError("lof_gemm: out must be a contiguous float32 (M, N) tensor")
+    v = {"plain": 0, "tc": 1}[variant]
+    L = _native.lib()
+    with torch.cuda.device(A.device):
+        ws, wsb = None, 0
+        if v == 1:
+            buf = _tc_workspace(A.device, M, N, K)
+            ws, wsb = buf.data_ptr(), buf.numel()
+        check(L.lofgb_gemm_f32(A.data_ptr(), A.shape[1], int(trans_a), B.data_ptr(), B.shape[1],
+                               int(trans_b), D.data_ptr(), N, M, N, K, int(accum_mant_bits),
+                               int(RoundingMode.RoundToNearestEven), float(alpha), v, int(chunk),
+                               ws, wsb, _stream(A)), "lof_gemm")
+    return D
+
+
+def lof_gemm(A: torch.Tensor, B: torch.Tensor, accum_mant_bits: int,
+             round_mode=RoundingMode.RoundToNearestEven, stochastic_rounding_bits: int = 0,
+             scale_a: float = 1.0, scale_b: float = 1.0) -> torch.Tensor:
+    """Drop-in for the reference's lof_gemm (src/Lof_kernel.cu:96-154): D = (A @ B)
+    / (scale_a*scale_b) with the accumulator re-rounded to `accum_mant_bits`
+    after every multiply-add, bit-exact. Like the reference leaf, the
+    accumulator always rounds to nearest even; `round_mode` and
+    `stochastic_rounding_bits` are accepted and ignored
+    (src/cutlass_gemms.cuh:122)."""
+    del round_mode, stochastic_rounding_bits
+    if A.dim() != 2 or B.dim() != 2:
+        raise RuntimeError("LoF_gemm: A and B must be 2-D")
+    return gemm(A, B, accum_mant_bits, alpha=gemm_alpha(scale_a, scale_b))
+
+
+def gemm_f64_reference(A: torch.Tensor, B: torch.Tensor, *, trans_a: bool = False,
+                       trans_b: bool = False) -> torch.Tensor:
+    """FP64 GEMM of the FP32 operands on the GPU (the oracle for the tensor-core
+    form's error statistics)."""
+    A = A.contiguous()
+    B = B.contiguous()
+    M, K = (A.shape[1], A.shape[0]) if trans_a else (A.shape[0], A.shape[1])
+    N = B.shape[0] if trans_b else B.shape[1]
+    D = torch.empty((M, N), dtype=torch.float64, device=A.device)
+    with torch.cuda.device(A.device):
+        check(_native.lib().lofgb_gemm_f64_ref(A.data_ptr(), A.shape[1], int(trans_a), B.data_ptr(),
+                                               B.shape[1], int(trans_b), D.data_ptr(), N, M, N, K,
+                                               _stream(A)), "gemm_f64_reference")
+    return D

@@ -1,0 +1,201 @@
+// gemm_plain.cu — bit-exact emulated-accumulation GEMM on the CUDA cores, and
+// the FP64 oracle GEMM used to state the tensor-core form's error.
+//
+// Replaces the forked-CUTLASS SIMT GEMM (src/cutlass_gemms.cuh:1629-1896,
+// launched from src/Lof_kernel.cu:96-154). Semantics of the leaf
+// thread::Mma<OpLoFMultiplyAdd> (src/cutlass_gemms.cuh:118-167):
+//   acc_0 = +0;  acc_{k+1} = RNE_m(rto_fma(A[i,k], B[k,j], acc_k)), k = 0..K-1
+//   D[i,j] = alpha * acc_K
+// with rto_fma the round-to-odd FMA of src/cutlass_gemms.cuh:73-88
+// (rd = fma.rm, ru = fma.rp, rz = rd >= 0 ? rd : ru, sticky = rd != ru).
+// Every output keeps that exact k order, so any M/N tiling is bit-exact;
+// K is never split.
+//
+// Tiling: 128x128 CTA tile, 256 threads, 8x8 outputs per thread, k-tiles of
+// 16 staged through double-buffered shared memory (k-major for both
+// operands). Loads are scalar and bounds-checked, so every layout / leading
+// dimension / tail works; the kernel is bound by ~10 integer+FP instructions
+// per emulated MAC, not by memory.
+#include <cuda_runtime.h>
+
+#include "lof_round.cuh"
+
+namespace lofgb {
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 16, NT = 256;
+constexpr int PAD = 4;
+
+// One emulated MAC. The round-to-odd word v = rz | sticky: when the two
+// directed FMAs differ they are adjacent, so (rd | ru) & 1 is 1 exactly when
+// the sum was inexact or rz is already odd — the same word as rz | (rd != ru).
+// The RNE step works on the signed word: for finite values (and the GPU's
+// positive canonical NaN) adding < 2^ro never carries into the sign bit.
+template <bool ROUND>
+__device__ __forceinline__ float emac(float a, float b, float acc, int ro, uint32_t half_m1,
+                                      uint32_t mask) {
+    const float rd = __fmaf_rd(a, b, acc);
+    const float ru = __fmaf_ru(a, b, acc);
+    const uint32_t rz = __float_as_uint(rd >= 0.0f ? rd : ru);
+    const uint32_t v = rz | ((__float_as_uint(rd) | __float_as_uint(ru)) & 1u);
+    if (!ROUND) return __uint_as_float(v);
+    const uint32_t t = v + ((v >> ro) & 1u) + half_m1;
+    return __uint_as_float(t & mask);
+}
+
+template <bool ROUND>
+__global__ void __launch_bounds__(NT)
+gemm_plain_kernel(const float* __restrict__ A, int64_t lda, int ta, const float* __restrict__ B,
+                  int64_t ldb, int tb, float* __restrict__ D, int64_t ldd, int M, int N, int K,
+                  int ro, float alpha) {
+    __shared__ __align__(16) float As[2][BK][BM + PAD];
+    __shared__ __align__(16) float Bs[2][BK][BN + PAD];
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const uint32_t half_m1 = ROUND ? (1u << (ro - 1)) - 1u : 0u;
+    const uint32_t mask = ROUND ? ~((1u << ro) - 1u) : ~0u;
+
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+
+    float ra[8], rb[8];
+    auto gload = [&](int k0) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int idx = tid + q * NT;
+            int m, k;
+            if (ta) { k = idx / BM; m = idx % BM; } else { m = idx / BK; k = idx % BK; }
+            const int gm = m0 + m, gk = k0 + k;
+            ra[q] = (gm < M && gk < K) ? (ta ? A[(int64_t)gk * lda + gm] : A[(int64_t)gm * lda + gk]) : 0.0f;
+            int n, kb;
+            if (tb) { n = idx / BK; kb = idx % BK; } else { kb = idx / BN; n = idx % BN; }
+            const int gn = n0 + n, gkb = k0 + kb;
+            rb[q] = (gn < N && gkb < K) ? (tb ? B[(int64_t)gn * ldb + gkb] : B[(int64_t)gkb * ldb + gn]) : 0.0f;
+        }
+    };
+    auto sstore = [&](int buf) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int idx = tid + q * NT;
+            int m, k;
+            if (ta) { k = idx / BM; m = idx % BM; } else { m = idx / BK; k = idx % BK; }
+            As[buf][k][m] = ra[q];
+            int n, kb;
+            if (tb) { n = idx / BK; kb = idx % BK; } else { kb = idx / BN; n = idx % BN; }
+            Bs[buf][kb][n] = rb[q];
+        }
+    };
+
+    const int ktiles = (K + BK - 1) / BK;
+    gload(0);
+    sstore(0);
+    __syncthreads();
+    for (int kt = 0; kt < ktiles; ++kt) {
+        const int buf = kt & 1;
+        if (kt + 1 < ktiles) gload((kt + 1) * BK);
+        const int kmax = min(BK, K - kt * BK);
+        auto step = [&](int kk) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][64 + ty * 4]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][kk][64 + tx * 4]);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    acc[i][j] = emac<ROUND>(av[i], bv[j], acc[i][j], ro, half_m1, mask);
+        };
+        if (kmax == BK) {
+#pragma unroll
+            for (int kk = 0; kk < BK; ++kk) step(kk);
+        } else {
+            for (int kk = 0; kk < kmax; ++kk) step(kk);
+        }
+        if (kt + 1 < ktiles) {
+            sstore(buf ^ 1);
+        }
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int gm = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+        if (gm >= M) continue;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int gn = n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
+            if (gn < N) D[(int64_t)gm * ldd + gn] = __fmul_rn(alpha, acc[i][j]);
+        }
+    }
+}
+
+// FP64 oracle: D = sum_k (double)A[i,k] * (double)B[k,j], 64x64 tiles,
+// 256 threads, 4x4 outputs per thread.
+__global__ void __launch_bounds__(256)
+gemm_f64_kernel(const float* __restrict__ A, int64_t lda, int ta, const float* __restrict__ B,
+                int64_t ldb, int tb, double* __restrict__ D, int64_t ldd, int M, int N, int K) {
+    __shared__ double As[16][64 + 1];
+    __shared__ double Bs[16][64 + 1];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int m0 = blockIdx.y * 64, n0 = blockIdx.x * 64;
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < K; k0 += 16) {
+        for (int idx = tid; idx < 64 * 16; idx += 256) {
+            const int m = idx % 64, k = idx / 64;
+            const int gm = m0 + m, gk = k0 + k;
+            As[k][m] = (gm < M && gk < K) ? (double)(ta ? A[(int64_t)gk * lda + gm] : A[(int64_t)gm * lda + gk]) : 0.0;
+            const int n = idx % 64;
+            const int gn = n0 + n;
+            Bs[k][n] = (gn < N && gk < K) ? (double)(tb ? B[(int64_t)gn * ldb + gk] : B[(int64_t)gk * ldb + gn]) : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(As[k][ty * 4 + i], Bs[k][tx * 4 + j], acc[i][j]);
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
+            if (gm < M && gn < N) D[(int64_t)gm * ldd + gn] = acc[i][j];
+        }
+}
+
+}  // namespace
+
+int launch_gemm_plain(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
+                      float* D, int64_t ldd, int M, int N, int K, int mbits, float alpha,
+                      void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+    if (grid.y > 65535) return set_error(LOFGB_ERR_SIZE, "M too large for the plain GEMM grid");
+    const int ro = 23 - mbits;
+    if (ro > 0)
+        gemm_plain_kernel<true><<<grid, NT, 0, st>>>(A, lda, ta, B, ldb, tb, D, ldd, M, N, K, ro, alpha);
+    else
+        gemm_plain_kernel<false><<<grid, NT, 0, st>>>(A, lda, ta, B, ldb, tb, D, ldd, M, N, K, ro, alpha);
+    return check_launch("gemm_plain_kernel");
+}
+
+int launch_gemm_f64(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
+                    double* D, int64_t ldd, int M, int N, int K, void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    dim3 grid((N + 63) / 64, (M + 63) / 64);
+    if (grid.y > 65535) return set_error(LOFGB_ERR_SIZE, "M too large for the FP64 GEMM grid");
+    gemm_f64_kernel<<<grid, 256, 0, st>>>(A, lda, ta, B, ldb, tb, D, ldd, M, N, K);
+    return check_launch("gemm_f64_kernel");
+}
+
+}  // namespace lofgb

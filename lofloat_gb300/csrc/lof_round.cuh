@@ -1,0 +1,228 @@
+// lof_round.cuh — device rounding core shared by every kernel in liblofgb.
+//
+// Bit-level semantics follow the reference's scalar functions
+// (SudhanvaKulkarni123/LoFloat):
+//   RoundMantissa and helpers         src/lo_float.h:570-1272
+//   virtual_round(x, ToMantissaBits)  src/lo_float.h:2715-2756
+//   virtual_round(x, params, ps)      src/lo_float.h:2843-2939
+// The host precomputes a RoundPlan per (source type, format, mode) so the
+// device path is integer-only: every float comparison of the reference
+// (|x| < tiny, |x| vs tiny/2, |x| > 0 after narrowing to float) becomes a
+// comparison of the magnitude's bit pattern against a precomputed threshold,
+// exact because non-negative IEEE bit patterns order like their values.
+//
+// Defined behaviour where the reference's is undefined (shared with the
+// oracle): roundoff 0 leaves every mode unchanged; a random addend wider than
+// the dropped bits is shifted right instead of left by a negative count; SR-C
+// on 64-bit words uses 64-bit arithmetic; a subnormal-branch shift wider than
+// the word is clamped to width-1 (reachable only when the result is ±0).
+#pragma once
+#include <cuda_fp16.h>
+
+#include <cstdint>
+
+#include "lofgb_internal.h"
+
+namespace lofgb {
+
+// ---- counter-based RNG: SplitMix64 (Steele, Lea, Flood 2014) ---------------
+// The idx-th output of a SplitMix64 stream whose state starts at `seed`.
+__device__ __forceinline__ uint64_t rng64(uint64_t seed, uint64_t idx) {
+    uint64_t z = seed + (idx + 1ull) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double usamp_of(uint64_t r) {
+    return (double)(r >> 11) * 0x1.0p-53;
+}
+
+template <typename U>
+__device__ __forceinline__ U shl_s(U v, int s) {
+    constexpr int W = sizeof(U) * 8;
+    if (s >= W || s <= -W) return U(0);
+    return s >= 0 ? U(v << s) : U(v >> (-s));
+}
+
+template <typename U>
+__device__ __forceinline__ U lowmask(int n) {
+    constexpr int W = sizeof(U) * 8;
+    return n >= W ? ~U(0) : U((U(1) << n) - U(1));
+}
+
+// RoundMantissa (src/lo_float.h:1231-1272) on a W-bit magnitude held in U
+// (uint32_t for f32/f16 words, uint64_t for f64). `W` is the source word
+// width; results are truncated to W bits as the reference's Bits type does.
+// MODE < 0 selects the runtime mode `rmode`.
+template <int MODE, int W, typename U>
+__device__ __forceinline__ U round_mantissa(U bits, int ro, int rmode, int len, bool pos,
+                                            uint64_t r) {
+    const int mode = MODE >= 0 ? MODE : rmode;
+    if (ro <= 0) return bits;
+    if (ro > W - 1) ro = W - 1;
+    const U one_ro = U(1) << ro;
+    const U low = one_ro - U(1);
+    const U trunc = bits & ~low;
+    const U tail = bits & low;
+    U res;
+    switch (mode) {
+    case LOFGB_RNE: res = bits + ((bits >> ro) & U(1)) + (one_ro >> 1) - U(1); break;
+    case LOFGB_RNO: res = bits + (((bits >> ro) & U(1)) ^ U(1)) + (one_ro >> 1) - U(1); break;
+    case LOFGB_RTZ: res = trunc; break;
+    case LOFGB_RAFZ: res = trunc + (tail ? one_ro : U(0)); break;
+    case LOFGB_RU: res = trunc + ((pos && tail) ? one_ro : U(0)); break;
+    case LOFGB_RD: res = trunc + ((!pos && tail) ? one_ro : U(0)); break;
+    case LOFGB_RTA: res = trunc + (((bits >> (ro - 1)) & U(1)) << ro); break;
+    case LOFGB_SR_A: {
+        if (len <= 0) { res = bits; break; }
+        res = bits + shl_s<U>(U(r) & lowmask<U>(len), ro - len);
+        break;
+    }
+    case LOFGB_SR_B: {
+        const U add = (U(r) & lowmask<U>(len)) + U(1);
+        res = bits + (tail ? shl_s<U>(add, ro - len) : U(0));
+        break;
+    }
+    case LOFGB_SR_C: {
+        if (len == 0 || tail == 0) { res = bits; break; }
+        const U samp = U(r) & lowmask<U>(len);
+        U add = shl_s<U>((samp >> 1) + (samp & U(1)), ro - len + 1);
+        if (W <= 32) add = U(uint32_t(add));
+        res = bits + add;
+        break;
+    }
+    case LOFGB_SR_D: {
+        if (len <= 0) { res = bits; break; }
+        const U add = (U(r) & lowmask<U>(len)) + (U(r >> len) & U(1));
+        res = bits + shl_s<U>(add, ro - len);
+        break;
+    }
+    case LOFGB_TRUE_SR: {
+        const double prob = (double)tail / (double)one_ro;
+        if (usamp_of(r) < prob) {
+            U rounded = (trunc + one_ro) & lowmask<U>(W);
+            res = rounded < trunc ? trunc : rounded;
+        } else {
+            res = trunc;
+        }
+        break;
+    }
+    case LOFGB_PROB: res = trunc + ((tail ? (U(r) & U(1)) : U(0)) << ro); break;
+    case LOFGB_RTO: res = trunc | (tail ? one_ro : U(0)); break;
+    case LOFGB_RTTZ: res = bits + (one_ro >> 1) - U(1); break;
+    default: res = bits;
+    }
+    return res & lowmask<U>(W);
+}
+
+__device__ __forceinline__ bool mode_is_stochastic(int mode) {
+    return mode == LOFGB_SR_A || mode == LOFGB_SR_B || mode == LOFGB_SR_C ||
+           mode == LOFGB_SR_D || mode == LOFGB_TRUE_SR || mode == LOFGB_PROB;
+}
+
+// Source word traits.
+template <int W> struct Src;
+template <> struct Src<32> {
+    using U = uint32_t;
+    static constexpr int M = 23;
+    static constexpr U SIGN = 0x80000000u, PINF = 0x7F800000u, QNAN = 0x7FC00000u;
+};
+template <> struct Src<64> {
+    using U = uint64_t;
+    static constexpr int M = 52;
+    static constexpr U SIGN = 0x8000000000000000ull, PINF = 0x7FF0000000000000ull,
+                       QNAN = 0x7FF8000000000000ull;
+};
+template <> struct Src<16> {
+    using U = uint32_t;  // 16-bit words held in 32-bit registers
+    static constexpr int M = 10;
+    static constexpr U SIGN = 0x8000u, PINF = 0x7C00u, QNAN = 0x7E00u;
+};
+
+// from_double<From>((double)k * (double)tiny) for the subnormal branch
+// (src/lo_float.h:2921). tiny is a power of two, 0, or (excluded by format
+// validation) inf, so the product is exact in every source type.
+template <int W>
+__device__ __forceinline__ typename Src<W>::U subnormal_value(uint64_t k, const RoundPlan& p);
+template <>
+__device__ __forceinline__ uint32_t subnormal_value<32>(uint64_t k, const RoundPlan& p) {
+    return __float_as_uint(__fmul_rn(__uint2float_rn((uint32_t)k), p.tiny_f));
+}
+template <>
+__device__ __forceinline__ uint64_t subnormal_value<64>(uint64_t k, const RoundPlan& p) {
+    return (uint64_t)__double_as_longlong(__dmul_rn(__ull2double_rn(k), (double)p.tiny_f));
+}
+template <>
+__device__ __forceinline__ uint32_t subnormal_value<16>(uint64_t k, const RoundPlan& p) {
+    const float v = __fmul_rn(__uint2float_rn((uint32_t)k), p.tiny_f);
+    return (uint32_t)__half_as_ushort(__float2half_rn(v));
+}
+
+// virtual_round(x, params, ps), src/lo_float.h:2843-2939, on a source word.
+template <int MODE, int W>
+__device__ __forceinline__ typename Src<W>::U vr_format(typename Src<W>::U x, const RoundPlan& p,
+                                                        uint64_t r) {
+    using S = Src<W>;
+    using U = typename S::U;
+    const U sign = x & S::SIGN;
+    const U mag = x & (S::SIGN - U(1));
+    // :2869 NaN -> quiet NaN, sign dropped
+    if (mag > S::PINF) return S::QNAN;
+    // :2871-2909 magnitude below the smallest subnormal (compared as float)
+    if ((uint64_t)mag < p.tiny_thr) {
+        const int mode = MODE >= 0 ? MODE : p.mode;
+        const bool nz = (uint64_t)mag >= p.pos_thr;
+        bool to_min;
+        switch (mode) {
+        case LOFGB_RTO:
+        case LOFGB_RAFZ: to_min = nz; break;
+        case LOFGB_RU: to_min = (sign == 0) && nz; break;
+        case LOFGB_RD: to_min = (sign != 0) && nz; break;
+        case LOFGB_RNE:
+        case LOFGB_RNO:
+        case LOFGB_RTTZ:
+        case LOFGB_RTA:
+            if ((uint64_t)mag < p.half_lt) to_min = false;
+            else if ((uint64_t)mag >= p.half_gt) to_min = true;
+            else to_min = (mode == LOFGB_RNO || mode == LOFGB_RTA);
+            break;
+        default: to_min = false;  // RTZ and the stochastic modes flush to 0
+        }
+        return (to_min ? U(p.tiny_bits) : U(0)) | sign;
+    }
+    const int expf = (int)(mag >> S::M);
+    // :2910-2923 target-subnormal grid
+    if (expf < p.to_min_field) {
+        int shift = p.d + (p.to_min_field - expf);
+        if (shift > W - 1) shift = W - 1;
+        U sig = (mag & ((U(1) << S::M) - U(1))) | (U(1) << S::M);
+        sig = round_mantissa<MODE, W, U>(sig, shift, p.mode, p.len, sign == 0, r);
+        const uint64_t k = (uint64_t)(sig >> shift);
+        return subnormal_value<W>(k, p) | sign;
+    }
+    // :2925-2933 normal rounding
+    U b = mag;
+    if (p.d > 0) {
+        b = round_mantissa<MODE, W, U>(b, p.d, p.mode, p.len, sign == 0, r);
+        b &= ~((U(1) << p.d) - U(1));
+    }
+    // :2935-2936 overflow: Saturating returns the input, Extended +inf
+    if ((int64_t)(b >> S::M) > (int64_t)p.to_max_field) return p.saturating ? x : S::PINF;
+    return b | sign;
+}
+
+// virtual_round(x, ToMantissaBits, ps), src/lo_float.h:2715-2756.
+template <int MODE, int W>
+__device__ __forceinline__ typename Src<W>::U vr_mantissa(typename Src<W>::U x, int d,
+                                                          int rmode, int len, uint64_t r) {
+    using S = Src<W>;
+    using U = typename S::U;
+    const U sign = x & S::SIGN;
+    U b = x & (S::SIGN - U(1));
+    b = round_mantissa<MODE, W, U>(b, d, rmode, len, sign == 0, r);
+    if (d > 0) b &= ~((U(1) << d) - U(1));
+    return (b | sign) & lowmask<U>(W);
+}
+
+}  // namespace lofgb

@@ -1,0 +1,56 @@
+// lofgb_internal.h — types shared by the host launchers and the kernels of
+// liblofgb.so. Not part of the public C ABI (include/lofgb.h).
+#pragma once
+#include <cstdint>
+
+#include "../../include/lofgb.h"
+
+namespace lofgb {
+
+// Per-(source type, format, mode) constants, computed on the host by
+// make_round_plan() and passed to kernels by value. Thresholds are bit
+// patterns of the source type's magnitude, so that
+//   (float)|x| <  tiny   <=>  mag <  tiny_thr
+//   (float)|x| >  0      <=>  mag >= pos_thr
+//   (float)|x| <  tiny/2 <=>  mag <  half_lt
+//   (float)|x| >  tiny/2 <=>  mag >= half_gt
+// reproduce the reference's float comparisons (src/lo_float.h:2871-2896).
+struct RoundPlan {
+    int32_t mode;          // lofgb_rounding_mode
+    int32_t len;           // stoch_len
+    int32_t d;             // source mantissa bits - target mantissa bits (>= 0)
+    int32_t to_min_field;  // (1 - bias) + source exponent bias
+    int32_t to_max_field;  // ToMax_exp + source exponent bias
+    int32_t saturating;    // Inf_Behaviors::Saturating
+    uint64_t tiny_thr, pos_thr, half_lt, half_gt;
+    uint64_t tiny_bits;    // from_double<From>(tiny) bit pattern
+    float tiny_f;          // To_min_val (a float in the reference)
+    int32_t pad;
+};
+
+// Host side.
+int validate_format(const lofgb_format* f, int src_mant_bits);
+int make_round_plan(RoundPlan* p, const lofgb_format* f, int src_bits, int mode, int len);
+int make_mantissa_plan(RoundPlan* p, int src_bits, int mbits, int mode, int len);
+int sm_count();
+int set_error(int status, const char* fmt, ...);
+int check_launch(const char* what);
+
+// Kernel launchers (one translation unit each).
+int launch_round(int src_bits, bool fmt, const void* in, void* out, int64_t n,
+                 const RoundPlan& p, double scale, uint64_t seed, uint64_t offset,
+                 void* stream);
+int launch_mx(const float* in, float* out, int64_t n, int block, const RoundPlan& pe,
+              const RoundPlan& ps, float pmn, float inv_pmn, uint64_t seed, uint64_t offset,
+              void* stream);
+int launch_gemm_plain(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
+                      float* D, int64_t ldd, int M, int N, int K, int mbits, float alpha,
+                      void* stream);
+int launch_gemm_f64(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
+                    double* D, int64_t ldd, int M, int N, int K, void* stream);
+int launch_gemm_tc(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
+                   float* D, int64_t ldd, int M, int N, int K, int mbits, float alpha,
+                   int chunk, void* workspace, size_t workspace_bytes, void* stream);
+size_t gemm_tc_workspace(int M, int N, int K);
+
+}  // namespace lofgb

