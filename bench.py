@@ -54,6 +54,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-secondary", action="store_true", help="headline workload only")
+    ap.add_argument("--only", default=None,
+                    choices=["mx", "round_rne", "round_sr", "gemm_plain", "gemm_tc"],
+                    help="run one workload's kernel warmup+steps times and exit (for ncu captures)")
+    ap.add_argument("--size", default="full", choices=["full", "small"],
+                    help="with --only: full-size workload or a small case (GEMM 1024^3)")
     return ap.parse_args()
 
 
@@ -402,9 +407,54 @@ def run_ours(args, world, rank, local):
         dist.destroy_process_group()
 
 
+def run_only(args):
+    """One workload, warmup + steps launches, timed with CUDA events; the
+    command ncu captures (python bench.py --only <w> --steps K --warmup W)."""
+    import torch
+
+    import lofloat_gb300 as lg
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    e4m3 = fmt_desc(lg, 8, 3, 7)
+    e8 = lg.create_e8m0_params()
+    if args.only == "mx":
+        x = config2_input(torch, None).to(dev)
+        y = torch.empty_like(x)
+        fn = lambda: lg.virtual_mx_round(x, MX_BLOCK, e4m3, e8, out=y)  # noqa: E731
+        work, unit = MX_BYTES, "GB/s"
+    elif args.only in ("round_rne", "round_sr"):
+        g = torch.Generator().manual_seed(0)
+        n = C1_N * 2  # 2^25 elements: 128 MiB in + 128 MiB out, above L2
+        x = (torch.randn(n, generator=g) * torch.exp2(torch.randint(-20, 21, (n,), generator=g).float())).to(dev)
+        y = torch.empty_like(x)
+        mode, ln = (0, 0) if args.only == "round_rne" else (3, 8)
+        fn = lambda: lg.virtual_round(x, e4m3, round_mode=mode, stoch_len=ln, seed=1, offset=0, out=y)  # noqa: E731
+        work, unit = n * 8, "GB/s"
+    else:
+        n = GEMM_N if args.size == "full" else 1024
+        g = torch.Generator().manual_seed(3)
+        A = lg.virtual_mx_round(torch.randn(n, n, generator=g).to(dev), 32, e4m3, e8)
+        Bt = lg.virtual_mx_round(torch.randn(n, n, generator=g).to(dev), 32, e4m3, e8)
+        D = torch.empty(n, n, device=dev)
+        variant = "plain" if args.only == "gemm_plain" else "tc"
+        fn = lambda: lg.gemm(A, Bt, 10, trans_b=True, variant=variant, chunk=32, out=D)  # noqa: E731
+        work, unit = 2.0 * n ** 3, "TFLOP/s"
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize()
+    ms = time_events(torch, fn, args.steps, stream)
+    med = statistics.median(ms) * 1e-3
+    rate = work / med / (1e12 if unit == "TFLOP/s" else 1e9)
+    print(json.dumps({"only": args.only, "size": args.size, "median_ms": med * 1e3,
+                      "value": rate, "unit": unit, "launches": args.warmup + args.steps}), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
+    if args.only:
+        run_only(args)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:

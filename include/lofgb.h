@@ -174,6 +174,38 @@ int lofgb_gemm_f64_ref(const float* A, int64_t lda, int trans_a, const float* B,
                        int64_t ldb, int trans_b, double* D, int64_t ldd, int M, int N,
                        int K, void* stream);
 
+/* ---- grouped rounding: many tensors, each with its own format, one launch --
+ * Batched form of lofgb_round_f32 (the reference rounds one tensor per call,
+ * src/LoPy_bind.cpp:122-139). Two phases so that the launch can be captured
+ * in a CUDA graph:
+ *   1. lofgb_round_grouped_prepare() validates the tasks on the host and writes
+ *      a task table of lofgb_round_grouped_table_size(ntasks) bytes into the
+ *      caller's HOST buffer `table` (no device work, no allocation);
+ *   2. the caller copies that table to device memory (any 256-byte aligned
+ *      buffer) and calls lofgb_round_grouped_f32() with it as often as it likes
+ *      — one kernel launch, nothing else, so it can be captured.
+ * Each task rounds `n` floats from `in` to `out` exactly as lofgb_round_f32
+ * would with the same arguments. */
+typedef struct lofgb_round_task {
+    const float* in;
+    float* out;
+    int64_t n;
+    lofgb_format fmt;
+    int32_t mode;
+    int32_t stoch_len;
+    float scale;
+    int32_t reserved;
+    uint64_t seed;
+    uint64_t offset;
+} lofgb_round_task;
+
+size_t lofgb_round_grouped_table_size(int ntasks);
+/* Returns LOFGB_OK and stores the number of work items in *num_items. */
+int lofgb_round_grouped_prepare(const lofgb_round_task* tasks, int ntasks, void* table,
+                                size_t table_bytes, int64_t* num_items);
+int lofgb_round_grouped_f32(const void* device_table, int ntasks, int64_t num_items,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,6 +21,7 @@ from .formats import (create_e8m0_params, create_half_params, create_p3109_param
 from .layers import (LinearConfig, LoF_Linear, LoF_Quantize, LoFLinearFunction, STEMXRound,
                      STERound, _fwht, _lof_gemm_2d, _lof_linear, lof_linear)
 from ._custom_ops import get_format, register_format
+from .grouped import GroupedRound
 
 __all__ = [
     "FloatFormatDescriptor", "InfBehavior", "NaNBehavior", "RoundingMode", "Signedness",
@@ -28,5 +29,5 @@ __all__ = [
     "set_seed", "get_rng_state", "set_rng_state", "create_p3109_params", "create_e8m0_params",
     "create_half_params", "create_single_params", "make_format", "STERound", "STEMXRound",
     "LoF_Quantize", "LoF_Linear", "LoFLinearFunction", "LinearConfig", "lof_linear",
-    "register_format", "get_format",
+    "register_format", "get_format", "GroupedRound",
 ]

@@ -22,6 +22,13 @@ class LofgbFormat(C.Structure):
                 ("signedness", C.c_uint8), ("reserved", C.c_uint8)]
 
 
+class LofgbRoundTask(C.Structure):
+    """``lofgb_round_task`` (include/lofgb.h)."""
+    _fields_ = [("in_", C.c_void_p), ("out", C.c_void_p), ("n", C.c_int64), ("fmt", LofgbFormat),
+                ("mode", C.c_int32), ("stoch_len", C.c_int32), ("scale", C.c_float),
+                ("reserved", C.c_int32), ("seed", C.c_uint64), ("offset", C.c_uint64)]
+
+
 # (name, restype, argtypes) for every entry point of include/lofgb.h
 _vp, _i64, _i32, _u64, _f32, _f64, _sz = (C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_float,
                                           C.c_double, C.c_size_t)
@@ -43,6 +50,10 @@ SIGNATURES = [
     ("lofgb_gemm_tc_workspace_size", _sz, [_i32, _i32, _i32]),
     ("lofgb_gemm_f64_ref", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32,
                                   _vp]),
+    ("lofgb_round_grouped_table_size", _sz, [_i32]),
+    ("lofgb_round_grouped_prepare", _i32, [C.POINTER(LofgbRoundTask), _i32, _vp, _sz,
+                                           C.POINTER(C.c_int64)]),
+    ("lofgb_round_grouped_f32", _i32, [_vp, _i32, _i64, _vp]),
 ]
 
 

@@ -249,12 +249,27 @@ _ws_cache: dict = {}
 
 def _tc_workspace(device: torch.device, M: int, N: int, K: int) -> torch.Tensor:
     need = int(_native.lib().lofgb_gemm_tc_workspace_size(M, N, K))
-    key = device
+    # one workspace per (device, stream): calls on one stream are ordered, so
+    # reusing it is race-free; another stream gets its own
+    key = (device, torch.cuda.current_stream(device).cuda_stream)
     buf = _ws_cache.get(key)
     if buf is None or buf.numel() < need:
         buf = torch.empty(max(need, 256), dtype=torch.uint8, device=device)
         _ws_cache[key] = buf
     return buf
+
+
+def tc_device_status(device=None) -> int:
+    """Status word the tensor-core GEMM left in its workspace on `device`
+    (0, or LOFGB_ERR_TIMEOUT if a bounded device-side wait expired). Reads
+    device memory, so it synchronises with the current stream."""
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    buf = _ws_cache.get((dev, torch.cuda.current_stream(dev).cuda_stream))
+    if buf is None:
+        return 0
+    return int(buf[:4].view(torch.int32).item())
 
 
 def gemm(A: torch.Tensor, B: torch.Tensor, accum_mant_bits: int, *, trans_a: bool = False,

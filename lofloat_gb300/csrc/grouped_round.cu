@@ -1,0 +1,167 @@
+// grouped_round.cu — one persistent launch that rounds many FP32 tensors, each
+// with its own format, mode, scale and RNG stream.
+//
+// The host splits every tensor into work items of GROUPED_ITEM elements and
+// writes one GroupedTask row per tensor (with the prefix sum of item counts)
+// into a table the caller uploads once. CTAs walk the item space with a
+// grid-stride loop; each item finds its task by binary search over the
+// prefix sums, then rounds its slice with 16-byte vectors. The mode is
+// uniform per item, so the specialised element loops for RNE, RTZ,
+// round-to-odd and SR-A are chosen once per item; other modes use the
+// runtime-dispatched loop. Results are bit-identical to lofgb_round_f32 on
+// each task.
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "lof_round.cuh"
+
+namespace lofgb {
+
+namespace {
+
+constexpr int GT = 256;
+
+template <int MODE>
+__device__ __forceinline__ uint32_t elem(uint32_t w, const GroupedTask& t, uint64_t idx) {
+    if (t.apply_scale) w = __float_as_uint(__fmul_rn(t.scale, __uint_as_float(w)));
+    const int mode = MODE >= 0 ? MODE : t.plan.mode;
+    const uint64_t r = mode_is_stochastic(mode) ? rng64(t.seed, t.offset + idx) : 0ull;
+    return vr_format<MODE, 32>(w, t.plan, r);
+}
+
+template <int MODE>
+__device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
+    const bool aligned =
+        ((reinterpret_cast<uintptr_t>(t.in) | reinterpret_cast<uintptr_t>(t.out)) & 15) == 0 &&
+        (e0 & 3) == 0;
+    if (aligned) {
+        const int64_t v0 = e0 >> 2, v1 = e1 >> 2;  // full float4s
+        const uint4* vin = reinterpret_cast<const uint4*>(t.in);
+        uint4* vout = reinterpret_cast<uint4*>(t.out);
+        for (int64_t v = v0 + threadIdx.x; v < v1; v += GT) {
+            const uint4 a = __ldcs(vin + v);
+            const uint64_t i = (uint64_t)v * 4;
+            uint4 o;
+            o.x = elem<MODE>(a.x, t, i + 0);
+            o.y = elem<MODE>(a.y, t, i + 1);
+            o.z = elem<MODE>(a.z, t, i + 2);
+            o.w = elem<MODE>(a.w, t, i + 3);
+            __stcs(vout + v, o);
+        }
+        for (int64_t i = (v1 << 2) + threadIdx.x; i < e1; i += GT) {
+            const uint32_t w = reinterpret_cast<const uint32_t*>(t.in)[i];
+            reinterpret_cast<uint32_t*>(t.out)[i] = elem<MODE>(w, t, (uint64_t)i);
+        }
+    } else {
+        for (int64_t i = e0 + threadIdx.x; i < e1; i += GT) {
+            const uint32_t w = reinterpret_cast<const uint32_t*>(t.in)[i];
+            reinterpret_cast<uint32_t*>(t.out)[i] = elem<MODE>(w, t, (uint64_t)i);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(GT)
+grouped_round_kernel(const GroupedTask* __restrict__ tasks, int ntasks, int64_t num_items) {
+    __shared__ GroupedTask st;
+    for (int64_t item = blockIdx.x; item < num_items; item += gridDim.x) {
+        if (threadIdx.x == 0) {
+            int lo = 0, hi = ntasks - 1;  // last task with item_begin <= item
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (tasks[mid].item_begin <= item) lo = mid;
+                else hi = mid - 1;
+            }
+            st = tasks[lo];
+        }
+        __syncthreads();
+        const GroupedTask t = st;
+        __syncthreads();
+        const int64_t e0 = (item - t.item_begin) * GROUPED_ITEM;
+        const int64_t e1 = min(e0 + GROUPED_ITEM, t.n);
+        switch (t.plan.mode) {
+        case LOFGB_RNE: run_item<LOFGB_RNE>(t, e0, e1); break;
+        case LOFGB_RTZ: run_item<LOFGB_RTZ>(t, e0, e1); break;
+        case LOFGB_RTO: run_item<LOFGB_RTO>(t, e0, e1); break;
+        case LOFGB_SR_A: run_item<LOFGB_SR_A>(t, e0, e1); break;
+        default: run_item<-1>(t, e0, e1); break;
+        }
+    }
+}
+
+}  // namespace
+
+int launch_round_grouped(const void* table, int ntasks, int64_t num_items, void* stream) {
+    if (num_items == 0) return LOFGB_OK;
+    const int64_t maxg = (int64_t)sm_count() * (2048 / GT);
+    const int grid = (int)(num_items < maxg ? num_items : maxg);
+    grouped_round_kernel<<<grid, GT, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const GroupedTask*>(table), ntasks, num_items);
+    return check_launch("grouped_round_kernel");
+}
+
+}  // namespace lofgb
+
+using namespace lofgb;
+
+extern "C" {
+
+size_t lofgb_round_grouped_table_size(int ntasks) {
+    return ntasks <= 0 ? 0 : (size_t)ntasks * sizeof(GroupedTask);
+}
+
+int lofgb_round_grouped_prepare(const lofgb_round_task* tasks, int ntasks, void* table,
+                                size_t table_bytes, int64_t* num_items) {
+    if (ntasks < 0) return set_error(LOFGB_ERR_SIZE, "negative task count");
+    if (ntasks > 0 && (!tasks || !table || !num_items))
+        return set_error(LOFGB_ERR_NULL, "NULL tasks, table or num_items");
+    if (table_bytes < lofgb_round_grouped_table_size(ntasks))
+        return set_error(LOFGB_ERR_WORKSPACE, "table needs %zu bytes",
+                         lofgb_round_grouped_table_size(ntasks));
+    GroupedTask* rows = static_cast<GroupedTask*>(table);
+    int64_t items = 0;
+    for (int i = 0; i < ntasks; ++i) {
+        const lofgb_round_task& t = tasks[i];
+        if (t.n < 0) return set_error(LOFGB_ERR_SIZE, "task %d: negative size", i);
+        if (t.n > 0 && (!t.in || !t.out)) return set_error(LOFGB_ERR_NULL, "task %d: NULL data", i);
+        if (t.n > 0) {
+            const char* a = (const char*)t.in;
+            const char* b = (const char*)t.out;
+            if (a != b && a < b + t.n * 4 && b < a + t.n * 4)
+                return set_error(LOFGB_ERR_ALIAS, "task %d: input and output partially overlap", i);
+        }
+        GroupedTask g;
+        memset(&g, 0, sizeof(g));
+        int st = make_round_plan(&g.plan, &t.fmt, 32, t.mode, t.stoch_len);
+        if (st) {
+            char why[256];
+            strncpy(why, lofgb_last_error_detail(), sizeof(why) - 1);
+            why[sizeof(why) - 1] = 0;
+            return set_error(st, "task %d: %s", i, why);
+        }
+        g.in = t.in;
+        g.out = t.out;
+        g.n = t.n;
+        g.item_begin = items;
+        g.scale = t.scale;
+        g.apply_scale = t.scale != 1.0f;
+        g.seed = t.seed;
+        g.offset = t.offset;
+        rows[i] = g;
+        items += (t.n + GROUPED_ITEM - 1) / GROUPED_ITEM;
+    }
+    if (num_items) *num_items = items;
+    return LOFGB_OK;
+}
+
+int lofgb_round_grouped_f32(const void* device_table, int ntasks, int64_t num_items,
+                            void* stream) {
+    if (ntasks < 0 || num_items < 0) return set_error(LOFGB_ERR_SIZE, "negative count");
+    if (num_items > 0 && (!device_table || ntasks == 0))
+        return set_error(LOFGB_ERR_NULL, "NULL device table");
+    if ((reinterpret_cast<uintptr_t>(device_table) & 255) != 0)
+        return set_error(LOFGB_ERR_WORKSPACE, "device table must be 256-byte aligned");
+    return launch_round_grouped(device_table, ntasks, num_items, stream);
+}
+
+}  // extern "C"

@@ -54,3 +54,22 @@ int launch_gemm_tc(const float* A, int64_t lda, int ta, const float* B, int64_t 
 size_t gemm_tc_workspace(int M, int N, int K);
 
 }  // namespace lofgb
+
+namespace lofgb {
+
+// Device-side row of the grouped rounding table (one per tensor).
+struct GroupedTask {
+    const float* in;
+    float* out;
+    int64_t n;
+    int64_t item_begin;  // first work item of this task (exclusive prefix sum)
+    RoundPlan plan;
+    float scale;
+    int32_t apply_scale;
+    uint64_t seed, offset;
+};
+constexpr int64_t GROUPED_ITEM = 1 << 16;  // elements per work item
+
+int launch_round_grouped(const void* table, int ntasks, int64_t num_items, void* stream);
+
+}  // namespace lofgb

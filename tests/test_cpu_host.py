@@ -138,3 +138,27 @@ def test_cpu_tensors_rejected():
         lg.virtual_mx_round(torch.ones(64), 32, lg.create_p3109_params(8, 4), lg.create_e8m0_params())
     with pytest.raises(RuntimeError):
         lg.lof_gemm(torch.ones(4, 4), torch.ones(4, 4), 10)
+
+
+def test_grouped_prepare_host_only():
+    """The grouped table is built on the host: sizes, item counts and
+    per-task validation, no device work."""
+    L = _native.lib()
+    T = _native.LofgbRoundTask
+    ok = fmt()
+    tasks = (T * 3)(T(0x1000, 0x100000, 70000, ok, 0, 0, 1.0, 0, 1, 0),
+                    T(0x200000, 0x300000, 1, ok, 3, 8, 2.0, 0, 2, 5),
+                    T(0x400000, 0x400000, 0, ok, 1, 0, 1.0, 0, 3, 0))
+    nbytes = L.lofgb_round_grouped_table_size(3)
+    assert nbytes > 0 and L.lofgb_round_grouped_table_size(0) == 0
+    buf = (C.c_uint8 * nbytes)()
+    items = C.c_int64(-1)
+    assert L.lofgb_round_grouped_prepare(tasks, 3, buf, nbytes, C.byref(items)) == 0
+    assert items.value == 2 + 1 + 0  # 70000 elements -> 2 items of 2^16, 1 -> 1, 0 -> 0
+    assert L.lofgb_round_grouped_prepare(tasks, 3, buf, nbytes - 1, C.byref(items)) == -9
+    bad = (T * 1)(T(0x1000, 0x1004, 16, ok, 0, 0, 1.0, 0, 0, 0))
+    assert L.lofgb_round_grouped_prepare(bad, 1, buf, nbytes, C.byref(items)) == -6
+    bad = (T * 1)(T(0x1000, 0x100000, 16, fmt(m=30), 0, 0, 1.0, 0, 0, 0))
+    assert L.lofgb_round_grouped_prepare(bad, 1, buf, nbytes, C.byref(items)) == -3
+    assert "task 0" in L.lofgb_last_error_detail().decode()
+    assert L.lofgb_round_grouped_f32(None, 0, 0, None) == 0

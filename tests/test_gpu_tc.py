@@ -1,0 +1,125 @@
+"""The tcgen05 chunked emulated-accumulation GEMM. Not bit-exact by design
+(each k-chunk is summed in FP32 by the tensor cores before it is folded into
+the emulated accumulator); checked against
+
+  * the CPU chunked model with exact chunk sums (same fold, same chunks):
+    results agree to within one accumulator ulp, mostly exactly;
+  * the FP64 oracle GEMM: error of the order of the accumulator's precision;
+  * exactly representable inputs: identical to the bit-exact CUDA-core form.
+"""
+import numpy as np
+import pytest
+import torch
+
+import lofloat_gb300 as lg
+from gpu_util import from_gpu, to_gpu
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _ulp_diff(a, b, mbits):
+    """|a-b| in units of an mbits-mantissa ulp at max(|a|,|b|)."""
+    m = np.maximum(np.abs(a), np.abs(b)).astype(np.float64)
+    e = np.floor(np.log2(np.where(m > 0, m, 1.0)))
+    return np.abs(a.astype(np.float64) - b.astype(np.float64)) / np.exp2(e - mbits)
+
+
+def _status_ok():
+    torch.cuda.synchronize()
+    assert lg.binding.tc_device_status("cuda:0") == 0
+
+
+@pytest.mark.parametrize("shape", [(128, 128, 64), (256, 256, 256), (200, 136, 300), (1, 1, 1),
+                                   (129, 257, 33), (384, 128, 1000)])
+@pytest.mark.parametrize("chunk", [32, 64])
+def test_vs_chunked_model(shape, chunk):
+    M, N, K = shape
+    rng = np.random.default_rng(M + N + K + chunk)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((K, N)).astype(np.float32)
+    got = from_gpu(lg.gemm(to_gpu(A), to_gpu(B), 10, variant="tc", chunk=chunk))
+    _status_ok()
+    want = O.gemm_chunked(A, B, 10, chunk)
+    d = _ulp_diff(got, want, 10)
+    # a chunk sum off by ~2^-17 relative (BF16 hi/lo split, FP32 sums) moves a
+    # 10-bit rounding only rarely; one flipped rounding is one ulp (two when
+    # the value later crosses into a lower binade)
+    assert np.all(d <= 2.0 + 1e-9), d.max()
+    assert np.mean(d > 0) < 0.25
+
+
+@pytest.mark.parametrize("ta", [0, 1])
+@pytest.mark.parametrize("tb", [0, 1])
+def test_layouts(ta, tb):
+    M, N, K = 160, 192, 320
+    rng = np.random.default_rng(ta * 2 + tb)
+    A = rng.standard_normal((K, M) if ta else (M, K)).astype(np.float32)
+    B = rng.standard_normal((N, K) if tb else (K, N)).astype(np.float32)
+    got = from_gpu(lg.gemm(to_gpu(A), to_gpu(B), 12, trans_a=bool(ta), trans_b=bool(tb),
+                           variant="tc", chunk=32))
+    _status_ok()
+    want = O.gemm_chunked(A, B, 12, 32, trans_a=ta, trans_b=tb)
+    assert np.all(_ulp_diff(got, want, 12) <= 2.0 + 1e-9)
+
+
+@pytest.mark.parametrize("chunk", [16, 48, 128, 256])
+@pytest.mark.parametrize("mbits", [7, 23])
+def test_chunks_and_widths(chunk, mbits):
+    M, N, K = 128, 256, 512
+    rng = np.random.default_rng(chunk + mbits)
+    A = rng.uniform(-1, 1, (M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    got = from_gpu(lg.gemm(to_gpu(A), to_gpu(B), mbits, variant="tc", chunk=chunk, alpha=0.5))
+    _status_ok()
+    want = O.gemm_chunked(A, B, mbits, chunk, alpha=0.5)
+    if mbits < 23:
+        assert np.all(_ulp_diff(got, want, mbits) <= 2.0 + 1e-9)
+    else:  # no accumulator rounding: only the FP32 chunk sums differ
+        assert np.allclose(got, want, rtol=1e-4, atol=1e-3)
+
+
+def test_exact_inputs_match_plain():
+    """Small integers: every partial sum is exact, so all accumulation orders
+    agree (the reference's exact-input check, test/test_blis_lof_accum.cpp:200-235)."""
+    rng = np.random.default_rng(0)
+    A = rng.integers(-3, 4, (256, 512)).astype(np.float32)
+    B = rng.integers(-3, 4, (512, 128)).astype(np.float32)
+    tc = lg.gemm(to_gpu(A), to_gpu(B), 23, variant="tc", chunk=32)
+    pl = lg.gemm(to_gpu(A), to_gpu(B), 23)
+    _status_ok()
+    assert torch.equal(tc, pl)
+    assert np.array_equal(from_gpu(tc), (A.astype(np.float64) @ B).astype(np.float32))
+
+
+def test_config3_error_vs_fp64():
+    """M=N=K=4096, MX-E4M3 operands along K, 10-bit accumulator, chunk 32:
+    the error against the FP64 oracle is of the accumulator's order and
+    close to the bit-exact CUDA-core form's."""
+    g = torch.Generator().manual_seed(3)
+    A = torch.randn(4096, 4096, generator=g).cuda()
+    Bt = torch.randn(4096, 4096, generator=g).cuda()
+    e4m3 = lg.create_p3109_params(8, 4)
+    e8 = lg.create_e8m0_params()
+    Aq = lg.virtual_mx_round(A, 32, e4m3, e8)
+    Btq = lg.virtual_mx_round(Bt, 32, e4m3, e8)
+    tc = lg.gemm(Aq, Btq, 10, trans_b=True, variant="tc", chunk=32)
+    pl = lg.gemm(Aq, Btq, 10, trans_b=True)
+    _status_ok()
+    ref = lg.gemm_f64_reference(Aq, Btq, trans_b=True)
+    big = ref.abs() > 1e-2 * ref.abs().mean()
+    rel_tc = ((tc.double() - ref).abs() / ref.abs())[big]
+    rel_pl = ((pl.double() - ref).abs() / ref.abs())[big]
+    assert rel_tc.mean().item() < 2 * rel_pl.mean().item() + 1e-3
+    assert rel_tc.mean().item() < 2e-2
+
+
+def test_workspace_errors():
+    A = torch.randn(64, 64, device="cuda")
+    L = lg._native.lib()
+    need = L.lofgb_gemm_tc_workspace_size(64, 64, 64)
+    assert need > 0
+    D = torch.empty(64, 64, device="cuda")
+    st = L.lofgb_gemm_f32(A.data_ptr(), 64, 0, A.data_ptr(), 64, 0, D.data_ptr(), 64, 64, 64, 64, 10,
+                          0, 1.0, 1, 32, None, 0, None)
+    assert st == -9
