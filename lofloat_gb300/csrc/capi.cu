@@ -134,6 +134,29 @@ int make_round_plan(RoundPlan* p, const lofgb_format* f, int src_bits, int mode,
     if (src_bits == 32) p->tiny_bits = f2u(t);
     else if (src_bits == 64) p->tiny_bits = d2u((double)t);
     else p->tiny_bits = float_to_half_bits(t);
+    // exponent-field thresholds expressed on the magnitude bits
+    const uint64_t wmax = src_bits == 64 ? ~0ull : ((1ull << src_bits) - 1);
+    auto field_thr = [&](int64_t field) -> uint64_t {  // smallest b with (b >> srcM) >= field
+        if (field <= 0) return 0;
+        if (field > (int64_t)(wmax >> srcM)) return wmax;
+        return (uint64_t)field << srcM;
+    };
+    p->keep_mask = ~((1ull << p->d) - 1ull) & wmax;
+    p->norm_thr = field_thr((int64_t)p->to_min_field);
+    p->ovf_thr = field_thr((int64_t)p->to_max_field + 1);
+    // tiny-branch decision per sign (src/lo_float.h:2879-2903)
+    const uint64_t never = ~0ull;
+    switch (mode) {
+    case LOFGB_RNE:
+    case LOFGB_RTTZ: p->tmin_pos = p->tmin_neg = p->half_gt; break;
+    case LOFGB_RNO:
+    case LOFGB_RTA: p->tmin_pos = p->tmin_neg = p->half_lt; break;
+    case LOFGB_RTO:
+    case LOFGB_RAFZ: p->tmin_pos = p->tmin_neg = p->pos_thr; break;
+    case LOFGB_RU: p->tmin_pos = p->pos_thr; p->tmin_neg = never; break;
+    case LOFGB_RD: p->tmin_pos = never; p->tmin_neg = p->pos_thr; break;
+    default: p->tmin_pos = p->tmin_neg = never;  // RTZ and the stochastic modes flush to 0
+    }
     return LOFGB_OK;
 }
 
@@ -147,6 +170,7 @@ int make_mantissa_plan(RoundPlan* p, int src_bits, int mbits, int mode, int len)
     p->mode = mode;
     p->len = len;
     p->d = srcM - mbits;
+    p->keep_mask = ~((1ull << p->d) - 1ull);
     return LOFGB_OK;
 }
 

@@ -13,9 +13,10 @@
 //
 // Tiling: 128x128 CTA tile, 256 threads, 8x8 outputs per thread, k-tiles of
 // 16 staged through double-buffered shared memory (k-major for both
-// operands). Loads are scalar and bounds-checked, so every layout / leading
-// dimension / tail works; the kernel is bound by ~10 integer+FP instructions
-// per emulated MAC, not by memory.
+// operands) by 4-byte cp.async copies, zero-filled out of range, so every
+// layout / leading dimension / tail works. Two CTAs per SM (<= 128 registers);
+// the kernel is bound by ~10 integer+FP instructions per emulated MAC, not by
+// memory.
 #include <cuda_runtime.h>
 
 #include "lof_round.cuh"
@@ -44,8 +45,18 @@ __device__ __forceinline__ float emac(float a, float b, float acc, int ro, uint3
     return __uint_as_float(t & mask);
 }
 
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float* src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src),
+                 "r"(valid ? 4 : 0)
+                 : "memory");
+}
+
 template <bool ROUND>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, 2)
 gemm_plain_kernel(const float* __restrict__ A, int64_t lda, int ta, const float* __restrict__ B,
                   int64_t ldb, int tb, float* __restrict__ D, int64_t ldd, int M, int N, int K,
                   int ro, float alpha) {
@@ -63,43 +74,45 @@ gemm_plain_kernel(const float* __restrict__ A, int64_t lda, int ta, const float*
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
 
-    float ra[8], rb[8];
-    auto gload = [&](int k0) {
+    // Next k-tile: 4-byte cp.async copies straight from global memory into
+    // the k-major shared tiles (no register staging); out-of-range elements
+    // are zero-filled (src-size 0, the source pointer stays in bounds).
+    auto issue = [&](int buf, int k0) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int idx = tid + q * NT;
             int m, k;
             if (ta) { k = idx / BM; m = idx % BM; } else { m = idx / BK; k = idx % BK; }
             const int gm = m0 + m, gk = k0 + k;
-            ra[q] = (gm < M && gk < K) ? (ta ? A[(int64_t)gk * lda + gm] : A[(int64_t)gm * lda + gk]) : 0.0f;
+            const bool va = gm < M && gk < K;
+            const float* src = va ? (ta ? A + (int64_t)gk * lda + gm : A + (int64_t)gm * lda + gk) : A;
+            cp_async4(smem_addr(&As[buf][k][m]), src, va);
             int n, kb;
             if (tb) { n = idx / BK; kb = idx % BK; } else { kb = idx / BN; n = idx % BN; }
             const int gn = n0 + n, gkb = k0 + kb;
-            rb[q] = (gn < N && gkb < K) ? (tb ? B[(int64_t)gn * ldb + gkb] : B[(int64_t)gkb * ldb + gn]) : 0.0f;
+            const bool vb = gn < N && gkb < K;
+            const float* srcb = vb ? (tb ? B + (int64_t)gn * ldb + gkb : B + (int64_t)gkb * ldb + gn) : B;
+            cp_async4(smem_addr(&Bs[buf][kb][n]), srcb, vb);
         }
-    };
-    auto sstore = [&](int buf) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int idx = tid + q * NT;
-            int m, k;
-            if (ta) { k = idx / BM; m = idx % BM; } else { m = idx / BK; k = idx % BK; }
-            As[buf][k][m] = ra[q];
-            int n, kb;
-            if (tb) { n = idx / BK; kb = idx % BK; } else { kb = idx / BN; n = idx % BN; }
-            Bs[buf][kb][n] = rb[q];
-        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
     };
 
     const int ktiles = (K + BK - 1) / BK;
-    gload(0);
-    sstore(0);
-    __syncthreads();
+    issue(0, 0);
     for (int kt = 0; kt < ktiles; ++kt) {
         const int buf = kt & 1;
-        if (kt + 1 < ktiles) gload((kt + 1) * BK);
+        if (kt + 1 < ktiles) {
+            issue(buf ^ 1, (kt + 1) * BK);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
         const int kmax = min(BK, K - kt * BK);
-        auto step = [&](int kk) {
+        // one 8x8 MAC block per k (640 instructions) stays resident in the
+        // instruction cache; unrolling k as well overflows it
+#pragma unroll 1
+        for (int kk = 0; kk < kmax; ++kk) {
             const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
             const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][64 + ty * 4]);
             const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
@@ -111,17 +124,8 @@ gemm_plain_kernel(const float* __restrict__ A, int64_t lda, int ta, const float*
 #pragma unroll
                 for (int j = 0; j < 8; ++j)
                     acc[i][j] = emac<ROUND>(av[i], bv[j], acc[i][j], ro, half_m1, mask);
-        };
-        if (kmax == BK) {
-#pragma unroll
-            for (int kk = 0; kk < BK; ++kk) step(kk);
-        } else {
-            for (int kk = 0; kk < kmax; ++kk) step(kk);
         }
-        if (kt + 1 < ktiles) {
-            sstore(buf ^ 1);
-        }
-        __syncthreads();
+        __syncthreads();  // buffer `buf` is refilled by the next iteration's issue()
     }
 
 #pragma unroll

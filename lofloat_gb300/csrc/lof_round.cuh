@@ -20,6 +20,7 @@
 #include <cuda_fp16.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "lofgb_internal.h"
 
@@ -159,57 +160,53 @@ __device__ __forceinline__ uint32_t subnormal_value<16>(uint64_t k, const RoundP
     return (uint32_t)__half_as_ushort(__float2half_rn(v));
 }
 
+// The rare branches of virtual_round (src/lo_float.h:2869-2923): NaN, below
+// the smallest subnormal, and the target-subnormal grid.
+template <int MODE, int W>
+__device__ __forceinline__ typename Src<W>::U vr_special(typename Src<W>::U x, const RoundPlan& p,
+                                                      uint64_t r) {
+    using S = Src<W>;
+    using U = typename S::U;
+    using T = typename std::conditional<(W <= 32), uint32_t, uint64_t>::type;
+    const U sign = x & S::SIGN;
+    const U mag = x & (S::SIGN - U(1));
+    // :2869 NaN -> quiet NaN, sign dropped
+    if (mag > S::PINF) return S::QNAN;
+    // :2871-2909 below the smallest subnormal: 0 or +-tiny by mode and sign
+    if ((T)mag < (T)p.tiny_thr) {
+        const T th = sign ? (T)p.tmin_neg : (T)p.tmin_pos;
+        return ((T)mag >= th ? U(p.tiny_bits) : U(0)) | sign;
+    }
+    // :2910-2923 target-subnormal grid
+    const int expf = (int)(mag >> S::M);
+    int shift = p.d + (p.to_min_field - expf);
+    if (shift > W - 1) shift = W - 1;
+    U sig = (mag & ((U(1) << S::M) - U(1))) | (U(1) << S::M);
+    sig = round_mantissa<MODE, W, U>(sig, shift, p.mode, p.len, sign == 0, r);
+    return subnormal_value<W>((uint64_t)(sig >> shift), p) | sign;
+}
+
 // virtual_round(x, params, ps), src/lo_float.h:2843-2939, on a source word.
+// Common case first, on the signed word: RoundMantissa never carries into the
+// sign bit of a finite value, so rounding x and masking the dropped bits equals
+// the reference's round-the-magnitude-then-OR-the-sign (:2925-2933); then the
+// overflow rule (:2935-2936). Inputs whose magnitude is NaN or below the
+// smallest normal of the target (exponent field < to_min_field) take the
+// special branch instead, which a single unsigned range compare detects.
 template <int MODE, int W>
 __device__ __forceinline__ typename Src<W>::U vr_format(typename Src<W>::U x, const RoundPlan& p,
                                                         uint64_t r) {
     using S = Src<W>;
     using U = typename S::U;
+    using T = typename std::conditional<(W <= 32), uint32_t, uint64_t>::type;
     const U sign = x & S::SIGN;
     const U mag = x & (S::SIGN - U(1));
-    // :2869 NaN -> quiet NaN, sign dropped
-    if (mag > S::PINF) return S::QNAN;
-    // :2871-2909 magnitude below the smallest subnormal (compared as float)
-    if ((uint64_t)mag < p.tiny_thr) {
-        const int mode = MODE >= 0 ? MODE : p.mode;
-        const bool nz = (uint64_t)mag >= p.pos_thr;
-        bool to_min;
-        switch (mode) {
-        case LOFGB_RTO:
-        case LOFGB_RAFZ: to_min = nz; break;
-        case LOFGB_RU: to_min = (sign == 0) && nz; break;
-        case LOFGB_RD: to_min = (sign != 0) && nz; break;
-        case LOFGB_RNE:
-        case LOFGB_RNO:
-        case LOFGB_RTTZ:
-        case LOFGB_RTA:
-            if ((uint64_t)mag < p.half_lt) to_min = false;
-            else if ((uint64_t)mag >= p.half_gt) to_min = true;
-            else to_min = (mode == LOFGB_RNO || mode == LOFGB_RTA);
-            break;
-        default: to_min = false;  // RTZ and the stochastic modes flush to 0
-        }
-        return (to_min ? U(p.tiny_bits) : U(0)) | sign;
-    }
-    const int expf = (int)(mag >> S::M);
-    // :2910-2923 target-subnormal grid
-    if (expf < p.to_min_field) {
-        int shift = p.d + (p.to_min_field - expf);
-        if (shift > W - 1) shift = W - 1;
-        U sig = (mag & ((U(1) << S::M) - U(1))) | (U(1) << S::M);
-        sig = round_mantissa<MODE, W, U>(sig, shift, p.mode, p.len, sign == 0, r);
-        const uint64_t k = (uint64_t)(sig >> shift);
-        return subnormal_value<W>(k, p) | sign;
-    }
-    // :2925-2933 normal rounding
-    U b = mag;
-    if (p.d > 0) {
-        b = round_mantissa<MODE, W, U>(b, p.d, p.mode, p.len, sign == 0, r);
-        b &= ~((U(1) << p.d) - U(1));
-    }
-    // :2935-2936 overflow: Saturating returns the input, Extended +inf
-    if ((int64_t)(b >> S::M) > (int64_t)p.to_max_field) return p.saturating ? x : S::PINF;
-    return b | sign;
+    U t = x;
+    if (p.d > 0) t = round_mantissa<MODE, W, U>(x, p.d, p.mode, p.len, sign == 0, r);
+    U res = t & (U)p.keep_mask;
+    if ((T)(res & (S::SIGN - U(1))) >= (T)p.ovf_thr) res = p.saturating ? x : S::PINF;
+    if ((T)(mag - (U)p.norm_thr) > (T)(S::PINF - (U)p.norm_thr)) res = vr_special<MODE, W>(x, p, r);
+    return res;
 }
 
 // virtual_round(x, ToMantissaBits, ps), src/lo_float.h:2715-2756.

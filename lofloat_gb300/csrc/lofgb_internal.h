@@ -24,6 +24,16 @@ struct RoundPlan {
     int32_t saturating;    // Inf_Behaviors::Saturating
     uint64_t tiny_thr, pos_thr, half_lt, half_gt;
     uint64_t tiny_bits;    // from_double<From>(tiny) bit pattern
+    // Derived thresholds for the branch-light device path:
+    //   mag <  norm_thr  <=>  exponent field < to_min_field (target-subnormal range)
+    //   b   >= ovf_thr   <=>  exponent field of the rounded b > to_max_field
+    //   in the tiny branch the result is +-tiny iff mag >= (sign ? tmin_neg : tmin_pos)
+    uint64_t norm_thr, ovf_thr, tmin_pos, tmin_neg;
+    // Fast path on the signed word: res = round(x) & keep_mask (keep_mask
+    // clears the d dropped bits, keeps the sign); overflow iff the magnitude
+    // of res >= ovf_thr; everything with magnitude < norm_thr or NaN takes the
+    // special path.
+    uint64_t keep_mask;
     float tiny_f;          // To_min_val (a float in the reference)
     int32_t pad;
 };

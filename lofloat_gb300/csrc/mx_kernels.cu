@@ -66,9 +66,10 @@ __device__ __forceinline__ BlockScale block_scale(float amax, const RoundPlan& p
     BlockScale b;
     b.scale = __uint_as_float(sb);
     b.pos = b.scale > 0.0f;
-    const uint32_t ef = sb >> 23;  // sign is 0 whenever pos
-    b.pow2 = b.pos && (sb & 0x7FFFFFu) == 0 && ef >= 1 && ef <= 254;
-    b.inv = b.pow2 ? __frcp_rn(b.scale) : 0.0f;
+    // scale = 2^(E-127) with exponent field E in [1, 253]: 1/scale = 2^(127-E)
+    // is a normal float with field 254-E, built directly from the bits
+    b.pow2 = (sb & 0x807FFFFFu) == 0 && (sb - 0x00800000u) <= 0x7E000000u;
+    b.inv = __uint_as_float(0x7F000000u - (sb & 0x7F800000u));
     return b;
 }
 
