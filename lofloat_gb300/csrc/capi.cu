@@ -157,6 +157,20 @@ int make_round_plan(RoundPlan* p, const lofgb_format* f, int src_bits, int mode,
     case LOFGB_RD: p->tmin_pos = never; p->tmin_neg = p->pos_thr; break;
     default: p->tmin_pos = p->tmin_neg = never;  // RTZ and the stochastic modes flush to 0
     }
+    // float-grid rounding of below-normal f32 magnitudes (see RoundPlan::grid)
+    p->grid = 0;
+    const int gexp = to_min - m;  // tiny = 2^gexp
+    if (src_bits == 32 && gexp >= -149 && gexp + 23 <= 127) {
+        p->grid_c = std::ldexp(1.0f, gexp + 23);
+        switch (mode) {
+        case LOFGB_RNE: p->grid = 1; break;
+        case LOFGB_RTZ: p->grid = 2; p->grid_up_pos = 0; p->grid_up_neg = 0; break;
+        case LOFGB_RAFZ: p->grid = 2; p->grid_up_pos = 1; p->grid_up_neg = 1; break;
+        case LOFGB_RU: p->grid = 2; p->grid_up_pos = 1; p->grid_up_neg = 0; break;
+        case LOFGB_RD: p->grid = 2; p->grid_up_pos = 0; p->grid_up_neg = 1; break;
+        default: break;
+        }
+    }
     return LOFGB_OK;
 }
 

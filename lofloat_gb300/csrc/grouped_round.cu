@@ -42,12 +42,16 @@ __device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
         for (int64_t v = v0 + threadIdx.x; v < v1; v += GT) {
             const uint4 a = __ldcs(vin + v);
             const uint64_t i = (uint64_t)v * 4;
-            uint4 o;
-            o.x = elem<MODE>(a.x, t, i + 0);
-            o.y = elem<MODE>(a.y, t, i + 1);
-            o.z = elem<MODE>(a.z, t, i + 2);
-            o.w = elem<MODE>(a.w, t, i + 3);
-            __stcs(vout + v, o);
+            uint32_t w[4] = {a.x, a.y, a.z, a.w};
+            uint64_t r[4];
+            const int mode = MODE >= 0 ? MODE : t.plan.mode;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (t.apply_scale) w[q] = __float_as_uint(__fmul_rn(t.scale, __uint_as_float(w[q])));
+                r[q] = mode_is_stochastic(mode) ? rng64(t.seed, t.offset + i + q) : 0ull;
+            }
+            vr_format_f32x4<MODE>(w, t.plan, r);
+            __stcs(vout + v, make_uint4(w[0], w[1], w[2], w[3]));
         }
         for (int64_t i = (v1 << 2) + threadIdx.x; i < e1; i += GT) {
             const uint32_t w = reinterpret_cast<const uint32_t*>(t.in)[i];

@@ -161,52 +161,117 @@ __device__ __forceinline__ uint32_t subnormal_value<16>(uint64_t k, const RoundP
 }
 
 // The rare branches of virtual_round (src/lo_float.h:2869-2923): NaN, below
-// the smallest subnormal, and the target-subnormal grid.
+// the smallest subnormal, and the target-subnormal grid — computed without
+// branches (every candidate, then a select), so that a warp running them
+// for a few lanes pays no divergence bookkeeping.
 template <int MODE, int W>
 __device__ __forceinline__ typename Src<W>::U vr_special(typename Src<W>::U x, const RoundPlan& p,
-                                                      uint64_t r) {
+                                                         uint64_t r) {
     using S = Src<W>;
     using U = typename S::U;
     using T = typename std::conditional<(W <= 32), uint32_t, uint64_t>::type;
     const U sign = x & S::SIGN;
     const U mag = x & (S::SIGN - U(1));
-    // :2869 NaN -> quiet NaN, sign dropped
-    if (mag > S::PINF) return S::QNAN;
     // :2871-2909 below the smallest subnormal: 0 or +-tiny by mode and sign
-    if ((T)mag < (T)p.tiny_thr) {
-        const T th = sign ? (T)p.tmin_neg : (T)p.tmin_pos;
-        return ((T)mag >= th ? U(p.tiny_bits) : U(0)) | sign;
-    }
-    // :2910-2923 target-subnormal grid
+    const T th = sign ? (T)p.tmin_neg : (T)p.tmin_pos;
+    const U tiny_res = ((T)mag >= th ? U(p.tiny_bits) : U(0)) | sign;
+    // :2910-2923 target-subnormal grid (shift clamped to a defined range for
+    // lanes whose result is not selected)
     const int expf = (int)(mag >> S::M);
     int shift = p.d + (p.to_min_field - expf);
-    if (shift > W - 1) shift = W - 1;
+    shift = shift < 0 ? 0 : (shift > W - 1 ? W - 1 : shift);
     U sig = (mag & ((U(1) << S::M) - U(1))) | (U(1) << S::M);
     sig = round_mantissa<MODE, W, U>(sig, shift, p.mode, p.len, sign == 0, r);
-    return subnormal_value<W>((uint64_t)(sig >> shift), p) | sign;
+    const U sub_res = subnormal_value<W>((uint64_t)(sig >> shift), p) | sign;
+    U res = (T)mag < (T)p.tiny_thr ? tiny_res : sub_res;
+    // :2869 NaN -> quiet NaN, sign dropped
+    return mag > S::PINF ? U(S::QNAN) : res;
 }
 
-// virtual_round(x, params, ps), src/lo_float.h:2843-2939, on a source word.
-// Common case first, on the signed word: RoundMantissa never carries into the
-// sign bit of a finite value, so rounding x and masking the dropped bits equals
-// the reference's round-the-magnitude-then-OR-the-sign (:2925-2933); then the
-// overflow rule (:2935-2936). Inputs whose magnitude is NaN or below the
-// smallest normal of the target (exponent field < to_min_field) take the
-// special branch instead, which a single unsigned range compare detects.
+// Common case of virtual_round(x, params, ps) (src/lo_float.h:2925-2936), on
+// the signed word: RoundMantissa never carries into the sign bit of a finite
+// value, so rounding x and masking the dropped bits equals the reference's
+// round-the-magnitude-then-OR-the-sign; then the overflow rule.
 template <int MODE, int W>
-__device__ __forceinline__ typename Src<W>::U vr_format(typename Src<W>::U x, const RoundPlan& p,
+__device__ __forceinline__ typename Src<W>::U vr_normal(typename Src<W>::U x, const RoundPlan& p,
                                                         uint64_t r) {
     using S = Src<W>;
     using U = typename S::U;
     using T = typename std::conditional<(W <= 32), uint32_t, uint64_t>::type;
-    const U sign = x & S::SIGN;
-    const U mag = x & (S::SIGN - U(1));
     U t = x;
-    if (p.d > 0) t = round_mantissa<MODE, W, U>(x, p.d, p.mode, p.len, sign == 0, r);
+    if (p.d > 0) t = round_mantissa<MODE, W, U>(x, p.d, p.mode, p.len, (x & S::SIGN) == 0, r);
     U res = t & (U)p.keep_mask;
     if ((T)(res & (S::SIGN - U(1))) >= (T)p.ovf_thr) res = p.saturating ? x : S::PINF;
-    if ((T)(mag - (U)p.norm_thr) > (T)(S::PINF - (U)p.norm_thr)) res = vr_special<MODE, W>(x, p, r);
     return res;
+}
+
+// True when x needs the rare branches: NaN, or magnitude below the target's
+// smallest normal (exponent field < to_min_field).
+template <int W>
+__device__ __forceinline__ bool vr_is_special(typename Src<W>::U x, const RoundPlan& p) {
+    using S = Src<W>;
+    using U = typename S::U;
+    using T = typename std::conditional<(W <= 32), uint32_t, uint64_t>::type;
+    const U mag = x & (S::SIGN - U(1));
+    return (T)(mag - (U)p.norm_thr) > (T)(S::PINF - (U)p.norm_thr);
+}
+
+// Rare branches for f32 words. With a float grid (RoundPlan::grid) the tiny
+// and target-subnormal branches are one directed fadd against C and one exact
+// fsub; FP32-subnormal inputs that reach the target-subnormal branch (the
+// reference treats them as exponent -127 with an implicit 1) and NaN keep the
+// exact integer path.
+template <int MODE>
+__device__ __forceinline__ uint32_t vr_special_f32(uint32_t x, const RoundPlan& p, uint64_t r) {
+    if (p.grid == 0) return vr_special<MODE, 32>(x, p, r);
+    const uint32_t sign = x & 0x80000000u, mag = x & 0x7FFFFFFFu;
+    const float a = __uint_as_float(mag);
+    float s;
+    if (p.grid == 1) {
+        s = __fadd_rn(a, p.grid_c);
+    } else {
+        const bool up = sign ? p.grid_up_neg : p.grid_up_pos;
+        s = up ? __fadd_ru(a, p.grid_c) : __fadd_rz(a, p.grid_c);
+    }
+    uint32_t res = __float_as_uint(__fsub_rn(s, p.grid_c)) | sign;
+    const bool exact_path = (mag < 0x00800000u && mag >= (uint32_t)p.tiny_thr) || mag > 0x7F800000u;
+    return exact_path ? vr_special<MODE, 32>(x, p, r) : res;
+}
+
+// virtual_round(x, params, ps), src/lo_float.h:2843-2939, on one source word.
+template <int MODE, int W>
+__device__ __forceinline__ typename Src<W>::U vr_format(typename Src<W>::U x, const RoundPlan& p,
+                                                        uint64_t r) {
+    if (!vr_is_special<W>(x, p)) return vr_normal<MODE, W>(x, p, r);
+    if constexpr (W == 32) return vr_special_f32<MODE>(x, p, r);
+    else return vr_special<MODE, W>(x, p, r);
+}
+
+// Four f32 words at once: the common case for all four, then one warp vote
+// decides whether any lane of the warp needs the rare branches; if so they
+// run for all four words and are selected per word. `r` holds the four
+// random words (zeros for deterministic modes).
+template <int MODE>
+__device__ __forceinline__ void vr_format_f32x4(uint32_t (&w)[4], const RoundPlan& p,
+                                                const uint64_t (&r)[4]) {
+    uint32_t res[4];
+    bool sp[4];
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        res[q] = vr_normal<MODE, 32>(w[q], p, r[q]);
+        sp[q] = vr_is_special<32>(w[q], p);
+        any |= sp[q];
+    }
+    if (__any_sync(__activemask(), any)) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t s = vr_special_f32<MODE>(w[q], p, r[q]);
+            res[q] = sp[q] ? s : res[q];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) w[q] = res[q];
 }
 
 // virtual_round(x, ToMantissaBits, ps), src/lo_float.h:2715-2756.

@@ -35,7 +35,15 @@ struct RoundPlan {
     // special path.
     uint64_t keep_mask;
     float tiny_f;          // To_min_val (a float in the reference)
-    int32_t pad;
+    // Below-normal magnitudes of f32 words by float arithmetic: with
+    // C = 2^(23 + ToMin - m) (so ulp(C) = tiny), fadd(|x|, C) - C rounds |x| to
+    // a multiple of tiny in the fadd's rounding direction — the reference's
+    // tiny and target-subnormal branches for RNE (grid = 1, round to nearest
+    // even) and RTZ/RAFZ/RU/RD (grid = 2, magnitude up iff grid_up_{pos,neg}).
+    // grid = 0: integer path only.
+    int32_t grid;
+    float grid_c;
+    int32_t grid_up_pos, grid_up_neg;
 };
 
 // Host side.

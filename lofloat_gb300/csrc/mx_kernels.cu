@@ -69,18 +69,40 @@ __device__ __forceinline__ BlockScale block_scale(float amax, const RoundPlan& p
     // scale = 2^(E-127) with exponent field E in [1, 253]: 1/scale = 2^(127-E)
     // is a normal float with field 254-E, built directly from the bits
     b.pow2 = (sb & 0x807FFFFFu) == 0 && (sb - 0x00800000u) <= 0x7E000000u;
+    // a non-positive scale zeroes the block; keep the divide off that path
+    b.pow2 = b.pow2 || !b.pos;
     b.inv = __uint_as_float(0x7F000000u - (sb & 0x7F800000u));
     return b;
 }
 
+// Four elements of one block: q = x / scale (x * (1/scale) for power-of-two
+// scales, chosen once per warp), round, rescale; a block whose scale is not
+// positive gives +0 (src/mx_round.cuh:70-75).
 template <int EMODE>
-__device__ __forceinline__ float quant(float x, const BlockScale& b, const RoundPlan& pe,
-                                       uint64_t seed, uint64_t e) {
-    if (!b.pos) return 0.0f;
-    const float q = b.pow2 ? __fmul_rn(x, b.inv) : __fdiv_rn(x, b.scale);
-    const uint64_t r = stoch<EMODE>(pe.mode) ? rng64(seed, e) : 0ull;
-    const float qr = __uint_as_float(vr_format<EMODE, 32>(__float_as_uint(q), pe, r));
-    return __fmul_rn(qr, b.scale);
+__device__ __forceinline__ float4 quant4(float4 x, const BlockScale& b, const RoundPlan& pe,
+                                        uint64_t seed, uint64_t e) {
+    float q[4] = {x.x, x.y, x.z, x.w};
+    if (__all_sync(__activemask(), b.pow2)) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) q[i] = __fmul_rn(q[i], b.inv);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) q[i] = b.pow2 ? __fmul_rn(q[i], b.inv) : __fdiv_rn(q[i], b.scale);
+    }
+    uint32_t w[4];
+    uint64_t r[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        w[i] = __float_as_uint(q[i]);
+        r[i] = stoch<EMODE>(pe.mode) ? rng64(seed, e + i) : 0ull;
+    }
+    vr_format_f32x4<EMODE>(w, pe, r);
+    float4 o;
+    o.x = b.pos ? __fmul_rn(__uint_as_float(w[0]), b.scale) : 0.0f;
+    o.y = b.pos ? __fmul_rn(__uint_as_float(w[1]), b.scale) : 0.0f;
+    o.z = b.pos ? __fmul_rn(__uint_as_float(w[2]), b.scale) : 0.0f;
+    o.w = b.pos ? __fmul_rn(__uint_as_float(w[3]), b.scale) : 0.0f;
+    return o;
 }
 
 // BS: block size; VPT float4s per lane per block; L lanes per block.
@@ -123,12 +145,7 @@ mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, fl
             for (int j = 0; j < VPT; ++j) {
                 const int64_t e = (s0 + u) * SLOT + j * 128 + lane * 4;
                 const uint64_t g = offset + (uint64_t)e;
-                float4 o;
-                o.x = quant<EMODE>(v[u][j].x, b, pe, seed, g + 0);
-                o.y = quant<EMODE>(v[u][j].y, b, pe, seed, g + 1);
-                o.z = quant<EMODE>(v[u][j].z, b, pe, seed, g + 2);
-                o.w = quant<EMODE>(v[u][j].w, b, pe, seed, g + 3);
-                store4<ALIGNED>(out, e, n, o);
+                store4<ALIGNED>(out, e, n, quant4<EMODE>(v[u][j], b, pe, seed, g));
             }
         }
     }

@@ -76,7 +76,17 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
             if (vi >= nvec) continue;
             const uint64_t e0 = offset + (uint64_t)vi * EPV;
             uint4 o;
-            if constexpr (W == 32) {
+            if constexpr (W == 32 && FMT) {
+                uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+                uint64_t r[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (s.apply) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
+                    r[q] = needs_rng<MODE>(p) ? rng64(seed, e0 + q) : 0ull;
+                }
+                vr_format_f32x4<MODE>(w, p, r);
+                o = make_uint4(w[0], w[1], w[2], w[3]);
+            } else if constexpr (W == 32) {
                 o.x = process<MODE, 32, FMT>(v[u].x, p, s, seed, e0 + 0);
                 o.y = process<MODE, 32, FMT>(v[u].y, p, s, seed, e0 + 1);
                 o.z = process<MODE, 32, FMT>(v[u].z, p, s, seed, e0 + 2);
