@@ -166,6 +166,39 @@ int lofgb_gemm_f32(const float* A, int64_t lda, int trans_a, const float* B, int
                    void* workspace, size_t workspace_bytes, void* stream);
 size_t lofgb_gemm_tc_workspace_size(int M, int N, int K);
 
+/* Tensor-core GEMM for callers that cannot allocate device memory.
+ * No counterpart in the reference.
+ *
+ * Some callers may not call cudaMalloc at the point where they run a GEMM.
+ * Examples are a plugin whose host framework owns every byte of device
+ * memory and forbids allocation inside its execute callback, and a serving
+ * loop that allocates once at start-up. The usual tensor-core entry point
+ * (lofgb_gemm_f32 with LOFGB_GEMM_TC) needs a caller-provided workspace for
+ * the BF16 split operands, so these callers could not use it.
+ *
+ * This entry point computes exactly what lofgb_gemm_f32(..., mode = RNE,
+ * variant = LOFGB_GEMM_TC, chunk, ...) computes, same arguments and layouts.
+ * Its scratch is a fixed 64 MiB device array inside liblofgb.so. Every GPU
+ * that loads the library keeps that array until the process exits. The call
+ * itself allocates nothing: no cudaMalloc, no cudaFree, no allocating
+ * library routine.
+ *
+ * Limits and sharing:
+ *   - the split operands need lofgb_gemm_tc_workspace_size(M, N, K) bytes;
+ *     above 64 MiB (for example M = N = K = 2048 fits, 4096 does not) the
+ *     call returns LOFGB_ERR_WORKSPACE and does nothing;
+ *   - the first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture;
+ *   - all calls share the one array, which keeps the last call's contents
+ *     (every call rewrites the parts it reads, so nothing leaks into the
+ *     result); calls that overlap on the GPU (different streams, or
+ *     different host threads, without ordering between them) race on it. */
+int lofgb_gemm_tc_noalloc_f32(const float* A, int64_t lda, int trans_a, const float* B,
+                              int64_t ldb, int trans_b, float* D, int64_t ldd, int M, int N,
+                              int K, int accum_mant_bits, float alpha, int chunk,
+                              void* stream);
+
 /* FP64 GPU oracle GEMM used only to state the error of the tensor-core form:
  * D[i,j] = sum_k (double)A[i,k]*(double)B[k,j] in FP64, same layouts as above.
  * No counterpart in the reference (its harness compares against cuBLAS SGEMM,

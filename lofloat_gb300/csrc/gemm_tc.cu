@@ -552,3 +552,69 @@ int launch_gemm_tc(const float* A, int64_t lda, int ta, const float* B, int64_t 
 }
 
 }  // namespace lofgb
+
+// ---- the no-allocation entry point -------------------------------------------
+// Scratch for lofgb_gemm_tc_noalloc_f32: a fixed device array in this module.
+// Host code must not use the symbol as a pointer; its device address comes
+// from cudaGetSymbolAddress, once per device.
+namespace lofgb {
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = 64ull << 20;
+__device__ __align__(256) uint8_t g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device (first call per
+// device resolves it), or nullptr with the error recorded.
+void* noalloc_scratch(int* status) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        *status = set_error(LOFGB_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+        return nullptr;
+    }
+    if (dev < 0 || dev >= 64) {
+        *status = set_error(LOFGB_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            *status = set_error(LOFGB_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            return nullptr;
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    *status = LOFGB_OK;
+    return g_noalloc_ptr[dev];
+}
+
+}  // namespace
+}  // namespace lofgb
+
+extern "C" int lofgb_gemm_tc_noalloc_f32(const float* A, int64_t lda, int trans_a, const float* B,
+                                         int64_t ldb, int trans_b, float* D, int64_t ldd, int M,
+                                         int N, int K, int accum_mant_bits, float alpha, int chunk,
+                                         void* stream) {
+    using namespace lofgb;
+    if (M > 0 && N > 0 && K > 0) {
+        const size_t need = gemm_tc_workspace(M, N, K);
+        if (need > NOALLOC_SCRATCH_BYTES)
+            return set_error(LOFGB_ERR_WORKSPACE,
+                             "no-alloc GEMM needs %zu bytes of scratch; the built-in array holds %zu",
+                             need, NOALLOC_SCRATCH_BYTES);
+    }
+    int st = LOFGB_OK;
+    void* scratch = nullptr;
+    if (M > 0 && N > 0 && K > 0) {
+        scratch = noalloc_scratch(&st);
+        if (!scratch) return st;
+    }
+    return lofgb_gemm_f32(A, lda, trans_a, B, ldb, trans_b, D, ldd, M, N, K, accum_mant_bits,
+                          LOFGB_RNE, alpha, LOFGB_GEMM_TC, chunk, scratch,
+                          scratch ? NOALLOC_SCRATCH_BYTES : 0, stream);
+}
