@@ -55,7 +55,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-secondary", action="store_true", help="headline workload only")
     ap.add_argument("--only", default=None,
-                    choices=["mx", "round_rne", "round_sr", "gemm_plain", "gemm_tc"],
+                    choices=["mx", "round_rne", "round_sr", "gemm_plain", "gemm_tc", "conv_plain",
+                             "conv_tc", "pwl"],
                     help="run one workload's kernel warmup+steps times and exit (for ncu captures)")
     ap.add_argument("--size", default="full", choices=["full", "small"],
                     help="with --only: full-size workload or a small case (GEMM 1024^3)")
@@ -284,6 +285,166 @@ def secondary(torch, lg, dev, peaks):
         })
     except Exception as e:  # tensor-core form unavailable: report why
         out["gemm_tc_unavailable"] = str(e)[:200]
+    del A, Bt, Aq, Btq, D
+    out.update(linear_fwd_bwd(torch, lg, dev))
+    out.update(grouped_workloads(torch, lg, dev))
+    out.update(conv_workloads(torch, lg, dev, peaks))
+    return out
+
+
+CONV_SHAPE = (32, 256, 14, 14, 256, 3, 3)  # N, C, H, W, K, R, S; stride 1, pad 1
+
+
+def conv_data(torch, lg, dev, shape=CONV_SHAPE):
+    n, c, h, w, k, r, s_ = shape
+    g = torch.Generator(device=dev).manual_seed(6)
+    e4m3 = fmt_desc(lg, 8, 3, 7)
+    x = lg.virtual_round(torch.randn(n, c, h, w, device=dev, generator=g), e4m3)
+    wt = lg.virtual_round(torch.randn(k, c, r, s_, device=dev, generator=g) * 0.05, e4m3)
+    return x, wt
+
+
+def conv_workloads(torch, lg, dev, peaks):
+    """Emulated-accumulation conv2d on a ResNet stage-4 layer: N=32, C=K=256,
+    14x14, 3x3, pad 1, E4M3-rounded activations and weights, 10-bit
+    accumulator; lof_conv2d's order (8-channel tiles) on the CUDA cores and on
+    the tensor cores (chunk 32). Then PWL SiLU over 2^26 FP32 values (16
+    segments on [-8, 8])."""
+    out = {}
+    stream = torch.cuda.current_stream(dev)
+    x, wt = conv_data(torch, lg, dev)
+    n, c, h, w, k, r, s_ = CONV_SHAPE
+    flops = 2.0 * n * k * h * w * c * r * s_
+    y = torch.empty(n, k, h, w, device=dev)
+    for variant in ("plain", "tc"):
+        fn = lambda: lg.conv2d(x, wt, 10, padding=1, order="tiled8", variant=variant, out=y)  # noqa: E731
+        fn()
+        ms = statistics.median(time_events(torch, fn, 5, stream))
+        out[f"conv_resnet_{variant}_TFLOPs"] = round(flops / ms / 1e9, 2)
+        out[f"conv_resnet_{variant}_ms"] = round(ms, 3)
+    out["conv_tc_over_plain"] = round(out["conv_resnet_tc_TFLOPs"] / out["conv_resnet_plain_TFLOPs"], 2)
+    del x, wt, y
+    m = lg.PWLSiLU(R=8.0, lut_bits=4)
+    lut = m.lut.to(dev)
+    g = torch.Generator(device=dev).manual_seed(7)
+    xs = torch.randn(1 << 26, device=dev, generator=g) * 4
+    ys = torch.empty_like(xs)
+    fn = lambda: lg.pwl_silu(xs, lut, 8.0, out=ys)  # noqa: E731
+    for _ in range(3):
+        fn()
+    ms = statistics.median(time_events(torch, fn, 20, stream))
+    gbs = (1 << 26) * 8 / (ms * 1e-3) / 1e9
+    out["pwl_silu_2^26_GBs"] = round(gbs, 1)
+    out["pwl_silu_2^26_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)
+    return out
+
+
+def linear_fwd_bwd(torch, lg, dev):
+    """Differentiable LoFloat linear layer, forward + backward: X 8192x4096 and
+    W 4096x4096 BF16 masters (N(0,1), N(0,0.02), seed 4), MX-E4M3 along K,
+    10-bit emulated accumulator in 64-element chunks on the tensor cores,
+    loss = sum(Y^2), dY stochastic-rounded to E5M2; three 8192x4096x4096 GEMMs."""
+    g = torch.Generator(device=dev).manual_seed(4)
+    X = torch.randn(8192, 4096, device=dev, generator=g).bfloat16().requires_grad_(True)
+    W = (torch.randn(4096, 4096, device=dev, generator=g) * 0.02).bfloat16().requires_grad_(True)
+    e4m3 = fmt_desc(lg, 8, 3, 7)
+    cfg = lg.LinearConfig(act_format=e4m3, weight_format=e4m3, accum_mant_bits=10, variant="tc",
+                          chunk=64, grad_format=fmt_desc(lg, 8, 2, 15), grad_stoch_len=8)
+
+    def step():
+        X.grad = W.grad = None
+        y = lg.lof_linear(X, W, cfg)
+        (y * y).sum().backward()
+
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    s.record()
+    for _ in range(reps):
+        step()
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / reps
+    flops = 3 * 2.0 * 8192 * 4096 * 4096
+    # gradient error against autograd through STE MX rounding and FP64 GEMMs
+    lg.set_seed(0)
+    step()
+    xq = lg.virtual_mx_round(X.detach().float(), 32, e4m3, cfg.scale_format).double()
+    wq = lg.virtual_mx_round(W.detach().float(), 32, e4m3, cfg.scale_format).double()
+    y = xq @ wq.T
+    dy = 2 * y
+    gx, gw = dy @ wq, dy.T @ xq
+    rel_x = ((X.grad.double() - gx).norm() / gx.norm()).item()
+    rel_w = ((W.grad.double() - gw).norm() / gw.norm()).item()
+    return {"linear_fwd_bwd_ms": round(ms, 3), "linear_fwd_bwd_TFLOPs": round(flops / ms / 1e9, 2),
+            "linear_grad_rel_err_vs_fp64": {"dX": rel_x, "dW": rel_w,
+                                             "note": "dY rounded to E5M2 by SR-A: ~2^-3 noise"}}
+
+
+def grouped_workloads(torch, lg, dev):
+    """Config-5 workloads. Part 1: 512 FP32 tensors, n ~ 2^U(10,24), values
+    N(0,1)*2^U(-10,10), each with its own format (exp 2-8, mant 1-10, bias
+    2^(e-1)-1, saturating or not) and mode (RNE/RTZ/RTO/SR-A), seed 5: one
+    grouped launch replayed from a CUDA graph. Part 2: 64 emulated GEMMs,
+    M,N,K in {256..4096 step 256}, MX-E4M3 operands, accumulator bits 7-12,
+    one grouped tensor-core launch with the autotuned schedule, from a graph."""
+    out = {}
+    rng = np.random.default_rng(5)
+    g = torch.Generator(device=dev).manual_seed(5)
+    ins, outs, fmts, modes, lens, seeds = [], [], [], [], [], []
+    for i in range(512):
+        n = int(2 ** rng.uniform(10, 24))
+        x = torch.randn(n, device=dev, generator=g) * float(2 ** rng.uniform(-10, 10))
+        ins.append(x)
+        outs.append(torch.empty_like(x))
+        e, m = int(rng.integers(2, 9)), int(rng.integers(1, 11))
+        fmts.append(lg.make_format(e, m, saturating=bool(rng.integers(0, 2))))
+        modes.append(int(rng.choice([0, 1, 12, 3])))
+        lens.append(8 if modes[-1] == 3 else 0)
+        seeds.append(int(rng.integers(0, 2**62)))
+    gr = lg.GroupedRound(ins, outs, fmts, modes, stoch_lens=lens, seeds=seeds)
+    gr.capture()
+    for _ in range(3):
+        gr.replay()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(10):
+        gr.replay()
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / 10
+    out["grouped_round_512_GBs"] = round(gr.bytes / ms / 1e6, 1)
+    out["grouped_round_512_elements"] = int(gr.bytes // 8)
+    del ins, outs, gr
+    torch.cuda.empty_cache()
+    e4m3 = fmt_desc(lg, 8, 3, 7)
+    e8 = lg.create_e8m0_params()
+    tasks = []
+    for i in range(64):
+        M, N, K = (int(v) for v in rng.integers(1, 17, 3) * 256)
+        A = lg.virtual_mx_round(torch.randn(M, K, device=dev, generator=g), 32, e4m3, e8)
+        Bt = lg.virtual_mx_round(torch.randn(N, K, device=dev, generator=g), 32, e4m3, e8)
+        tasks.append(dict(A=A, B=Bt, D=torch.empty(M, N, device=dev), trans_b=1,
+                          accum_mant_bits=int(rng.integers(7, 13)), chunk=32))
+    gg = lg.GroupedGemm(tasks, schedule="auto")
+    gg.capture()
+    for _ in range(2):
+        gg.replay()
+    torch.cuda.synchronize()
+    s.record()
+    for _ in range(5):
+        gg.replay()
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / 5
+    out["grouped_gemm_64_TFLOPs"] = round(gg.flops / ms / 1e9, 2)
+    out["grouped_gemm_64_ms"] = round(ms, 3)
+    out["grouped_gemm_64_schedule"] = gg.schedule
+    out["grouped_gemm_64_tuning_ms"] = gg.tuning["ms"] if gg.tuning else None
+    out["grouped_gemm_status"] = gg.status()
     return out
 
 
@@ -430,6 +591,20 @@ def run_only(args):
         mode, ln = (0, 0) if args.only == "round_rne" else (3, 8)
         fn = lambda: lg.virtual_round(x, e4m3, round_mode=mode, stoch_len=ln, seed=1, offset=0, out=y)  # noqa: E731
         work, unit = n * 8, "GB/s"
+    elif args.only in ("conv_plain", "conv_tc"):
+        shape = CONV_SHAPE if args.size == "full" else (4, 64, 14, 14, 64, 3, 3)
+        x, wt = conv_data(torch, lg, dev, shape)
+        n, c, h, w, k, r, s_ = shape
+        y = torch.empty(n, k, h, w, device=dev)
+        variant = args.only.split("_")[1]
+        fn = lambda: lg.conv2d(x, wt, 10, padding=1, order="tiled8", variant=variant, out=y)  # noqa: E731
+        work, unit = 2.0 * n * k * h * w * c * r * s_, "TFLOP/s"
+    elif args.only == "pwl":
+        xs = torch.randn(1 << 26, device=dev) * 4
+        lut = lg.PWLSiLU(R=8.0, lut_bits=4).lut.to(dev)
+        ys = torch.empty_like(xs)
+        fn = lambda: lg.pwl_silu(xs, lut, 8.0, out=ys)  # noqa: E731
+        work, unit = (1 << 26) * 8, "GB/s"
     else:
         n = GEMM_N if args.size == "full" else 1024
         g = torch.Generator().manual_seed(3)

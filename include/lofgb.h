@@ -207,6 +207,48 @@ int lofgb_gemm_f64_ref(const float* A, int64_t lda, int trans_a, const float* B,
                        int64_t ldb, int trans_b, double* D, int64_t ldd, int M, int N,
                        int K, void* stream);
 
+/* ---- grouped tensor-core GEMM: many GEMMs of different sizes, one launch ----
+ * Batched form of the tensor-core GEMM (the reference loops over a batch in
+ * Python, LoFloat/layers.py:136-150). Two phases so that the launches can be
+ * captured in a CUDA graph:
+ *   1. lofgb_gemm_grouped_prepare() validates the tasks on the host, lays the
+ *      split operands of every task out in the caller's device `workspace`
+ *      (lofgb_gemm_grouped_workspace_size bytes, 256-byte aligned; only its
+ *      address is used here) and writes a table of
+ *      lofgb_gemm_grouped_table_size bytes into the caller's HOST buffer:
+ *      per-task rows with their TMA descriptors, and the list of 128 x 128
+ *      output tiles in the order given by `schedule`:
+ *        0 = task by task, 1 = longest K first, dealt round-robin to the
+ *        `grid` CTAs, 2 = longest K first, dealt boustrophedon;
+ *   2. the caller copies the table to device memory (256-byte aligned) and
+ *      calls lofgb_gemm_grouped_launch(): one operand-split launch and one
+ *      persistent tensor-core launch of `grid` CTAs (0 = one per SM).
+ * Each task computes what lofgb_gemm_f32(..., LOFGB_RNE, ..., LOFGB_GEMM_TC,
+ * chunk, ...) computes for it. The first 4 bytes of the workspace receive the
+ * device status (0, or LOFGB_ERR_TIMEOUT). */
+typedef struct lofgb_gemm_task {
+    const float* A;
+    int64_t lda;
+    const float* B;
+    int64_t ldb;
+    float* D;
+    int64_t ldd;
+    int32_t trans_a;
+    int32_t trans_b;
+    int32_t M, N, K;
+    int32_t accum_mant_bits;
+    float alpha;
+    int32_t chunk;
+} lofgb_gemm_task;
+
+size_t lofgb_gemm_grouped_workspace_size(const lofgb_gemm_task* tasks, int ntasks);
+size_t lofgb_gemm_grouped_table_size(const lofgb_gemm_task* tasks, int ntasks);
+int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* workspace,
+                               size_t workspace_bytes, int schedule, int grid, void* table,
+                               size_t table_bytes, int64_t* num_tiles, int64_t* split_items);
+int lofgb_gemm_grouped_launch(const void* device_table, int64_t num_tiles, int64_t split_items,
+                              int grid, void* stream);
+
 /* ---- grouped rounding: many tensors, each with its own format, one launch --
  * Batched form of lofgb_round_f32 (the reference rounds one tensor per call,
  * src/LoPy_bind.cpp:122-139). Two phases so that the launch can be captured
@@ -238,6 +280,67 @@ int lofgb_round_grouped_prepare(const lofgb_round_task* tasks, int ntasks, void*
                                 size_t table_bytes, int64_t* num_items);
 int lofgb_round_grouped_f32(const void* device_table, int ntasks, int64_t num_items,
                             void* stream);
+
+/* ---- emulated-accumulation conv2d -----------------------------------------
+ * Replaces LoF_conv2d (src/Lof_kernel.cu:156-227) → lo_float::Conv2d
+ * (src/cutlass_conv.cuh:57-184), and the im2col + lof_gemm path of
+ * LoF_Conv2d.forward (LoFloat/layers.py:684-713). Cross-correlation,
+ * groups = 1, FP32. input N×C×H×W, weight K×C×R×S (OIHW), output N×K×P×Q
+ * (NCHW) with P = (H + 2·pad_h − dil_h·(R−1) − 1)/stride_h + 1 and Q alike.
+ *
+ * Each output is one emulated-accumulator dot product over the reduction
+ * index t ↔ (c, r, s), with the per-MAC leaf of lofgb_gemm_f32:
+ *   acc_0 = +0, acc_{t+1} = RNE_m(rto_fma(w[k,c,r,s], x[n,c,h,w], acc_t)),
+ *   y = alpha·acc,  h = p·stride_h − pad_h + r·dil_h, w = q·stride_w − pad_w + s·dil_w,
+ * where x outside the input is +0 (zero padding). The order of t:
+ *   LOFGB_CONV_CRS     c outer, then r, then s — the row order of
+ *                      F.unfold's columns, so lof_gemm(w.view(K,−1),
+ *                      unfold(x)[n]) (layers.py:690-705) gives the same bits;
+ *   LOFGB_CONV_TILED8  channel tiles of 8 outer, then r, then s, then the 8
+ *                      channels of the tile — CUTLASS's analytic implicit-GEMM
+ *                      fprop iterators with a k-tile of 8 (Conv2d<> default
+ *                      TbK = 8, src/cutlass_conv.cuh:57-65); channels past C in
+ *                      the last tile are (0, 0) products, which leave the
+ *                      accumulator unchanged.
+ * mode must be LOFGB_RNE (the leaf ignores it). alpha: lof_conv2d passes
+ * (float)(1.0 / (weight_scale·input_scale)) computed in double, or 1 when the
+ * product is 0 (src/Lof_kernel.cu:203-206); the im2col path passes lof_gemm's
+ * float alpha. variant LOFGB_GEMM_PLAIN: bit-exact, no workspace.
+ * LOFGB_GEMM_TC: the chunked tensor-core form of lofgb_gemm_f32 over the same
+ * t order, workspace of lofgb_conv2d_workspace_size() bytes (256-byte
+ * aligned). No counterpart for TC in the reference. */
+typedef struct lofgb_conv2d_shape {
+    int32_t n, c, h, w;  /* input N×C×H×W */
+    int32_t k, r, s;     /* weight K×C×R×S */
+    int32_t pad_h, pad_w;
+    int32_t stride_h, stride_w;
+    int32_t dil_h, dil_w;
+} lofgb_conv2d_shape;
+
+enum lofgb_conv_order { LOFGB_CONV_CRS = 0, LOFGB_CONV_TILED8 = 1 };
+
+/* Output spatial size; LOFGB_ERR_SIZE for an invalid shape or P, Q <= 0. */
+int lofgb_conv2d_out_size(const lofgb_conv2d_shape* shape, int32_t* p, int32_t* q);
+size_t lofgb_conv2d_workspace_size(const lofgb_conv2d_shape* shape, int order, int variant);
+int lofgb_conv2d_f32(const float* input, const float* weight, float* output,
+                     const lofgb_conv2d_shape* shape, int accum_mant_bits, int mode,
+                     float alpha, int order, int variant, int chunk, void* workspace,
+                     size_t workspace_bytes, void* stream);
+
+/* ---- piecewise-linear SiLU -------------------------------------------------
+ * Replaces pwl_silu / pwl_silu_kernel (src/LoPy_bind.cpp:228-272,
+ * src/Lof_kernel.cu:240-264). `lut` (device, FP32) holds segments + 1 knots of
+ * SiLU over [-R, R]; segments is a power of two in [2, 4096]. Per element, in
+ * FP32: xc = clamp(x, -R, R); u = (xc + R)·(segments / (2R)); i = min((int)u,
+ * segments − 1); y = fma(u − i, lut[i+1] − lut[i], lut[i]); y = x > 0 ? x : 0
+ * when |x| > R. Half / double inputs are widened to FP32 and the result
+ * narrowed back, as the reference's static_cast does. */
+int lofgb_pwl_silu_f32(const float* in, float* out, int64_t n, const float* lut,
+                       int segments, float R, void* stream);
+int lofgb_pwl_silu_f64(const double* in, double* out, int64_t n, const float* lut,
+                       int segments, float R, void* stream);
+int lofgb_pwl_silu_f16(const uint16_t* in, uint16_t* out, int64_t n, const float* lut,
+                       int segments, float R, void* stream);
 
 #ifdef __cplusplus
 }

@@ -7,21 +7,25 @@ Drop-in surface of the reference package ``LoFloat`` for that path:
 * ``torch.ops.lofloat.virtual_round / virtual_mx_round / lof_gemm`` with the
   reference's schemas (LoFloat/_custom_ops.py);
 * the format factories (LoFloat/formats.py);
-* ``STERound``, ``STEMXRound``, ``LoF_Quantize``, ``LoF_Linear`` (LoFloat/layers.py),
-  plus a differentiable emulated linear (``lof_linear``).
+* ``lof_conv2d`` and ``pwl_silu`` of the compiled module;
+* ``STERound``, ``STEMXRound``, ``LoF_Quantize``, ``LoF_Linear``, ``LoF_Conv2d``,
+  ``PWLSiLU`` (LoFloat/layers.py), plus a differentiable emulated linear
+  (``lof_linear``).
 
 All compute runs in liblofgb.so (include/lofgb.h) on CUDA tensors.
 """
 from . import _custom_ops  # noqa: F401  (registers torch.ops.lofloat.*)
 from .binding import (FloatFormatDescriptor, InfBehavior, NaNBehavior, RoundingMode, Signedness,
-                      gemm, gemm_alpha, gemm_f64_reference, get_rng_state, lof_gemm, set_rng_state,
-                      set_seed, virtual_mx_round, virtual_round)
+                      conv2d, conv2d_alpha, gemm, gemm_alpha, gemm_f64_reference, get_rng_state,
+                      lof_conv2d, lof_gemm, pwl_silu, set_rng_state, set_seed, virtual_mx_round,
+                      virtual_round)
 from .formats import (create_e8m0_params, create_half_params, create_p3109_params,
                       create_single_params, make_format)
-from .layers import (LinearConfig, LoF_Linear, LoF_Quantize, LoFLinearFunction, STEMXRound,
-                     STERound, _fwht, _lof_gemm_2d, _lof_linear, lof_linear)
+from .layers import (LinearConfig, LoF_Conv2d, LoF_Linear, LoF_Quantize, LoFLinearFunction,
+                     PWLSiLU, STEMXRound, STERound, _fwht, _lof_gemm_2d, _lof_linear, lof_linear)
 from ._custom_ops import get_format, register_format
 from .grouped import GroupedRound
+from .autotune import GroupedGemm
 
 __all__ = [
     "FloatFormatDescriptor", "InfBehavior", "NaNBehavior", "RoundingMode", "Signedness",
@@ -29,5 +33,6 @@ __all__ = [
     "set_seed", "get_rng_state", "set_rng_state", "create_p3109_params", "create_e8m0_params",
     "create_half_params", "create_single_params", "make_format", "STERound", "STEMXRound",
     "LoF_Quantize", "LoF_Linear", "LoFLinearFunction", "LinearConfig", "lof_linear",
-    "register_format", "get_format", "GroupedRound",
+    "register_format", "get_format", "GroupedRound", "GroupedGemm", "lof_conv2d", "conv2d",
+    "conv2d_alpha", "pwl_silu", "LoF_Conv2d", "PWLSiLU",
 ]

@@ -29,6 +29,20 @@ class LofgbRoundTask(C.Structure):
                 ("reserved", C.c_int32), ("seed", C.c_uint64), ("offset", C.c_uint64)]
 
 
+class LofgbGemmTask(C.Structure):
+    """``lofgb_gemm_task`` (include/lofgb.h)."""
+    _fields_ = [("A", C.c_void_p), ("lda", C.c_int64), ("B", C.c_void_p), ("ldb", C.c_int64),
+                ("D", C.c_void_p), ("ldd", C.c_int64), ("trans_a", C.c_int32),
+                ("trans_b", C.c_int32), ("M", C.c_int32), ("N", C.c_int32), ("K", C.c_int32),
+                ("accum_mant_bits", C.c_int32), ("alpha", C.c_float), ("chunk", C.c_int32)]
+
+
+class LofgbConv2dShape(C.Structure):
+    """``lofgb_conv2d_shape`` (include/lofgb.h)."""
+    _fields_ = [(f, C.c_int32) for f in ("n", "c", "h", "w", "k", "r", "s", "pad_h", "pad_w",
+                                         "stride_h", "stride_w", "dil_h", "dil_w")]
+
+
 # (name, restype, argtypes) for every entry point of include/lofgb.h
 _vp, _i64, _i32, _u64, _f32, _f64, _sz = (C.c_void_p, C.c_int64, C.c_int, C.c_uint64, C.c_float,
                                           C.c_double, C.c_size_t)
@@ -52,10 +66,23 @@ SIGNATURES = [
                                          _i32, _i32, _f32, _i32, _vp]),
     ("lofgb_gemm_f64_ref", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32,
                                   _vp]),
+    ("lofgb_gemm_grouped_workspace_size", _sz, [C.POINTER(LofgbGemmTask), _i32]),
+    ("lofgb_gemm_grouped_table_size", _sz, [C.POINTER(LofgbGemmTask), _i32]),
+    ("lofgb_gemm_grouped_prepare", _i32, [C.POINTER(LofgbGemmTask), _i32, _vp, _sz, _i32, _i32, _vp,
+                                          _sz, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    ("lofgb_gemm_grouped_launch", _i32, [_vp, _i64, _i64, _i32, _vp]),
     ("lofgb_round_grouped_table_size", _sz, [_i32]),
     ("lofgb_round_grouped_prepare", _i32, [C.POINTER(LofgbRoundTask), _i32, _vp, _sz,
                                            C.POINTER(C.c_int64)]),
     ("lofgb_round_grouped_f32", _i32, [_vp, _i32, _i64, _vp]),
+    ("lofgb_conv2d_out_size", _i32, [C.POINTER(LofgbConv2dShape), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32)]),
+    ("lofgb_conv2d_workspace_size", _sz, [C.POINTER(LofgbConv2dShape), _i32, _i32]),
+    ("lofgb_conv2d_f32", _i32, [_vp, _vp, _vp, C.POINTER(LofgbConv2dShape), _i32, _i32, _f32, _i32,
+                                _i32, _i32, _vp, _sz, _vp]),
+    ("lofgb_pwl_silu_f32", _i32, [_vp, _vp, _i64, _vp, _i32, _f32, _vp]),
+    ("lofgb_pwl_silu_f64", _i32, [_vp, _vp, _i64, _vp, _i32, _f32, _vp]),
+    ("lofgb_pwl_silu_f16", _i32, [_vp, _vp, _i64, _vp, _i32, _f32, _vp]),
 ]
 
 

@@ -248,7 +248,10 @@ _ws_cache: dict = {}
 
 
 def _tc_workspace(device: torch.device, M: int, N: int, K: int) -> torch.Tensor:
-    need = int(_native.lib().lofgb_gemm_tc_workspace_size(M, N, K))
+    return _workspace(device, int(_native.lib().lofgb_gemm_tc_workspace_size(M, N, K)))
+
+
+def _workspace(device: torch.device, need: int) -> torch.Tensor:
     # one workspace per (device, stream): calls on one stream are ordered, so
     # reusing it is race-free; another stream gets its own
     key = (device, torch.cuda.current_stream(device).cuda_stream)
@@ -338,3 +341,120 @@ def gemm_f64_reference(A: torch.Tensor, B: torch.Tensor, *, trans_a: bool = Fals
                                                B.shape[1], int(trans_b), D.data_ptr(), N, M, N, K,
                                                _stream(A)), "gemm_f64_reference")
     return D
+
+
+# ---- conv2d -------------------------------------------------------------------
+CONV_ORDERS = {"crs": 0, "tiled8": 1}
+
+
+def conv2d_alpha(weight_scale: float, input_scale: float) -> float:
+    """(float)(1.0 / (weight_scale * input_scale)) computed in double, 1 when the
+    product is 0 (src/Lof_kernel.cu:203-206)."""
+    denom = float(weight_scale) * float(input_scale)
+    return 1.0 if denom == 0.0 else float(np.float32(1.0 / denom))
+
+
+def _pair(v) -> tuple[int, int]:
+    return (int(v[0]), int(v[1])) if isinstance(v, (tuple, list)) else (int(v), int(v))
+
+
+def conv2d_shape(input_shape, weight_shape, stride=1, padding=0, dilation=1):
+    """lofgb_conv2d_shape for an NCHW input and a KCRS weight."""
+    sh, sw = _pair(stride)
+    ph, pw = _pair(padding)
+    dh, dw = _pair(dilation)
+    n, c, h, w = (int(v) for v in input_shape)
+    k, _, r, s_ = (int(v) for v in weight_shape)
+    return _native.LofgbConv2dShape(n, c, h, w, k, r, s_, ph, pw, sh, sw, dh, dw)
+
+
+def conv2d(input: torch.Tensor, weight: torch.Tensor, accum_mant_bits: int, *, stride=1,
+           padding=0, dilation=1, alpha: float = 1.0, order: str = "crs",
+           variant: str = "plain", chunk: int = 32,
+           out: torch.Tensor | None = None) -> torch.Tensor:
+    """Emulated-accumulation conv2d (cross-correlation, groups = 1) on NCHW
+    input and KCRS weight, output NCHW. `order` picks the reduction order:
+    "crs" (c, r, s — the im2col + lof_gemm path of LoF_Conv2d) or "tiled8"
+    (8-channel tiles outer — lof_conv2d's implicit GEMM). variant "plain" is
+    bit-exact; "tc" is the chunked tensor-core form."""
+    for t, nm in ((input, "input"), (weight, "weight")):
+        if t.dim() != 4:
+            raise RuntimeError("LoF_conv2d: input and weight must be 4-D (NCHW / OIHW)")
+        if t.dtype != torch.float32:
+            raise RuntimeError("LoF_conv2d: only float32 inputs are supported")
+        _require_cuda(t, "LoF_conv2d")
+    if input.shape[1] != weight.shape[1]:
+        raise RuntimeError(f"LoF_conv2d: input C_in ({input.shape[1]}) != weight C_in "
+                           f"({weight.shape[1]})")
+    x = input.contiguous()
+    w = weight.contiguous()
+    shape = conv2d_shape(x.shape, w.shape, stride, padding, dilation)
+    L = _native.lib()
+    P, Q = C.c_int32(), C.c_int32()
+    check(L.lofgb_conv2d_out_size(C.byref(shape), C.byref(P), C.byref(Q)), "LoF_conv2d")
+    oshape = (x.shape[0], w.shape[0], P.value, Q.value)
+    y = torch.empty(oshape, dtype=torch.float32, device=x.device) if out is None else out
+    if tuple(y.shape) != oshape or not y.is_contiguous() or y.dtype != torch.float32:
+        raise RuntimeError(f"LoF_conv2d: out must be a contiguous float32 {oshape} tensor")
+    o = CONV_ORDERS[order]
+    v = {"plain": 0, "tc": 1}[variant]
+    with torch.cuda.device(x.device):
+        ws, wsb = None, 0
+        if v == 1:
+            buf = _workspace(x.device, int(L.lofgb_conv2d_workspace_size(C.byref(shape), o, v)))
+            ws, wsb = buf.data_ptr(), buf.numel()
+        check(L.lofgb_conv2d_f32(x.data_ptr(), w.data_ptr(), y.data_ptr(), C.byref(shape),
+                                 int(accum_mant_bits), int(RoundingMode.RoundToNearestEven),
+                                 float(alpha), o, v, int(chunk), ws, wsb, _stream(x)),
+              "LoF_conv2d")
+    return y
+
+
+def lof_conv2d(input: torch.Tensor, weight: torch.Tensor, pad_h: int, pad_w: int, stride_h: int,
+               stride_w: int, dilation_h: int, dilation_w: int, accum_mant_bits: int,
+               round_mode=RoundingMode.RoundToNearestEven, stochastic_rounding_bits: int = 0,
+               weight_scale: float = 1.0, input_scale: float = 1.0) -> torch.Tensor:
+    """Drop-in for the reference's lof_conv2d (src/LoPy_bind.cpp:374-389 →
+    src/Lof_kernel.cu:156-227): NCHW / OIHW float32 CUDA tensors, output NCHW
+    divided by (weight_scale * input_scale), the accumulator re-rounded to
+    `accum_mant_bits` after every multiply-add in the implicit GEMM's order,
+    bit-exact. round_mode and stochastic_rounding_bits are accepted and
+    ignored, as by the shared GEMM leaf."""
+    del round_mode, stochastic_rounding_bits
+    return conv2d(input, weight, accum_mant_bits, stride=(stride_h, stride_w),
+                  padding=(pad_h, pad_w), dilation=(dilation_h, dilation_w),
+                  alpha=conv2d_alpha(weight_scale, input_scale), order="tiled8")
+
+
+# ---- piecewise-linear SiLU -------------------------------------------------------
+_PWL_FNS = {torch.float32: "lofgb_pwl_silu_f32", torch.float64: "lofgb_pwl_silu_f64",
+            torch.float16: "lofgb_pwl_silu_f16"}
+
+
+def pwl_silu(input: torch.Tensor, lut: torch.Tensor, R: float, *,
+             out: torch.Tensor | None = None) -> torch.Tensor:
+    """Drop-in for the reference's pwl_silu (src/LoPy_bind.cpp:228-272): SiLU
+    interpolated from `lut` (segments + 1 knots over [-R, R], segments a power
+    of two in [2, 4096]), the relu asymptote outside [-R, R]. Returns a new
+    tensor of the input's dtype (float16, float32 or float64)."""
+    if lut.dim() != 1 or lut.numel() < 2:
+        raise RuntimeError("pwl_silu: lut must be 1-D with >= 2 entries")
+    if not float(R) > 0.0:
+        raise RuntimeError("pwl_silu: R must be positive")
+    _require_cuda(input, "pwl_silu")
+    if input.dtype not in _PWL_FNS:
+        raise RuntimeError(f"pwl_silu: unsupported dtype {input.dtype}")
+    nseg = lut.numel() - 1
+    if nseg < 2 or nseg > 4096 or nseg & (nseg - 1):
+        raise RuntimeError(f"pwl_silu: lut length {nseg} is not a supported power of 2 in "
+                           "[2, 4096]")
+    x = input.contiguous()
+    lut_f = lut.to(device=x.device, dtype=torch.float32).contiguous()
+    y = torch.empty_like(x) if out is None else out
+    if y.shape != x.shape or y.dtype != x.dtype or not y.is_contiguous() or y.device != x.device:
+        raise RuntimeError("pwl_silu: out must be a contiguous tensor like input")
+    with torch.cuda.device(x.device):
+        check(getattr(_native.lib(), _PWL_FNS[x.dtype])(x.data_ptr(), y.data_ptr(), x.numel(),
+                                                        lut_f.data_ptr(), nseg, float(R),
+                                                        _stream(x)), "pwl_silu")
+    return y

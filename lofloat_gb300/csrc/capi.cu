@@ -24,6 +24,8 @@ int set_error(int status, const char* fmt, ...) {
     return status;
 }
 
+void clear_error() { g_detail[0] = 0; }
+
 int check_launch(const char* what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
@@ -170,6 +172,18 @@ int make_round_plan(RoundPlan* p, const lofgb_format* f, int src_bits, int mode,
         case LOFGB_RD: p->grid = 2; p->grid_up_pos = 0; p->grid_up_neg = 1; break;
         default: break;
         }
+    }
+    // whole-range float rounding (see RoundPlan::uni)
+    p->uni = 0;
+    p->sat_and = p->saturating ? 0xFFFFFFFFu : 0u;
+    p->sat_or = p->saturating ? 0u : 0x7F800000u;
+    const int hi = p->to_max_field + 1;
+    if (p->grid != 0 && p->d >= 1 && p->tiny_thr >= 0x00800000ull && hi + p->d <= 254 &&
+        p->to_min_field >= 1 && hi >= p->to_min_field) {
+        p->uni = p->grid;
+        p->uni_lo = (uint32_t)p->to_min_field << 23;
+        p->uni_hi = (uint32_t)hi << 23;
+        p->uni_d = (uint32_t)p->d << 23;
     }
     return LOFGB_OK;
 }

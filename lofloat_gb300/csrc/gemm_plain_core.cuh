@@ -1,0 +1,68 @@
+// gemm_plain_core.cuh — the per-MAC emulated-accumulation core shared by the
+// plain GEMM (gemm_plain.cu) and the plain implicit-GEMM conv2d (conv.cu):
+// the leaf, the 128 x 128 x 16 shared-memory tile shape and the MAC loop over
+// one k-tile.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "lof_round.cuh"
+
+namespace lofgb {
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 16, NT = 256;
+constexpr int PAD = 4;
+
+// One emulated MAC. The round-to-odd word v = rz | sticky: when the two
+// directed FMAs differ they are adjacent, so (rd | ru) & 1 is 1 exactly when
+// the sum was inexact or rz is already odd — the same word as rz | (rd != ru).
+// The RNE step works on the signed word: for finite values (and the GPU's
+// positive canonical NaN) adding < 2^ro never carries into the sign bit.
+template <bool ROUND>
+__device__ __forceinline__ float emac(float a, float b, float acc, int ro, uint32_t half_m1,
+                                      uint32_t mask) {
+    const float rd = __fmaf_rd(a, b, acc);
+    const float ru = __fmaf_ru(a, b, acc);
+    const uint32_t rz = __float_as_uint(rd >= 0.0f ? rd : ru);
+    const uint32_t v = rz | ((__float_as_uint(rd) | __float_as_uint(ru)) & 1u);
+    if (!ROUND) return __uint_as_float(v);
+    const uint32_t t = v + ((v >> ro) & 1u) + half_m1;
+    return __uint_as_float(t & mask);
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float* src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src),
+                 "r"(valid ? 4 : 0)
+                 : "memory");
+}
+
+// One staged k-tile: k-major shared tiles As[k][m], Bs[k][n]; thread (tx, ty)
+// owns rows {ty*4 .. ty*4+3, 64+ty*4 .. 64+ty*4+3} and the same columns of tx.
+// One 8x8 MAC block per k (640 instructions) stays resident in the
+// instruction cache; unrolling k as well overflows it.
+template <bool ROUND>
+__device__ __forceinline__ void mac_ktile(const float (*As)[BM + PAD], const float (*Bs)[BN + PAD],
+                                          float (&acc)[8][8], int kmax, int tx, int ty, int ro,
+                                          uint32_t half_m1, uint32_t mask) {
+#pragma unroll 1
+    for (int kk = 0; kk < kmax; ++kk) {
+        const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
+        const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][64 + ty * 4]);
+        const float4 b0 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+        const float4 b1 = *reinterpret_cast<const float4*>(&Bs[kk][64 + tx * 4]);
+        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                acc[i][j] = emac<ROUND>(av[i], bv[j], acc[i][j], ro, half_m1, mask);
+    }
+}
+
+}  // namespace
+}  // namespace lofgb

@@ -39,6 +39,7 @@
 #include <mutex>
 
 #include "lofgb_internal.h"
+#include "tc_split.cuh"
 
 namespace lofgb {
 
@@ -65,6 +66,8 @@ struct TcParams {
     int ro;                // 23 - accum_mant_bits
     float alpha;
     int* status;           // workspace status word
+    int64_t img_L;         // conv output: columns per image (0: plain row-major D)
+    int64_t img_stride;    // conv output: elements per image
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -204,11 +207,101 @@ __device__ __forceinline__ float fold(float acc, float s, int ro, uint32_t half_
     return __uint_as_float(t & mask);
 }
 
-__global__ void __launch_bounds__(NUM_THREADS, 1)
-gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant__ CUtensorMap tm_alo,
-               const __grid_constant__ CUtensorMap tm_bhi, const __grid_constant__ CUtensorMap tm_blo,
-               TcParams prm) {
-    extern __shared__ uint8_t smem_raw[];
+// ---- tile sources ------------------------------------------------------------
+// Everything the three roles need to know about one 128 x 128 output tile.
+struct TileInfo {
+    const CUtensorMap* map[4];  // A hi, A lo, B hi, B lo
+    float* D;
+    int64_t ldd;
+    int M, N, m0, n0, Kp, chunk16, ro;
+    float alpha;
+    // conv2d output (img_L > 0): column j = img * img_L + l of row i is
+    // stored at D[img * img_stride + i * ldd + l]
+    int64_t img_L, img_stride;
+};
+
+// One GEMM; its tensor maps are kernel parameters.
+struct SingleSrc {
+    const CUtensorMap* m[4];
+    TcParams prm;
+    __device__ __forceinline__ int count() const { return prm.tiles_m * prm.tiles_n; }
+    __device__ __forceinline__ TileInfo get(int t) const {
+        TileInfo ti;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) ti.map[i] = m[i];
+        ti.D = prm.D;
+        ti.ldd = prm.ldd;
+        ti.M = prm.M;
+        ti.N = prm.N;
+        ti.m0 = (t / prm.tiles_n) * TBM;
+        ti.n0 = (t % prm.tiles_n) * TBN;
+        ti.Kp = prm.Kp;
+        ti.chunk16 = prm.chunk16;
+        ti.ro = prm.ro;
+        ti.alpha = prm.alpha;
+        ti.img_L = prm.img_L;
+        ti.img_stride = prm.img_stride;
+        return ti;
+    }
+};
+
+// Many GEMMs: a device table of per-task rows (tensor maps in global memory,
+// 64-byte aligned) and a tile list whose order is the schedule.
+struct GroupRow {
+    CUtensorMap map[4];
+    float* D;
+    int64_t ldd;
+    int32_t M, N, Kp, chunk16, ro;
+    float alpha;
+    int32_t pad[8];
+};
+struct TileRef {
+    int32_t task, m0, n0, pad;
+};
+struct SplitRow {
+    const float* src;
+    int64_t ld;
+    __nv_bfloat16* hi;
+    __nv_bfloat16* lo;
+    int64_t item_begin;  // first 32 x 64 split item of this operand
+    int32_t kmajor, rows, K, R, Kp, pad;
+};
+struct GroupHeader {   // at the start of the device table; offsets from its base
+    int32_t ntasks, ntiles, nsplit, pad;
+    int64_t split_items;
+    int64_t rows_off, tiles_off, splits_off;
+    int* status;
+};
+
+struct GroupedSrc {
+    const GroupHeader* h;
+    __device__ __forceinline__ int count() const { return h->ntiles; }
+    __device__ __forceinline__ TileInfo get(int t) const {
+        const uint8_t* base = reinterpret_cast<const uint8_t*>(h);
+        const TileRef r = reinterpret_cast<const TileRef*>(base + h->tiles_off)[t];
+        const GroupRow* g = reinterpret_cast<const GroupRow*>(base + h->rows_off) + r.task;
+        TileInfo ti;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) ti.map[i] = &g->map[i];
+        ti.D = g->D;
+        ti.ldd = g->ldd;
+        ti.M = g->M;
+        ti.N = g->N;
+        ti.m0 = r.m0;
+        ti.n0 = r.n0;
+        ti.Kp = g->Kp;
+        ti.chunk16 = g->chunk16;
+        ti.ro = g->ro;
+        ti.alpha = g->alpha;
+        ti.img_L = 0;
+        ti.img_stride = 0;
+        return ti;
+    }
+};
+
+// ---- the persistent tensor-core body (shared by both launches) ---------------
+template <class Src>
+__device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* smem_raw) {
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                ~uintptr_t(1023));
     uint8_t* tiles = smem;
@@ -249,11 +342,7 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
-
-    const int num_tiles = prm.tiles_m * prm.tiles_n;
-    const int ksteps = prm.Kp / SK;        // pipeline stages per tile
-    const int k16 = prm.Kp / 16;           // MMA k-steps per tile
-    const int nchunks = (k16 + prm.chunk16 - 1) / prm.chunk16;
+    const int num_tiles = src.count();
 
     if (warp == 0) {
         // ---------------- TMA producer ----------------
@@ -261,18 +350,18 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
             uint32_t it = 0;
             bool ok = true;
             for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
-                const int m0 = (tile / prm.tiles_n) * TBM;
-                const int n0 = (tile % prm.tiles_n) * TBN;
+                const TileInfo ti = src.get(tile);
+                const int ksteps = ti.Kp / SK;
                 for (int ks = 0; ks < ksteps; ++ks, ++it) {
                     const uint32_t s = it % STAGES;
                     const uint32_t ph = (it / STAGES) & 1u;
-                    if (!mbar_wait(bar_empty + 8 * s, ph ^ 1u, abort_flag, prm.status)) { ok = false; break; }
+                    if (!mbar_wait(bar_empty + 8 * s, ph ^ 1u, abort_flag, status)) { ok = false; break; }
                     const uint32_t base = smem_u32(tiles + s * STAGE_BYTES);
                     mbar_arrive_expect_tx(bar_full + 8 * s, STAGE_BYTES);
-                    tma_load_2d(base + 0 * TILE_BYTES, &tm_ahi, ks * SK, m0, bar_full + 8 * s);
-                    tma_load_2d(base + 1 * TILE_BYTES, &tm_alo, ks * SK, m0, bar_full + 8 * s);
-                    tma_load_2d(base + 2 * TILE_BYTES, &tm_bhi, ks * SK, n0, bar_full + 8 * s);
-                    tma_load_2d(base + 3 * TILE_BYTES, &tm_blo, ks * SK, n0, bar_full + 8 * s);
+                    tma_load_2d(base + 0 * TILE_BYTES, ti.map[0], ks * SK, ti.m0, bar_full + 8 * s);
+                    tma_load_2d(base + 1 * TILE_BYTES, ti.map[1], ks * SK, ti.m0, bar_full + 8 * s);
+                    tma_load_2d(base + 2 * TILE_BYTES, ti.map[2], ks * SK, ti.n0, bar_full + 8 * s);
+                    tma_load_2d(base + 3 * TILE_BYTES, ti.map[3], ks * SK, ti.n0, bar_full + 8 * s);
                 }
             }
             if (!ok) {
@@ -288,17 +377,20 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
             uint32_t cg = 0;      // global chunk counter
             bool ok = true;
             for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
+                const TileInfo ti = src.get(tile);
+                const int ksteps = ti.Kp / SK;
+                const int k16 = ti.Kp / 16;
                 int kk16 = 0;
                 for (int ks = 0; ks < ksteps && ok; ++ks, ++it) {
                     const uint32_t s = it % STAGES;
-                    if (!mbar_wait(bar_full + 8 * s, (it / STAGES) & 1u, abort_flag, prm.status)) { ok = false; break; }
+                    if (!mbar_wait(bar_full + 8 * s, (it / STAGES) & 1u, abort_flag, status)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t base = smem_u32(tiles + s * STAGE_BYTES);
                     for (int j = 0; j < SK / 16; ++j, ++kk16) {
-                        const int pos = kk16 % prm.chunk16;
+                        const int pos = kk16 % ti.chunk16;
                         const uint32_t buf = cg & 1u;
                         if (pos == 0) {
-                            if (!mbar_wait(bar_tempty + 8 * buf, ((cg >> 1) & 1u) ^ 1u, abort_flag, prm.status)) { ok = false; break; }
+                            if (!mbar_wait(bar_tempty + 8 * buf, ((cg >> 1) & 1u) ^ 1u, abort_flag, status)) { ok = false; break; }
                             tc_fence_after();
                         }
                         const uint32_t d = tmem_base + buf * TBN;
@@ -309,7 +401,7 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
                         umma_f16(d, ahi, bhi, pos > 0 ? 1u : 0u);
                         umma_f16(d, ahi, blo, 1u);
                         umma_f16(d, alo, bhi, 1u);
-                        if (pos == prm.chunk16 - 1 || kk16 == k16 - 1) {
+                        if (pos == ti.chunk16 - 1 || kk16 == k16 - 1) {
                             umma_commit(bar_tfull + 8 * buf);
                             ++cg;
                         }
@@ -327,14 +419,14 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
         const int ew = warp - 2;              // 0..7
         const int quarter = warp & 3;         // TMEM lane quarter this warp may access
         const int half = ew >> 2;             // column half
-        const int ro = prm.ro;
-        const uint32_t half_m1 = ro > 0 ? (1u << (ro - 1)) - 1u : 0u;
-        const uint32_t mask = ro > 0 ? ~((1u << ro) - 1u) : ~0u;
         uint32_t cg = 0;
         bool ok = true;
         for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
-            const int m0 = (tile / prm.tiles_n) * TBM;
-            const int n0 = (tile % prm.tiles_n) * TBN;
+            const TileInfo ti = src.get(tile);
+            const int nchunks = (ti.Kp / 16 + ti.chunk16 - 1) / ti.chunk16;
+            const int ro = ti.ro;
+            const uint32_t half_m1 = ro > 0 ? (1u << (ro - 1)) - 1u : 0u;
+            const uint32_t mask = ro > 0 ? ~((1u << ro) - 1u) : ~0u;
             float acc[64];
 #pragma unroll
             for (int i = 0; i < 64; ++i) acc[i] = 0.0f;
@@ -342,7 +434,7 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
                 const uint32_t buf = cg & 1u;
                 // every lane waits; the warp proceeds only when all lanes saw the
                 // phase complete, reconverged for the .sync.aligned TMEM loads
-                const bool got = mbar_wait(bar_tfull + 8 * buf, (cg >> 1) & 1u, abort_flag, prm.status);
+                const bool got = mbar_wait(bar_tfull + 8 * buf, (cg >> 1) & 1u, abort_flag, status);
                 if (!__all_sync(0xFFFFFFFFu, got)) { ok = false; break; }
                 __syncwarp();
                 tc_fence_after();
@@ -359,21 +451,32 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
                 for (int i = 0; i < 32; ++i) acc[32 + i] = fold(acc[32 + i], __uint_as_float(r1[i]), ro, half_m1, mask);
             }
             if (!ok) break;
-            const int row = m0 + quarter * 32 + lane;
-            if (row < prm.M) {
-                float* drow = prm.D + (int64_t)row * prm.ldd + n0 + half * 64;
-                const int ncol = min(64, prm.N - (n0 + half * 64));
+            const int row = ti.m0 + quarter * 32 + lane;
+            if (row < ti.M && ti.img_L > 0) {
+                // conv2d output: walk (image, column-in-image) along the 64 columns
+                const int64_t col0 = ti.n0 + half * 64;
+                const int ncol = min(64, ti.N - (int)col0);
+                int64_t img = col0 / ti.img_L;
+                int64_t l = col0 - img * ti.img_L;
+#pragma unroll
+                for (int i = 0; i < 64; ++i) {
+                    if (i < ncol) ti.D[img * ti.img_stride + (int64_t)row * ti.ldd + l] = __fmul_rn(ti.alpha, acc[i]);
+                    if (++l == ti.img_L) { l = 0; ++img; }
+                }
+            } else if (row < ti.M) {
+                float* drow = ti.D + (int64_t)row * ti.ldd + ti.n0 + half * 64;
+                const int ncol = min(64, ti.N - (ti.n0 + half * 64));
                 if (ncol == 64 && ((reinterpret_cast<uintptr_t>(drow) & 15) == 0)) {
 #pragma unroll
                     for (int i = 0; i < 64; i += 4) {
-                        float4 v = make_float4(__fmul_rn(prm.alpha, acc[i]), __fmul_rn(prm.alpha, acc[i + 1]),
-                                               __fmul_rn(prm.alpha, acc[i + 2]), __fmul_rn(prm.alpha, acc[i + 3]));
+                        float4 v = make_float4(__fmul_rn(ti.alpha, acc[i]), __fmul_rn(ti.alpha, acc[i + 1]),
+                                               __fmul_rn(ti.alpha, acc[i + 2]), __fmul_rn(ti.alpha, acc[i + 3]));
                         *reinterpret_cast<float4*>(drow + i) = v;
                     }
                 } else {
 #pragma unroll
                     for (int i = 0; i < 64; ++i)
-                        if (i < ncol) drow[i] = __fmul_rn(prm.alpha, acc[i]);
+                        if (i < ncol) drow[i] = __fmul_rn(ti.alpha, acc[i]);
                 }
             }
         }
@@ -390,14 +493,36 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
     }
 }
 
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant__ CUtensorMap tm_alo,
+               const __grid_constant__ CUtensorMap tm_bhi, const __grid_constant__ CUtensorMap tm_blo,
+               TcParams prm) {
+    extern __shared__ uint8_t smem_raw[];
+    SingleSrc src;
+    src.m[0] = &tm_ahi;
+    src.m[1] = &tm_alo;
+    src.m[2] = &tm_bhi;
+    src.m[3] = &tm_blo;
+    src.prm = prm;
+    tc_body(src, prm.status, smem_raw);
+}
+
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+gemm_tc_grouped_kernel(const GroupHeader* __restrict__ h) {
+    extern __shared__ uint8_t smem_raw[];
+    GroupedSrc src{h};
+    tc_body(src, h->status, smem_raw);
+}
+
 // ---- operand split: FP32 -> K-major BF16 hi/lo, zero padded -----------------
-// Output rows [0, R) x cols [0, Kp) (bf16). Source element (r, k) is
-// src[r*ld + k] when kmajor, else src[k*ld + r]. Rows >= rows or k >= K are 0.
-__global__ void __launch_bounds__(256)
-split_bf16_kernel(const float* __restrict__ src, int64_t ld, int kmajor, int rows, int K, int R,
-                  int Kp, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
-    __shared__ float tile[32][65];
-    const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 64;
+// One 32-row x 64-k tile of an operand. Output rows [0, R) x cols [0, Kp)
+// (bf16). Source element (r, k) is src[r*ld + k] when kmajor, else
+// src[k*ld + r]. Rows >= rows or k >= K are 0. hi = RZ_bf16(x),
+// lo = RN_bf16(x - hi) (exact difference), lo = 0 for non-finite x.
+__device__ __forceinline__ void split_tile(const float* __restrict__ src, int64_t ld, int kmajor,
+                                           int rows, int K, int R, int Kp, __nv_bfloat16* hi,
+                                           __nv_bfloat16* lo, int tr, int tk, float (*tile)[65]) {
+    const int r0 = tr * 32, k0 = tk * 64;
     const int t = threadIdx.x;
     if (kmajor) {
         for (int i = t; i < 32 * 64; i += 256) {
@@ -413,32 +538,53 @@ split_bf16_kernel(const float* __restrict__ src, int64_t ld, int kmajor, int row
         }
     }
     __syncthreads();
-    for (int i = t; i < 32 * 32; i += 256) {
-        const int rr = i / 32, kp = (i % 32) * 2;
-        const int r = r0 + rr, k = k0 + kp;
-        if (r >= R || k >= Kp) continue;
-        __nv_bfloat162 h2, l2;
-        float x0 = tile[rr][kp], x1 = tile[rr][kp + 1];
-        __nv_bfloat16 h0 = __float2bfloat16_rz(x0), h1 = __float2bfloat16_rz(x1);
-        float d0 = x0 - __bfloat162float(h0), d1 = x1 - __bfloat162float(h1);
-        if (!isfinite(x0)) d0 = 0.0f;
-        if (!isfinite(x1)) d1 = 0.0f;
-        h2.x = h0;
-        h2.y = h1;
-        l2.x = __float2bfloat16_rn(d0);
-        l2.y = __float2bfloat16_rn(d1);
-        *reinterpret_cast<__nv_bfloat162*>(hi + (int64_t)r * Kp + k) = h2;
-        *reinterpret_cast<__nv_bfloat162*>(lo + (int64_t)r * Kp + k) = l2;
+    split_store_tile(tile, r0, k0, R, Kp, hi, lo);
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256)
+split_bf16_kernel(const float* __restrict__ src, int64_t ld, int kmajor, int rows, int K, int R,
+                  int Kp, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+    __shared__ float tile[32][65];
+    split_tile(src, ld, kmajor, rows, K, R, Kp, hi, lo, blockIdx.y, blockIdx.x, tile);
+}
+
+// All operands of a grouped launch: items are 32 x 64 tiles, walked
+// grid-stride; each finds its operand by binary search over item_begin.
+__global__ void __launch_bounds__(256)
+split_grouped_kernel(const GroupHeader* __restrict__ h) {
+    __shared__ float tile[32][65];
+    __shared__ SplitRow row;
+    const SplitRow* rows = reinterpret_cast<const SplitRow*>(
+        reinterpret_cast<const uint8_t*>(h) + h->splits_off);
+    const int nrows = h->nsplit;
+    // the device status word starts every launch cleared (this kernel runs
+    // first on the stream; the GEMM kernel only ever sets it)
+    if (blockIdx.x == 0 && threadIdx.x == 0) *h->status = 0;
+    for (int64_t item = blockIdx.x; item < h->split_items; item += gridDim.x) {
+        if (threadIdx.x == 0) {
+            int lo = 0, hi = nrows - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (rows[mid].item_begin <= item) lo = mid;
+                else hi = mid - 1;
+            }
+            row = rows[lo];
+        }
+        __syncthreads();
+        const SplitRow r = row;
+        __syncthreads();
+        const int64_t local = item - r.item_begin;
+        const int tiles_k = r.Kp / 64;
+        split_tile(r.src, r.ld, r.kmajor, r.rows, r.K, r.R, r.Kp, r.hi, r.lo,
+                   (int)(local / tiles_k), (int)(local % tiles_k), tile);
     }
 }
 
 // ---- host side ---------------------------------------------------------------
-struct WsLayout {
-    size_t status, ahi, alo, bhi, blo, total;
-    int Mp, Np, Kp;
-};
-
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
 
 WsLayout ws_layout(int M, int N, int K) {
     WsLayout w;
@@ -454,6 +600,8 @@ WsLayout ws_layout(int M, int N, int K) {
     w.total = align_up(w.blo + b, 1024);
     return w;
 }
+
+namespace {
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -517,7 +665,18 @@ int launch_gemm_tc(const float* A, int64_t lda, int ta, const float* B, int64_t 
     if (rc) return rc;
     split_bf16_kernel<<<dim3(w.Kp / 64, w.Np / 32), sb, 0, st>>>(B, ldb, tb ? 1 : 0, N, K, w.Np, w.Kp, bhi, blo);
     if ((rc = check_launch("split_bf16_kernel(B)"))) return rc;
+    return launch_tc_presplit(ws, w, D, ldd, M, N, mbits, alpha, chunk, 0, 0, stream);
+}
 
+int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int M, int N,
+                       int mbits, float alpha, int chunk, int64_t img_L, int64_t img_stride,
+                       void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto* ahi = reinterpret_cast<__nv_bfloat16*>(ws + w.ahi);
+    auto* alo = reinterpret_cast<__nv_bfloat16*>(ws + w.alo);
+    auto* bhi = reinterpret_cast<__nv_bfloat16*>(ws + w.bhi);
+    auto* blo = reinterpret_cast<__nv_bfloat16*>(ws + w.blo);
+    int rc;
     CUtensorMap m_ahi, m_alo, m_bhi, m_blo;
     if ((rc = make_map(&m_ahi, ahi, w.Mp, w.Kp))) return rc;
     if ((rc = make_map(&m_alo, alo, w.Mp, w.Kp))) return rc;
@@ -535,13 +694,15 @@ int launch_gemm_tc(const float* A, int64_t lda, int ta, const float* B, int64_t 
     p.chunk16 = chunk / 16;
     p.ro = 23 - mbits;
     p.alpha = alpha;
-    p.status = status;
+    p.status = reinterpret_cast<int*>(ws + w.status);
+    p.img_L = img_L;
+    p.img_stride = img_stride;
 
     int dev = 0;
     cudaGetDevice(&dev);
     static bool attr_set[64] = {false};
     if (dev < 0 || dev >= 64 || !attr_set[dev]) {
-        e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+        cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
         if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
         if (dev >= 0 && dev < 64) attr_set[dev] = true;
     }
@@ -618,3 +779,205 @@ extern "C" int lofgb_gemm_tc_noalloc_f32(const float* A, int64_t lda, int trans_
                           LOFGB_RNE, alpha, LOFGB_GEMM_TC, chunk, scratch,
                           scratch ? NOALLOC_SCRATCH_BYTES : 0, stream);
 }
+
+// ---- grouped launch: host side -----------------------------------------------
+#include <algorithm>
+#include <vector>
+
+namespace lofgb {
+namespace {
+
+struct GroupLayout {
+    size_t ws_total;
+    std::vector<size_t> ahi, alo, bhi, blo;
+    std::vector<int> Mp, Np, Kp;
+    int64_t tiles = 0, split_items = 0;
+    size_t rows_off, tiles_off, splits_off, table_total;
+};
+
+int check_task(const lofgb_gemm_task& t, int i) {
+    if (t.M < 0 || t.N < 0 || t.K < 0)
+        return set_error(LOFGB_ERR_SIZE, "task %d: negative dimension", i);
+    if ((t.trans_a != 0 && t.trans_a != 1) || (t.trans_b != 0 && t.trans_b != 1))
+        return set_error(LOFGB_ERR_SIZE, "task %d: trans flags must be 0 or 1", i);
+    if (t.M && t.N && !t.D) return set_error(LOFGB_ERR_NULL, "task %d: D is NULL", i);
+    if (t.M && t.N && t.K && (!t.A || !t.B)) return set_error(LOFGB_ERR_NULL, "task %d: A or B is NULL", i);
+    if (t.lda < (t.trans_a ? t.M : t.K) || t.lda < 1 || t.ldb < (t.trans_b ? t.K : t.N) || t.ldb < 1 ||
+        t.ldd < t.N || t.ldd < 1)
+        return set_error(LOFGB_ERR_SIZE, "task %d: leading dimension too small", i);
+    if (t.accum_mant_bits < 0 || t.accum_mant_bits > 23)
+        return set_error(LOFGB_ERR_FORMAT, "task %d: accum_mant_bits %d outside [0, 23]", i, t.accum_mant_bits);
+    if (t.chunk <= 0 || t.chunk % 16 != 0 || t.chunk > 256)
+        return set_error(LOFGB_ERR_SIZE, "task %d: chunk %d must be a multiple of 16 in [16, 256]", i, t.chunk);
+    if (t.M > 0 && t.N > 0 && t.K == 0)
+        return set_error(LOFGB_ERR_UNSUPPORTED, "task %d: K == 0 in a grouped launch", i);
+    return LOFGB_OK;
+}
+
+GroupLayout group_layout(const lofgb_gemm_task* tasks, int n) {
+    GroupLayout g;
+    size_t off = 1024;  // status word
+    for (int i = 0; i < n; ++i) {
+        const lofgb_gemm_task& t = tasks[i];
+        const bool empty = t.M <= 0 || t.N <= 0 || t.K <= 0;
+        const int Mp = empty ? 0 : (int)align_up((size_t)t.M, TBM);
+        const int Np = empty ? 0 : (int)align_up((size_t)t.N, TBN);
+        const int Kp = empty ? 0 : (int)align_up((size_t)t.K, SK);
+        g.Mp.push_back(Mp);
+        g.Np.push_back(Np);
+        g.Kp.push_back(Kp);
+        const size_t a = (size_t)Mp * Kp * 2, b = (size_t)Np * Kp * 2;
+        g.ahi.push_back(off); off = align_up(off + a, 1024);
+        g.alo.push_back(off); off = align_up(off + a, 1024);
+        g.bhi.push_back(off); off = align_up(off + b, 1024);
+        g.blo.push_back(off); off = align_up(off + b, 1024);
+        g.tiles += (int64_t)(Mp / TBM) * (Np / TBN);
+        g.split_items += (int64_t)(Mp / 32) * (Kp / 64) + (int64_t)(Np / 32) * (Kp / 64);
+    }
+    g.ws_total = off;
+    g.rows_off = align_up(sizeof(GroupHeader), 256);
+    g.tiles_off = align_up(g.rows_off + sizeof(GroupRow) * (size_t)n, 256);
+    g.splits_off = align_up(g.tiles_off + sizeof(TileRef) * (size_t)g.tiles, 256);
+    g.table_total = align_up(g.splits_off + sizeof(SplitRow) * (size_t)(2 * n), 256);
+    return g;
+}
+
+}  // namespace
+}  // namespace lofgb
+
+using namespace lofgb;
+
+extern "C" {
+
+size_t lofgb_gemm_grouped_workspace_size(const lofgb_gemm_task* tasks, int ntasks) {
+    if (!tasks || ntasks <= 0) return 0;
+    return group_layout(tasks, ntasks).ws_total;
+}
+
+size_t lofgb_gemm_grouped_table_size(const lofgb_gemm_task* tasks, int ntasks) {
+    if (!tasks || ntasks <= 0) return 0;
+    return group_layout(tasks, ntasks).table_total;
+}
+
+int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* workspace,
+                               size_t workspace_bytes, int schedule, int grid, void* table,
+                               size_t table_bytes, int64_t* num_tiles, int64_t* split_items) {
+    if (ntasks <= 0) return set_error(LOFGB_ERR_SIZE, "need at least one task");
+    if (!tasks || !table || !workspace || !num_tiles || !split_items)
+        return set_error(LOFGB_ERR_NULL, "NULL tasks, workspace, table or output count");
+    if (schedule < 0 || schedule > 2) return set_error(LOFGB_ERR_UNSUPPORTED, "schedule %d", schedule);
+    for (int i = 0; i < ntasks; ++i) {
+        const int st = check_task(tasks[i], i);
+        if (st) return st;
+    }
+    const GroupLayout g = group_layout(tasks, ntasks);
+    if (workspace_bytes < g.ws_total || (reinterpret_cast<uintptr_t>(workspace) & 255))
+        return set_error(LOFGB_ERR_WORKSPACE, "need %zu bytes of 256-byte aligned workspace", g.ws_total);
+    if (table_bytes < g.table_total)
+        return set_error(LOFGB_ERR_WORKSPACE, "table needs %zu bytes", g.table_total);
+    if (grid <= 0) grid = sm_count();
+    uint8_t* tb = static_cast<uint8_t*>(table);
+    memset(tb, 0, g.table_total);
+    uint8_t* ws = static_cast<uint8_t*>(workspace);
+    GroupHeader* h = reinterpret_cast<GroupHeader*>(tb);
+    h->ntasks = ntasks;
+    h->ntiles = (int32_t)g.tiles;
+    h->nsplit = 2 * ntasks;
+    h->split_items = g.split_items;
+    h->rows_off = (int64_t)g.rows_off;
+    h->tiles_off = (int64_t)g.tiles_off;
+    h->splits_off = (int64_t)g.splits_off;
+    h->status = reinterpret_cast<int*>(ws);
+    GroupRow* rows = reinterpret_cast<GroupRow*>(tb + g.rows_off);
+    SplitRow* splits = reinterpret_cast<SplitRow*>(tb + g.splits_off);
+    struct Cand { int32_t task, m0, n0; int64_t cost; };
+    std::vector<Cand> cands;
+    cands.reserve((size_t)g.tiles);
+    int64_t item = 0;
+    for (int i = 0; i < ntasks; ++i) {
+        const lofgb_gemm_task& t = tasks[i];
+        GroupRow& r = rows[i];
+        auto* ahi = reinterpret_cast<__nv_bfloat16*>(ws + g.ahi[i]);
+        auto* alo = reinterpret_cast<__nv_bfloat16*>(ws + g.alo[i]);
+        auto* bhi = reinterpret_cast<__nv_bfloat16*>(ws + g.bhi[i]);
+        auto* blo = reinterpret_cast<__nv_bfloat16*>(ws + g.blo[i]);
+        r.D = t.D;
+        r.ldd = t.ldd;
+        r.M = t.M;
+        r.N = t.N;
+        r.Kp = g.Kp[i];
+        r.chunk16 = t.chunk / 16;
+        r.ro = 23 - t.accum_mant_bits;
+        r.alpha = t.alpha;
+        SplitRow& sa = splits[2 * i];
+        SplitRow& sbr = splits[2 * i + 1];
+        sa.src = t.A; sa.ld = t.lda; sa.kmajor = t.trans_a ? 0 : 1; sa.rows = t.M; sa.K = t.K;
+        sa.R = g.Mp[i]; sa.Kp = g.Kp[i]; sa.hi = ahi; sa.lo = alo; sa.item_begin = item;
+        item += (int64_t)(g.Mp[i] / 32) * (g.Kp[i] / 64);
+        sbr.src = t.B; sbr.ld = t.ldb; sbr.kmajor = t.trans_b ? 1 : 0; sbr.rows = t.N; sbr.K = t.K;
+        sbr.R = g.Np[i]; sbr.Kp = g.Kp[i]; sbr.hi = bhi; sbr.lo = blo; sbr.item_begin = item;
+        item += (int64_t)(g.Np[i] / 32) * (g.Kp[i] / 64);
+        if (g.Mp[i] == 0 || g.Np[i] == 0 || g.Kp[i] == 0) continue;
+        int rc;
+        if ((rc = make_map(&r.map[0], ahi, g.Mp[i], g.Kp[i]))) return rc;
+        if ((rc = make_map(&r.map[1], alo, g.Mp[i], g.Kp[i]))) return rc;
+        if ((rc = make_map(&r.map[2], bhi, g.Np[i], g.Kp[i]))) return rc;
+        if ((rc = make_map(&r.map[3], blo, g.Np[i], g.Kp[i]))) return rc;
+        const int nchunks = (g.Kp[i] / 16 + r.chunk16 - 1) / r.chunk16;
+        const int64_t cost = 4 * (int64_t)nchunks + g.Kp[i] / SK;
+        for (int mt = 0; mt < g.Mp[i] / TBM; ++mt)
+            for (int nt = 0; nt < g.Np[i] / TBN; ++nt) cands.push_back({i, mt * TBM, nt * TBN, cost});
+    }
+    if (schedule >= 1)
+        std::stable_sort(cands.begin(), cands.end(),
+                         [](const Cand& a, const Cand& b) { return a.cost > b.cost; });
+    TileRef* tl = reinterpret_cast<TileRef*>(tb + g.tiles_off);
+    const int64_t nt = (int64_t)cands.size();
+    for (int64_t pidx = 0; pidx < nt; ++pidx) {
+        int64_t src_idx = pidx;
+        if (schedule == 2) {  // boustrophedon deal: odd rounds run the CTAs backwards
+            const int64_t round = pidx / grid, c = pidx % grid;
+            const int64_t base = round * grid;
+            const int64_t width = std::min<int64_t>(grid, nt - base);
+            src_idx = (round & 1) ? base + (width - 1 - c) : pidx;
+            if (src_idx >= nt) src_idx = pidx;
+        }
+        tl[pidx] = TileRef{cands[src_idx].task, cands[src_idx].m0, cands[src_idx].n0, 0};
+    }
+    *num_tiles = nt;
+    *split_items = g.split_items;
+    return LOFGB_OK;
+}
+
+int lofgb_gemm_grouped_launch(const void* device_table, int64_t num_tiles, int64_t split_items,
+                              int grid, void* stream) {
+    if (!device_table) return set_error(LOFGB_ERR_NULL, "NULL device table");
+    if ((reinterpret_cast<uintptr_t>(device_table) & 255) != 0)
+        return set_error(LOFGB_ERR_WORKSPACE, "device table must be 256-byte aligned");
+    if (num_tiles < 0 || split_items < 0) return set_error(LOFGB_ERR_SIZE, "negative count");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const auto* h = static_cast<const GroupHeader*>(device_table);
+    if (split_items > 0) {
+        const int64_t maxg = (int64_t)sm_count() * 8;
+        const int sg = (int)std::min<int64_t>(split_items, maxg);
+        split_grouped_kernel<<<sg, 256, 0, st>>>(h);
+        const int rc = check_launch("split_grouped_kernel");
+        if (rc) return rc;
+    }
+    if (num_tiles == 0) return LOFGB_OK;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    static bool attr_set[64] = {false};
+    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(gemm_tc_grouped_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+        if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
+        if (dev >= 0 && dev < 64) attr_set[dev] = true;
+    }
+    if (grid <= 0) grid = sm_count();
+    if (grid > num_tiles) grid = (int)num_tiles;
+    gemm_tc_grouped_kernel<<<grid, NUM_THREADS, SMEM_BYTES, st>>>(h);
+    return check_launch("gemm_tc_grouped_kernel");
+}
+
+}  // extern "C"

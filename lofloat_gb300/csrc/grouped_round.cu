@@ -30,7 +30,7 @@ __device__ __forceinline__ uint32_t elem(uint32_t w, const GroupedTask& t, uint6
     return vr_format<MODE, 32>(w, t.plan, r);
 }
 
-template <int MODE>
+template <int MODE, int UNI>
 __device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
     const bool aligned =
         ((reinterpret_cast<uintptr_t>(t.in) | reinterpret_cast<uintptr_t>(t.out)) & 15) == 0 &&
@@ -50,7 +50,12 @@ __device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
                 if (t.apply_scale) w[q] = __float_as_uint(__fmul_rn(t.scale, __uint_as_float(w[q])));
                 r[q] = mode_is_stochastic(mode) ? rng64(t.seed, t.offset + i + q) : 0ull;
             }
-            vr_format_f32x4<MODE>(w, t.plan, r);
+            if constexpr (UNI != 0) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) w[q] = vr_uni_f32<MODE, UNI>(w[q], t.plan);
+            } else {
+                vr_format_f32x4<MODE>(w, t.plan, r);
+            }
             __stcs(vout + v, make_uint4(w[0], w[1], w[2], w[3]));
         }
         for (int64_t i = (v1 << 2) + threadIdx.x; i < e1; i += GT) {
@@ -83,12 +88,22 @@ grouped_round_kernel(const GroupedTask* __restrict__ tasks, int ntasks, int64_t 
         __syncthreads();
         const int64_t e0 = (item - t.item_begin) * GROUPED_ITEM;
         const int64_t e1 = min(e0 + GROUPED_ITEM, t.n);
+        // uni is 1 only for RNE and 2 only for RTZ / RAFZ / RU / RD
         switch (t.plan.mode) {
-        case LOFGB_RNE: run_item<LOFGB_RNE>(t, e0, e1); break;
-        case LOFGB_RTZ: run_item<LOFGB_RTZ>(t, e0, e1); break;
-        case LOFGB_RTO: run_item<LOFGB_RTO>(t, e0, e1); break;
-        case LOFGB_SR_A: run_item<LOFGB_SR_A>(t, e0, e1); break;
-        default: run_item<-1>(t, e0, e1); break;
+        case LOFGB_RNE:
+            if (t.plan.uni) run_item<LOFGB_RNE, 1>(t, e0, e1);
+            else run_item<LOFGB_RNE, 0>(t, e0, e1);
+            break;
+        case LOFGB_RTZ:
+            if (t.plan.uni) run_item<LOFGB_RTZ, 2>(t, e0, e1);
+            else run_item<LOFGB_RTZ, 0>(t, e0, e1);
+            break;
+        case LOFGB_RTO: run_item<LOFGB_RTO, 0>(t, e0, e1); break;
+        case LOFGB_SR_A: run_item<LOFGB_SR_A, 0>(t, e0, e1); break;
+        default:
+            if (t.plan.uni) run_item<-1, 2>(t, e0, e1);
+            else run_item<-1, 0>(t, e0, e1);
+            break;
         }
     }
 }

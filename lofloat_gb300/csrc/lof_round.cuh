@@ -199,7 +199,12 @@ __device__ __forceinline__ typename Src<W>::U vr_normal(typename Src<W>::U x, co
     using U = typename S::U;
     using T = typename std::conditional<(W <= 32), uint32_t, uint64_t>::type;
     U t = x;
-    if (p.d > 0) t = round_mantissa<MODE, W, U>(x, p.d, p.mode, p.len, (x & S::SIGN) == 0, r);
+    if (MODE == LOFGB_RNE) {
+        // d >= 1 whenever any bit is dropped; d == 0 leaves x unchanged
+        if (p.d > 0) t = x + ((x >> p.d) & U(1)) + ((U(1) << (p.d - 1)) - U(1));
+    } else if (p.d > 0) {
+        t = round_mantissa<MODE, W, U>(x, p.d, p.mode, p.len, (x & S::SIGN) == 0, r);
+    }
     U res = t & (U)p.keep_mask;
     if ((T)(res & (S::SIGN - U(1))) >= (T)p.ovf_thr) res = p.saturating ? x : S::PINF;
     return res;
@@ -222,10 +227,9 @@ __device__ __forceinline__ bool vr_is_special(typename Src<W>::U x, const RoundP
 // reference treats them as exponent -127 with an implicit 1) and NaN keep the
 // exact integer path.
 template <int MODE>
-__device__ __forceinline__ uint32_t vr_special_f32(uint32_t x, const RoundPlan& p, uint64_t r) {
-    if (p.grid == 0) return vr_special<MODE, 32>(x, p, r);
-    const uint32_t sign = x & 0x80000000u, mag = x & 0x7FFFFFFFu;
-    const float a = __uint_as_float(mag);
+__device__ __forceinline__ uint32_t vr_grid_f32(uint32_t x, const RoundPlan& p) {
+    const uint32_t sign = x & 0x80000000u;
+    const float a = fabsf(__uint_as_float(x));
     float s;
     if (p.grid == 1) {
         s = __fadd_rn(a, p.grid_c);
@@ -233,9 +237,27 @@ __device__ __forceinline__ uint32_t vr_special_f32(uint32_t x, const RoundPlan& 
         const bool up = sign ? p.grid_up_neg : p.grid_up_pos;
         s = up ? __fadd_ru(a, p.grid_c) : __fadd_rz(a, p.grid_c);
     }
-    uint32_t res = __float_as_uint(__fsub_rn(s, p.grid_c)) | sign;
-    const bool exact_path = (mag < 0x00800000u && mag >= (uint32_t)p.tiny_thr) || mag > 0x7F800000u;
-    return exact_path ? vr_special<MODE, 32>(x, p, r) : res;
+    return __float_as_uint(__fsub_rn(s, p.grid_c)) | sign;
+}
+
+// True when the float grid does not reproduce the reference: FP32-subnormal
+// inputs in the target-subnormal branch (the reference treats them as
+// exponent -127 with an implicit 1), and NaN.
+__device__ __forceinline__ bool vr_grid_exception(uint32_t x, const RoundPlan& p) {
+    const uint32_t mag = x & 0x7FFFFFFFu;
+    return (mag < 0x00800000u && mag >= (uint32_t)p.tiny_thr) || mag > 0x7F800000u;
+}
+
+template <int MODE>
+__device__ __forceinline__ uint32_t vr_special_f32(uint32_t x, const RoundPlan& p, uint64_t r) {
+    if (p.grid == 0) return vr_special<MODE, 32>(x, p, r);
+    const uint32_t g = vr_grid_f32<MODE>(x, p);
+    const bool ex = vr_grid_exception(x, p);
+    if (__any_sync(__activemask(), ex)) {
+        const uint32_t e = vr_special<MODE, 32>(x, p, r);
+        return ex ? e : g;
+    }
+    return g;
 }
 
 // virtual_round(x, params, ps), src/lo_float.h:2843-2939, on one source word.
@@ -247,13 +269,29 @@ __device__ __forceinline__ typename Src<W>::U vr_format(typename Src<W>::U x, co
     else return vr_special<MODE, W>(x, p, r);
 }
 
+// One f32 word per lane, rare branches under a warp vote instead of a
+// divergent branch (for values computed once per lane, like an MX scale).
+template <int MODE>
+__device__ __forceinline__ uint32_t vr_format_f32_voted(uint32_t x, const RoundPlan& p,
+                                                        uint64_t r) {
+    uint32_t res = vr_normal<MODE, 32>(x, p, r);
+    const bool sp = vr_is_special<32>(x, p);
+    if (__any_sync(__activemask(), sp)) {
+        const uint32_t s = vr_special_f32<MODE>(x, p, r);
+        res = sp ? s : res;
+    }
+    return res;
+}
+
 // Four f32 words at once: the common case for all four, then one warp vote
 // decides whether any lane of the warp needs the rare branches; if so they
 // run for all four words and are selected per word. `r` holds the four
 // random words (zeros for deterministic modes).
-template <int MODE>
+template <int MODE, bool FULL = false>
 __device__ __forceinline__ void vr_format_f32x4(uint32_t (&w)[4], const RoundPlan& p,
                                                 const uint64_t (&r)[4]) {
+    // FULL: the caller guarantees all 32 lanes are here (no __activemask())
+    const unsigned mask = FULL ? 0xFFFFFFFFu : __activemask();
     uint32_t res[4];
     bool sp[4];
     bool any = false;
@@ -263,15 +301,61 @@ __device__ __forceinline__ void vr_format_f32x4(uint32_t (&w)[4], const RoundPla
         sp[q] = vr_is_special<32>(w[q], p);
         any |= sp[q];
     }
-    if (__any_sync(__activemask(), any)) {
+    if (__any_sync(mask, any)) {
+        if (p.grid == 0) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const uint32_t s = vr_special_f32<MODE>(w[q], p, r[q]);
-            res[q] = sp[q] ? s : res[q];
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t s = vr_special<MODE, 32>(w[q], p, r[q]);
+                res[q] = sp[q] ? s : res[q];
+            }
+        } else {
+            bool ex[4];
+            bool any_ex = false;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t g = vr_grid_f32<MODE>(w[q], p);
+                res[q] = sp[q] ? g : res[q];
+                ex[q] = sp[q] && vr_grid_exception(w[q], p);
+                any_ex |= ex[q];
+            }
+            if (__any_sync(mask, any_ex)) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t e = vr_special<MODE, 32>(w[q], p, r[q]);
+                    res[q] = ex[q] ? e : res[q];
+                }
+            }
         }
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) w[q] = res[q];
+}
+
+// virtual_round(x, params, ps) of an f32 word by float arithmetic over the
+// whole range (RoundPlan::uni; UNI = 1 round to nearest even, 2 directed).
+// C = 2^(clamp(e, to_min, hi) + d) puts the target's spacing at |x| in the
+// last place of C, so one fadd in the mode's direction and one exact fsub
+// give the rounded magnitude — the normal branch (src/lo_float.h:2925-2933),
+// the target-subnormal grid (:2915-2923) and the tiny branch (:2872-2908)
+// alike. Then the overflow rule (:2935-2936) and NaN -> quiet NaN (:2869).
+template <int MODE, int UNI>
+__device__ __forceinline__ uint32_t vr_uni_f32(uint32_t x, const RoundPlan& p) {
+    const uint32_t cb = min(max(x & 0x7F800000u, p.uni_lo), p.uni_hi) + p.uni_d;
+    const float c = __uint_as_float(cb);
+    const float a = fabsf(__uint_as_float(x));
+    float s;
+    if (UNI == 1) {
+        s = __fadd_rn(a, c);
+    } else if (MODE == LOFGB_RTZ) {
+        s = __fadd_rz(a, c);
+    } else {
+        const bool up = (x & 0x80000000u) ? p.grid_up_neg : p.grid_up_pos;
+        s = up ? __fadd_ru(a, c) : __fadd_rz(a, c);
+    }
+    const uint32_t r = __float_as_uint(__fsub_rn(s, c));
+    uint32_t res = r | (x & 0x80000000u);
+    res = r >= (uint32_t)p.ovf_thr ? ((x & p.sat_and) | p.sat_or) : res;
+    return (x & 0x7FFFFFFFu) > 0x7F800000u ? 0x7FC00000u : res;
 }
 
 // virtual_round(x, ToMantissaBits, ps), src/lo_float.h:2715-2756.

@@ -44,6 +44,19 @@ struct RoundPlan {
     int32_t grid;
     float grid_c;
     int32_t grid_up_pos, grid_up_neg;
+    // Whole-range float rounding of f32 words (uni = grid's 1 or 2, else 0):
+    // the per-element constant C = 2^(clamp(e, to_min, hi) + d), e the
+    // word's unbiased exponent, has ulp(C) equal to the target's spacing at
+    // |x| in the normal range as well as below it, so fadd(|x|, C) - C is the
+    // whole of virtual_round's rounding for RNE / RTZ / RAFZ / RU / RD. Valid
+    // when d >= 1, tiny >= 2^-126 (no FP32-subnormal input reaches the
+    // target-subnormal branch) and hi + d <= 254 with hi the FP32 exponent
+    // field just above the target's largest finite value (every |x| at or
+    // above 2^hi then still rounds to an overflow).
+    int32_t uni;
+    uint32_t uni_lo, uni_hi, uni_d;  // FP32 exponent fields, shifted to bit 23
+    uint32_t sat_and, sat_or;        // overflow result: (x & sat_and) | sat_or
+    int32_t pad2;
 };
 
 // Host side.
@@ -52,7 +65,24 @@ int make_round_plan(RoundPlan* p, const lofgb_format* f, int src_bits, int mode,
 int make_mantissa_plan(RoundPlan* p, int src_bits, int mbits, int mode, int len);
 int sm_count();
 int set_error(int status, const char* fmt, ...);
+void clear_error();
 int check_launch(const char* what);
+
+// Tensor-core GEMM workspace (gemm_tc.cu): a status word, then the BF16 hi /
+// lo splits of A (Mp x Kp) and B (Np x Kp), K-major and zero padded
+// (Mp, Np multiples of 128, Kp of 64), each 1024-byte aligned.
+struct WsLayout {
+    size_t status, ahi, alo, bhi, blo, total;
+    int Mp, Np, Kp;
+};
+WsLayout ws_layout(int M, int N, int K);
+// Runs the chunked tensor-core GEMM on operands already split into `ws`
+// (laid out by ws_layout) whose status word the caller has cleared.
+// img_L > 0 stores conv2d output: column j = img * img_L + l of row i goes to
+// D[img * img_stride + i * ldd + l].
+int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int M, int N,
+                       int mbits, float alpha, int chunk, int64_t img_L, int64_t img_stride,
+                       void* stream);
 
 // Kernel launchers (one translation unit each).
 int launch_round(int src_bits, bool fmt, const void* in, void* out, int64_t n,

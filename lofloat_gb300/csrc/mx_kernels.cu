@@ -62,7 +62,7 @@ __device__ __forceinline__ BlockScale block_scale(float amax, const RoundPlan& p
                                                   uint64_t seed, uint64_t blk_elem) {
     const float sin = __fmul_rn(amax, inv_pmn);
     const uint64_t r = stoch<SMODE>(ps.mode) ? rng64(seed ^ SCALE_SALT, blk_elem) : 0ull;
-    const uint32_t sb = vr_format<SMODE, 32>(__float_as_uint(sin), ps, r);
+    const uint32_t sb = vr_format_f32_voted<SMODE>(__float_as_uint(sin), ps, r);
     BlockScale b;
     b.scale = __uint_as_float(sb);
     b.pos = b.scale > 0.0f;
@@ -77,12 +77,14 @@ __device__ __forceinline__ BlockScale block_scale(float amax, const RoundPlan& p
 
 // Four elements of one block: q = x / scale (x * (1/scale) for power-of-two
 // scales, chosen once per warp), round, rescale; a block whose scale is not
-// positive gives +0 (src/mx_round.cuh:70-75).
-template <int EMODE>
+// positive gives +0 (src/mx_round.cuh:70-75). UNI != 0: the element format
+// takes the whole-range float rounding (RoundPlan::uni).
+template <int EMODE, bool FULL, int UNI>
 __device__ __forceinline__ float4 quant4(float4 x, const BlockScale& b, const RoundPlan& pe,
                                         uint64_t seed, uint64_t e) {
+    const unsigned mask = FULL ? 0xFFFFFFFFu : __activemask();
     float q[4] = {x.x, x.y, x.z, x.w};
-    if (__all_sync(__activemask(), b.pow2)) {
+    if (__all_sync(mask, b.pow2)) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) q[i] = __fmul_rn(q[i], b.inv);
     } else {
@@ -90,13 +92,18 @@ __device__ __forceinline__ float4 quant4(float4 x, const BlockScale& b, const Ro
         for (int i = 0; i < 4; ++i) q[i] = b.pow2 ? __fmul_rn(q[i], b.inv) : __fdiv_rn(q[i], b.scale);
     }
     uint32_t w[4];
-    uint64_t r[4];
+    if constexpr (UNI != 0) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        w[i] = __float_as_uint(q[i]);
-        r[i] = stoch<EMODE>(pe.mode) ? rng64(seed, e + i) : 0ull;
+        for (int i = 0; i < 4; ++i) w[i] = vr_uni_f32<EMODE, UNI>(__float_as_uint(q[i]), pe);
+    } else {
+        uint64_t r[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            w[i] = __float_as_uint(q[i]);
+            r[i] = stoch<EMODE>(pe.mode) ? rng64(seed, e + i) : 0ull;
+        }
+        vr_format_f32x4<EMODE, FULL>(w, pe, r);
     }
-    vr_format_f32x4<EMODE>(w, pe, r);
     float4 o;
     o.x = b.pos ? __fmul_rn(__uint_as_float(w[0]), b.scale) : 0.0f;
     o.y = b.pos ? __fmul_rn(__uint_as_float(w[1]), b.scale) : 0.0f;
@@ -106,7 +113,7 @@ __device__ __forceinline__ float4 quant4(float4 x, const BlockScale& b, const Ro
 }
 
 // BS: block size; VPT float4s per lane per block; L lanes per block.
-template <int BS, int EMODE, int SMODE, bool ALIGNED>
+template <int BS, int EMODE, int SMODE, bool ALIGNED, int UNI = 0>
 __global__ void __launch_bounds__(MT)
 mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, float inv_pmn,
           uint64_t seed, uint64_t offset) {
@@ -119,7 +126,36 @@ mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, fl
     const int64_t warp = ((int64_t)blockIdx.x * MT + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * MT) >> 5;
     const int64_t nslots = (n + SLOT - 1) / SLOT;
+    const int64_t full_slots = n / SLOT;  // slots entirely inside the tensor
     for (int64_t s0 = warp * U; s0 < nslots; s0 += nwarps * U) {
+        if (ALIGNED && s0 + U <= full_slots) {
+            // common case: U full slots, no bounds checks
+            float4 v[U][VPT];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int j = 0; j < VPT; ++j)
+                    v[u][j] = __ldcs(reinterpret_cast<const float4*>(in + (s0 + u) * SLOT + j * 128 + lane * 4));
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                float amax = 0.0f;
+#pragma unroll
+                for (int j = 0; j < VPT; ++j)
+                    amax = fmaxf(amax, fmaxf(fmaxf(fabsf(v[u][j].x), fabsf(v[u][j].y)),
+                                             fmaxf(fabsf(v[u][j].z), fabsf(v[u][j].w))));
+#pragma unroll
+                for (int off = L / 2; off > 0; off >>= 1)
+                    amax = fmaxf(amax, __shfl_xor_sync(0xFFFFFFFFu, amax, off));
+                const int64_t blk0 = (s0 + u) * SLOT + (int64_t)(lane / L) * BS;
+                const BlockScale b = block_scale<SMODE>(amax, ps, inv_pmn, seed, offset + blk0);
+#pragma unroll
+                for (int j = 0; j < VPT; ++j) {
+                    const int64_t e = (s0 + u) * SLOT + j * 128 + lane * 4;
+                    __stcs(reinterpret_cast<float4*>(out + e), quant4<EMODE, true, UNI>(v[u][j], b, pe, seed, offset + (uint64_t)e));
+                }
+            }
+            continue;
+        }
         float4 v[U][VPT];
 #pragma unroll
         for (int u = 0; u < U; ++u)
@@ -145,7 +181,7 @@ mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, fl
             for (int j = 0; j < VPT; ++j) {
                 const int64_t e = (s0 + u) * SLOT + j * 128 + lane * 4;
                 const uint64_t g = offset + (uint64_t)e;
-                store4<ALIGNED>(out, e, n, quant4<EMODE>(v[u][j], b, pe, seed, g));
+                store4<ALIGNED>(out, e, n, quant4<EMODE, false, UNI>(v[u][j], b, pe, seed, g));
             }
         }
     }
@@ -165,6 +201,8 @@ int launch_bs(const float* in, float* out, int64_t n, const RoundPlan& pe, const
     const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
     if (!aligned)
         mx_kernel<BS, -1, -1, false><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
+    else if (pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE && pe.uni == 1)
+        mx_kernel<BS, LOFGB_RNE, LOFGB_RNE, true, 1><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE)
         mx_kernel<BS, LOFGB_RNE, LOFGB_RNE, true><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (ps.mode == LOFGB_RNE)

@@ -35,12 +35,12 @@ __device__ __forceinline__ bool needs_rng(const RoundPlan& p) {
 
 // One source word: optional fused scale (in the source type, as
 // src/Lof_kernel.cu:40-41 and :52-53 do), then the rounding.
-template <int MODE, int W, bool FMT>
+template <int MODE, int W, bool FMT, bool SCALED = true>
 __device__ __forceinline__ typename Src<W>::U process(typename Src<W>::U w, const RoundPlan& p,
                                                       const ScaleArg& s, uint64_t seed,
                                                       uint64_t idx) {
     using U = typename Src<W>::U;
-    if (s.apply) {
+    if (SCALED && s.apply) {
         if constexpr (W == 32) {
             w = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w)));
         } else if constexpr (W == 64) {
@@ -55,7 +55,7 @@ __device__ __forceinline__ typename Src<W>::U process(typename Src<W>::U w, cons
     else return vr_mantissa<MODE, W>(w, p.d, p.mode, p.len, r);
 }
 
-template <int MODE, int W, bool FMT>
+template <int MODE, int W, bool FMT, bool SCALED, int UNI = 0>
 __global__ void __launch_bounds__(RT)
 round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
                  RoundPlan p, ScaleArg s, uint64_t seed, uint64_t offset) {
@@ -64,38 +64,48 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
     const int64_t nvec = n / EPV;
     const int64_t stride = (int64_t)gridDim.x * RT * RU;
     for (int64_t base = (int64_t)blockIdx.x * RT * RU; base < nvec; base += stride) {
+        const bool full = base + RT * RU <= nvec;  // CTA-uniform: no per-vector checks
         uint4 v[RU];
 #pragma unroll
         for (int u = 0; u < RU; ++u) {
             const int64_t vi = base + u * RT + threadIdx.x;
-            if (vi < nvec) v[u] = __ldcs(vin + vi);
+            if (full || vi < nvec) v[u] = __ldcs(vin + vi);
         }
 #pragma unroll
         for (int u = 0; u < RU; ++u) {
             const int64_t vi = base + u * RT + threadIdx.x;
-            if (vi >= nvec) continue;
+            if (!full && vi >= nvec) continue;
             const uint64_t e0 = offset + (uint64_t)vi * EPV;
             uint4 o;
-            if constexpr (W == 32 && FMT) {
+            if constexpr (W == 32 && FMT && UNI != 0) {
+                uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
+                    w[q] = vr_uni_f32<MODE, UNI>(w[q], p);
+                }
+                o = make_uint4(w[0], w[1], w[2], w[3]);
+            } else if constexpr (W == 32 && FMT) {
                 uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
                 uint64_t r[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    if (s.apply) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
+                    if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
                     r[q] = needs_rng<MODE>(p) ? rng64(seed, e0 + q) : 0ull;
                 }
-                vr_format_f32x4<MODE>(w, p, r);
+                if (full) vr_format_f32x4<MODE, true>(w, p, r);
+                else vr_format_f32x4<MODE, false>(w, p, r);
                 o = make_uint4(w[0], w[1], w[2], w[3]);
             } else if constexpr (W == 32) {
-                o.x = process<MODE, 32, FMT>(v[u].x, p, s, seed, e0 + 0);
-                o.y = process<MODE, 32, FMT>(v[u].y, p, s, seed, e0 + 1);
-                o.z = process<MODE, 32, FMT>(v[u].z, p, s, seed, e0 + 2);
-                o.w = process<MODE, 32, FMT>(v[u].w, p, s, seed, e0 + 3);
+                o.x = process<MODE, 32, FMT, SCALED>(v[u].x, p, s, seed, e0 + 0);
+                o.y = process<MODE, 32, FMT, SCALED>(v[u].y, p, s, seed, e0 + 1);
+                o.z = process<MODE, 32, FMT, SCALED>(v[u].z, p, s, seed, e0 + 2);
+                o.w = process<MODE, 32, FMT, SCALED>(v[u].w, p, s, seed, e0 + 3);
             } else if constexpr (W == 64) {
                 const uint64_t a = ((uint64_t)v[u].y << 32) | v[u].x;
                 const uint64_t b = ((uint64_t)v[u].w << 32) | v[u].z;
-                const uint64_t ra = process<MODE, 64, FMT>(a, p, s, seed, e0 + 0);
-                const uint64_t rb = process<MODE, 64, FMT>(b, p, s, seed, e0 + 1);
+                const uint64_t ra = process<MODE, 64, FMT, SCALED>(a, p, s, seed, e0 + 0);
+                const uint64_t rb = process<MODE, 64, FMT, SCALED>(b, p, s, seed, e0 + 1);
                 o.x = (uint32_t)ra;
                 o.y = (uint32_t)(ra >> 32);
                 o.z = (uint32_t)rb;
@@ -105,8 +115,8 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
                 uint32_t out4[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    const U lo = process<MODE, 16, FMT>(in4[q] & 0xFFFFu, p, s, seed, e0 + 2 * q);
-                    const U hi = process<MODE, 16, FMT>(in4[q] >> 16, p, s, seed, e0 + 2 * q + 1);
+                    const U lo = process<MODE, 16, FMT, SCALED>(in4[q] & 0xFFFFu, p, s, seed, e0 + 2 * q);
+                    const U hi = process<MODE, 16, FMT, SCALED>(in4[q] >> 16, p, s, seed, e0 + 2 * q + 1);
                     out4[q] = (lo & 0xFFFFu) | (hi << 16);
                 }
                 o = make_uint4(out4[0], out4[1], out4[2], out4[3]);
@@ -120,15 +130,15 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
             if constexpr (W == 32) {
                 const uint32_t w = reinterpret_cast<const uint32_t*>(vin)[i];
                 reinterpret_cast<uint32_t*>(vout)[i] =
-                    process<MODE, 32, FMT>(w, p, s, seed, offset + i);
+                    process<MODE, 32, FMT, SCALED>(w, p, s, seed, offset + i);
             } else if constexpr (W == 64) {
                 const uint64_t w = reinterpret_cast<const uint64_t*>(vin)[i];
                 reinterpret_cast<uint64_t*>(vout)[i] =
-                    process<MODE, 64, FMT>(w, p, s, seed, offset + i);
+                    process<MODE, 64, FMT, SCALED>(w, p, s, seed, offset + i);
             } else {
                 const uint32_t w = reinterpret_cast<const uint16_t*>(vin)[i];
                 reinterpret_cast<uint16_t*>(vout)[i] =
-                    (uint16_t)process<MODE, 16, FMT>(w, p, s, seed, offset + i);
+                    (uint16_t)process<MODE, 16, FMT, SCALED>(w, p, s, seed, offset + i);
             }
         }
     }
@@ -172,13 +182,31 @@ int launch_w(const void* in, void* out, int64_t n, const RoundPlan& p, const Sca
     const int grid = (int)(g < maxg ? g : maxg);
     auto vi = static_cast<const uint4*>(in);
     auto vo = static_cast<uint4*>(out);
-    switch (p.mode) {
-    case LOFGB_RNE: round_vec_kernel<LOFGB_RNE, W, FMT><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset); break;
-    case LOFGB_RTZ: round_vec_kernel<LOFGB_RTZ, W, FMT><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset); break;
-    case LOFGB_RTO: round_vec_kernel<LOFGB_RTO, W, FMT><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset); break;
-    case LOFGB_SR_A: round_vec_kernel<LOFGB_SR_A, W, FMT><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset); break;
-    default: round_vec_kernel<-1, W, FMT><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset); break;
+#define LOFGB_RVU(M, UNI)                                                                    \
+    (s.apply ? round_vec_kernel<M, W, FMT, true, UNI><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset) \
+             : round_vec_kernel<M, W, FMT, false, UNI><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset))
+#define LOFGB_RV(M) LOFGB_RVU(M, 0)
+    if constexpr (W == 32 && FMT) {
+        // whole-range float rounding: RNE (uni 1) or the directed modes (uni 2)
+        if (p.uni == 1) {
+            LOFGB_RVU(LOFGB_RNE, 1);
+            return check_launch("round_vec_kernel");
+        }
+        if (p.uni == 2) {
+            if (p.mode == LOFGB_RTZ) LOFGB_RVU(LOFGB_RTZ, 2);
+            else LOFGB_RVU(-1, 2);
+            return check_launch("round_vec_kernel");
+        }
     }
+    switch (p.mode) {
+    case LOFGB_RNE: LOFGB_RV(LOFGB_RNE); break;
+    case LOFGB_RTZ: LOFGB_RV(LOFGB_RTZ); break;
+    case LOFGB_RTO: LOFGB_RV(LOFGB_RTO); break;
+    case LOFGB_SR_A: LOFGB_RV(LOFGB_SR_A); break;
+    default: LOFGB_RV(-1); break;
+    }
+#undef LOFGB_RV
+#undef LOFGB_RVU
     return check_launch("round_vec_kernel");
 }
 

@@ -736,3 +736,100 @@ int orc_gemm_chunked_f32(const float* A, int64_t lda, int ta, const float* B,
     }
     return 0;
 }
+
+/* ---- conv2d ------------------------------------------------------------------
+ * The per-MAC leaf of orc_gemm_f32 over the conv reduction. CRS order: the
+ * reference's default LoF_Conv2d path unfolds the input (F.unfold: rows
+ * ordered c, then r, then s) and calls lof_gemm(w.view(K, -1), x_col[n])
+ * (LoFloat/layers.py:690-705), i.e. rto_fma(w, x, acc) in that row order, with
+ * +0 in the padded positions. TILED8 order: lof_conv2d runs CUTLASS's analytic
+ * fprop implicit GEMM (src/cutlass_conv.cuh:78-98, TbK = 8), whose activation
+ * and filter iterators advance s, then r, then the 8-channel tile, while the
+ * SIMT leaf walks the 8 channels of a tile in order; channels >= C load 0 in
+ * both operands. The product commutes exactly, so rto_fma(w, x, acc) equals
+ * the leaf's rto_fma(x, w, acc). */
+static int conv_shape_ok(const lofgb_conv2d_shape* s, int* P, int* Q) {
+    if (!s) return LOFGB_ERR_NULL;
+    if (s->n < 0 || s->c < 1 || s->h < 1 || s->w < 1 || s->k < 1 || s->r < 1 || s->s < 1 ||
+        s->pad_h < 0 || s->pad_w < 0 || s->stride_h < 1 || s->stride_w < 1 || s->dil_h < 1 ||
+        s->dil_w < 1)
+        return LOFGB_ERR_SIZE;
+    const int64_t ph = ((int64_t)s->h + 2 * (int64_t)s->pad_h - (int64_t)s->dil_h * (s->r - 1) - 1);
+    const int64_t pw = ((int64_t)s->w + 2 * (int64_t)s->pad_w - (int64_t)s->dil_w * (s->s - 1) - 1);
+    if (ph < 0 || pw < 0) return LOFGB_ERR_SIZE;
+    *P = (int)(ph / s->stride_h + 1);
+    *Q = (int)(pw / s->stride_w + 1);
+    return 0;
+}
+
+int orc_conv2d_f32(const float* x, const float* w, float* y, const lofgb_conv2d_shape* s,
+                   int mbits, float alpha, int order, int64_t col0, int64_t ncols,
+                   int nthreads) {
+    int P, Q;
+    int st = conv_shape_ok(s, &P, &Q);
+    if (st) return st;
+    if (!x || !w || !y) return LOFGB_ERR_NULL;
+    if (mbits < 0 || mbits > 23) return LOFGB_ERR_FORMAT;
+    if (order != LOFGB_CONV_CRS && order != LOFGB_CONV_TILED8) return LOFGB_ERR_UNSUPPORTED;
+    const int64_t L = (int64_t)P * Q, cols = (int64_t)s->n * L;
+    if (ncols < 0) { col0 = 0; ncols = cols; }
+    if (col0 < 0 || col0 + ncols > cols) return LOFGB_ERR_SIZE;
+    const int C = s->c, H = s->h, W = s->w, K = s->k, R = s->r, S = s->s;
+    const int ctiles = (C + 7) / 8;
+    const int64_t total = ncols * K;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthr(nthreads))
+    for (int64_t t = 0; t < total; ++t) {
+        const int64_t col = col0 + t / K;
+        const int k = (int)(t % K);
+        const int n = (int)(col / L), l = (int)(col % L), p = l / Q, q = l % Q;
+        const int h0 = p * s->stride_h - s->pad_h, w0 = q * s->stride_w - s->pad_w;
+        float acc = 0.0f;
+#define ORC_CONV_MAC(cc, rr, ss)                                                             \
+    do {                                                                                     \
+        float a = 0.0f, b = 0.0f;                                                            \
+        if ((cc) < C) {                                                                      \
+            const int hh = h0 + (rr) * s->dil_h, ww = w0 + (ss) * s->dil_w;                  \
+            a = w[(((int64_t)k * C + (cc)) * R + (rr)) * S + (ss)];                          \
+            if (hh >= 0 && hh < H && ww >= 0 && ww < W)                                      \
+                b = x[(((int64_t)n * C + (cc)) * H + hh) * W + ww];                          \
+        }                                                                                    \
+        const float v = orc_rto_fma(a, b, acc);                                              \
+        acc = u2f((uint32_t)vr_mant(f2u(v), &SRC_F32, mbits, LOFGB_RNE, 0, 0, 0.0));         \
+    } while (0)
+        if (order == LOFGB_CONV_CRS) {
+            for (int c = 0; c < C; ++c)
+                for (int r = 0; r < R; ++r)
+                    for (int q2 = 0; q2 < S; ++q2) ORC_CONV_MAC(c, r, q2);
+        } else {
+            for (int ct = 0; ct < ctiles; ++ct)
+                for (int r = 0; r < R; ++r)
+                    for (int q2 = 0; q2 < S; ++q2)
+                        for (int ci = 0; ci < 8; ++ci) ORC_CONV_MAC(ct * 8 + ci, r, q2);
+        }
+#undef ORC_CONV_MAC
+        y[(((int64_t)n * K + k) * L) + l] = alpha * acc;
+    }
+    return 0;
+}
+
+/* ---- piecewise-linear SiLU (src/LoPy_bind.cpp:258-269, the CPU loop; the
+ * CUDA kernel src/Lof_kernel.cu:240-256 is the same FP32 arithmetic) ------- */
+int orc_pwl_silu_f32(const float* in, float* out, int64_t n, const float* lut, int segments,
+                     float R) {
+    if (n < 0) return LOFGB_ERR_SIZE;
+    if (n > 0 && (!in || !out || !lut)) return LOFGB_ERR_NULL;
+    const float inv_step = (float)segments / (2.0f * R);
+    for (int64_t k = 0; k < n; ++k) {
+        const float xv = in[k];
+        const float xc = fminf(fmaxf(xv, -R), R);
+        const float u = (xc + R) * inv_step;
+        int i = (int)u;
+        if (i > segments - 1) i = segments - 1;
+        const float frac = u - (float)i;
+        const float y0 = lut[i], y1 = lut[i + 1];
+        float yv = fmaf(frac, y1 - y0, y0);
+        if (fabsf(xv) > R) yv = xv > 0.0f ? xv : 0.0f;
+        out[k] = yv;
+    }
+    return 0;
+}

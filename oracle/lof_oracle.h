@@ -103,6 +103,19 @@ int orc_gemm_chunked_f32(const float* A, int64_t lda, int trans_a, const float* 
                          int64_t ldb, int trans_b, float* D, int64_t ldd, int M, int N,
                          int K, int mbits, int chunk, float alpha, int nthreads);
 
+/* Emulated-accumulation conv2d (lofgb_conv2d_f32 semantics): NCHW input,
+ * KCRS weight, NKPQ output, per-MAC leaf in the t order `order`
+ * (LOFGB_CONV_CRS: the im2col + lof_gemm path, LoFloat/layers.py:684-705;
+ * LOFGB_CONV_TILED8: CUTLASS analytic fprop with 8-channel k-tiles,
+ * src/cutlass_conv.cuh:57-184). Only output columns (n, p, q) with flat index
+ * in [col0, col0 + ncols) are written (ncols < 0: all). */
+int orc_conv2d_f32(const float* x, const float* w, float* y, const lofgb_conv2d_shape* s,
+                   int mbits, float alpha, int order, int64_t col0, int64_t ncols,
+                   int nthreads);
+/* Piecewise-linear SiLU on FP32 values (src/LoPy_bind.cpp:258-269). */
+int orc_pwl_silu_f32(const float* in, float* out, int64_t n, const float* lut, int segments,
+                     float R);
+
 int orc_validate_format(const lofgb_format* f, int src_mant_bits);
 int orc_max_threads(void);
 

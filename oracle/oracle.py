@@ -19,6 +19,12 @@ _lib = None
 _ref = None
 
 
+class ConvShape(C.Structure):
+    """Same layout as ``lofgb_conv2d_shape`` in include/lofgb.h."""
+    _fields_ = [(f, C.c_int32) for f in ("n", "c", "h", "w", "k", "r", "s", "pad_h", "pad_w",
+                                         "stride_h", "stride_w", "dil_h", "dil_w")]
+
+
 class Format(C.Structure):
     """Same layout as ``lofgb_format`` in include/lofgb.h."""
     _fields_ = [("bitwidth", C.c_int32), ("mantissa_bits", C.c_int32), ("bias", C.c_int32),
@@ -60,6 +66,8 @@ def lib():
                                         f32, i32, i32, i32]
         L.orc_gemm_chunked_f32.argtypes = [vp, i64, i32, vp, i64, i32, vp, i64, i32, i32, i32, i32,
                                            i32, f32, i32]
+        L.orc_conv2d_f32.argtypes = [vp, vp, vp, C.POINTER(ConvShape), i32, f32, i32, i64, i64, i32]
+        L.orc_pwl_silu_f32.argtypes = [vp, vp, i64, vp, i32, f32]
         L.orc_rto_fma.restype = f32
         L.orc_rto_fma.argtypes = [f32, f32, f32]
         L.orc_max_threads.restype = i32
@@ -191,3 +199,40 @@ def rto_fma(a: float, b: float, c: float) -> float:
 
 def max_threads() -> int:
     return lib().orc_max_threads()
+
+
+CONV_ORDERS = {"crs": 0, "tiled8": 1}
+
+
+def conv_out_size(h, w, r, s, stride=(1, 1), padding=(0, 0), dilation=(1, 1)):
+    p = (h + 2 * padding[0] - dilation[0] * (r - 1) - 1) // stride[0] + 1
+    q = (w + 2 * padding[1] - dilation[1] * (s - 1) - 1) // stride[1] + 1
+    return p, q
+
+
+def conv2d(x, w, mbits: int, stride=(1, 1), padding=(0, 0), dilation=(1, 1), alpha: float = 1.0,
+           order: str = "crs", col0: int = 0, ncols: int = -1, nthreads: int = 0) -> np.ndarray:
+    """Emulated-accumulation conv2d, NCHW x KCRS -> NKPQ (lofgb_conv2d_f32).
+    With ncols >= 0 only output pixels [col0, col0 + ncols) of the flat (n, p, q)
+    index are computed; the rest of the returned array is 0."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    n, c, h, wd = x.shape
+    k, c2, r, s_ = w.shape
+    assert c == c2
+    sh = ConvShape(n, c, h, wd, k, r, s_, padding[0], padding[1], stride[0], stride[1],
+                   dilation[0], dilation[1])
+    p, q = conv_out_size(h, wd, r, s_, stride, padding, dilation)
+    y = np.zeros((n, k, p, q), np.float32)
+    _check(lib().orc_conv2d_f32(_p(x), _p(w), _p(y), C.byref(sh), mbits, alpha,
+                                CONV_ORDERS[order], col0, ncols, nthreads))
+    return y
+
+
+def pwl_silu(x, lut, R: float) -> np.ndarray:
+    """Piecewise-linear SiLU on float32 values (src/LoPy_bind.cpp:258-269)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    lut = np.ascontiguousarray(lut, dtype=np.float32)
+    y = np.empty_like(x)
+    _check(lib().orc_pwl_silu_f32(_p(x), _p(y), x.size, _p(lut), lut.size - 1, R))
+    return y

@@ -162,3 +162,30 @@ def test_grouped_prepare_host_only():
     assert L.lofgb_round_grouped_prepare(bad, 1, buf, nbytes, C.byref(items)) == -3
     assert "task 0" in L.lofgb_last_error_detail().decode()
     assert L.lofgb_round_grouped_f32(None, 0, 0, None) == 0
+
+
+def test_grouped_gemm_validation_host_only():
+    L = _native.lib()
+    T = _native.LofgbGemmTask
+    good = T(0x1000, 64, 0x2000, 32, 0x3000, 32, 0, 0, 16, 32, 64, 10, 1.0, 32)
+    arr = (T * 1)(good)
+    ws_need = L.lofgb_gemm_grouped_workspace_size(arr, 1)
+    tb_need = L.lofgb_gemm_grouped_table_size(arr, 1)
+    assert ws_need > 1024 and tb_need > 0
+    buf = (C.c_uint8 * tb_need)()
+    nt, si = C.c_int64(0), C.c_int64(0)
+
+    def prep(task, ws=0x100000, wsb=ws_need, sched=1, tbytes=tb_need):
+        a = (T * 1)(task)
+        return L.lofgb_gemm_grouped_prepare(a, 1, C.c_void_p(ws), wsb, sched, 4, buf, tbytes,
+                                            C.byref(nt), C.byref(si))
+    bad = T(0x1000, 63, 0x2000, 32, 0x3000, 32, 0, 0, 16, 32, 64, 10, 1.0, 32)
+    assert prep(bad) == -2                                   # lda < K
+    bad = T(0x1000, 64, 0x2000, 32, 0x3000, 32, 0, 0, 16, 32, 64, 10, 1.0, 24)
+    assert prep(bad) == -2                                   # chunk not a multiple of 16
+    bad = T(0x1000, 64, 0x2000, 32, 0x3000, 32, 0, 0, 16, 32, 64, 30, 1.0, 32)
+    assert prep(bad) == -3                                   # accumulator width
+    assert prep(good, wsb=ws_need - 1) == -9                 # workspace too small
+    assert prep(good, ws=0x100010) == -9                     # workspace misaligned
+    assert prep(good, tbytes=tb_need - 1) == -9              # table too small
+    assert prep(good, sched=5) == -7                         # unknown schedule

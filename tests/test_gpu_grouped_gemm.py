@@ -1,0 +1,74 @@
+"""Grouped tensor-core GEMM: every task equals the single-GEMM tensor-core
+path bit for bit (same MMA sequence per tile), under every schedule, from a
+captured CUDA graph, and with ragged shapes; the autotuner picks and caches a
+schedule."""
+import json
+
+import pytest
+import torch
+
+import lofloat_gb300 as lg
+from lofloat_gb300 import autotune
+
+pytestmark = pytest.mark.gpu
+
+
+def _tasks(count, seed, dims=(128, 640), ragged=False):
+    g = torch.Generator().manual_seed(seed)
+    out = []
+    for i in range(count):
+        M, N, K = (int(torch.randint(dims[0], dims[1], (1,), generator=g)) for _ in range(3))
+        if not ragged:
+            M, N, K = (x // 64 * 64 for x in (M, N, K))
+        ta, tb = i % 2, (i // 2) % 2
+        A = torch.randn((K, M) if ta else (M, K), generator=g).cuda()
+        B = torch.randn((N, K) if tb else (K, N), generator=g).cuda()
+        out.append(dict(A=A, B=B, D=torch.empty(M, N, device="cuda"), trans_a=ta, trans_b=tb,
+                        accum_mant_bits=int(7 + i % 6), alpha=float(0.5 + i % 3),
+                        chunk=[16, 32, 64, 48][i % 4]))
+    return out
+
+
+def _reference(t):
+    return lg.gemm(t["A"], t["B"], t["accum_mant_bits"], trans_a=bool(t["trans_a"]),
+                   trans_b=bool(t["trans_b"]), alpha=t["alpha"], variant="tc", chunk=t["chunk"])
+
+
+@pytest.mark.parametrize("schedule", ["task", "lpt", "lpt_snake"])
+def test_grouped_matches_single(schedule):
+    tasks = _tasks(10, 1)
+    gg = lg.GroupedGemm(tasks, schedule=schedule)
+    gg.ws.fill_(0xFF)  # the launch must clear the status word itself
+    gg()
+    torch.cuda.synchronize()
+    assert gg.status() == 0
+    for i, t in enumerate(tasks):
+        assert torch.equal(t["D"], _reference(t)), i
+
+
+def test_grouped_ragged_and_graph():
+    tasks = _tasks(7, 2, dims=(1, 300), ragged=True)
+    gg = lg.GroupedGemm(tasks, schedule="lpt_snake", grid=37)
+    gg.capture()
+    for t in tasks:
+        t["D"].zero_()
+    gg.replay()
+    torch.cuda.synchronize()
+    assert gg.status() == 0
+    for i, t in enumerate(tasks):
+        assert torch.equal(t["D"], _reference(t)), i
+
+
+def test_autotuner_caches(tmp_path, monkeypatch):
+    monkeypatch.setattr(autotune, "CACHE_PATH", str(tmp_path / "tune.json"))
+    tasks = _tasks(6, 3)
+    gg = lg.GroupedGemm(tasks, schedule="auto", tune_reps=2)
+    assert gg.schedule in autotune.SCHEDULES
+    cache = json.loads((tmp_path / "tune.json").read_text())
+    assert gg.signature in cache and set(cache[gg.signature]["ms"]) == set(autotune.SCHEDULES)
+    again = lg.GroupedGemm(tasks, schedule="auto")
+    assert again.schedule == gg.schedule
+    again()
+    torch.cuda.synchronize()
+    for i, t in enumerate(tasks):
+        assert torch.equal(t["D"], _reference(t)), i
