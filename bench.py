@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-secondary", action="store_true", help="headline workload only")
     ap.add_argument("--only", default=None,
                     choices=["mx", "round_rne", "round_sr", "gemm_plain", "gemm_tc", "conv_plain",
-                             "conv_tc", "pwl"],
+                             "conv_tc", "pwl", "encode", "decode"],
                     help="run one workload's kernel warmup+steps times and exit (for ncu captures)")
     ap.add_argument("--size", default="full", choices=["full", "small"],
                     help="with --only: full-size workload or a small case (GEMM 1024^3)")
@@ -336,6 +336,34 @@ def conv_workloads(torch, lg, dev, peaks):
     gbs = (1 << 26) * 8 / (ms * 1e-3) / 1e9
     out["pwl_silu_2^26_GBs"] = round(gbs, 1)
     out["pwl_silu_2^26_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)
+    del xs, ys
+    out.update(codec_workloads(torch, lg, dev, peaks))
+    return out
+
+
+def codec_workloads(torch, lg, dev, peaks):
+    """Storage codec over 2^26 FP32 values (config-1 distribution): encode to
+    packed E4M3 (8-bit) and P3109<6,3> (6-bit) codes and decode back, GB/s at
+    4 + n/8 bytes per value."""
+    out = {}
+    stream = torch.cuda.current_stream(dev)
+    n = 1 << 26
+    g = torch.Generator(device=dev).manual_seed(8)
+    x = torch.randn(n, device=dev, generator=g) * torch.exp2(
+        torch.randint(-20, 21, (n,), device=dev, generator=g).float())
+    y = torch.empty_like(x)
+    for name, fmt in (("e4m3", lg.create_p3109_params(8, 4)), ("p3109_6p3", lg.create_p3109_params(6, 3))):
+        bits = fmt.total_bits
+        packed = torch.empty(lg.packed_size(bits, n), dtype=torch.uint8, device=dev)
+        enc = lambda: lg.lof_encode(x, fmt, out=packed)  # noqa: E731
+        dec = lambda: lg.lof_decode(packed, n, fmt, out=y)  # noqa: E731
+        for fn, tag in ((enc, "encode"), (dec, "decode")):
+            for _ in range(3):
+                fn()
+            ms = statistics.median(time_events(torch, fn, 10, stream))
+            gbs = n * (4 + bits / 8) / (ms * 1e-3) / 1e9
+            out[f"codec_{tag}_{name}_2^26_GBs"] = round(gbs, 1)
+            out[f"codec_{tag}_{name}_2^26_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)
     return out
 
 
@@ -503,15 +531,37 @@ def run_ours(args, world, rank, local):
     elapsed = t0.elapsed_time(t1) / 1e3
     per_launch = statistics.mean(s.elapsed_time(e) for s, e in launch_ms) / 1e3
 
-    # end to end through the public API with host buffers
+    # end to end through the public API with host buffers: the matrix is
+    # streamed in row chunks (whole MX blocks) over three streams, so the
+    # host-to-device copy of chunk c+1, the rounding of chunk c and the
+    # device-to-host copies of chunk c-1 overlap
     xh = x_host.pin_memory()
     yh = [torch.empty_like(xh).pin_memory() for _ in efs]
+    xd_buf = torch.empty_like(x)
+    yd_buf = [torch.empty_like(x) for _ in efs]
+    s_in, s_cmp, s_out = (torch.cuda.Stream(dev) for _ in range(3))
+    E2E_CHUNKS = 16
+    rows = MX_ROWS // E2E_CHUNKS
+    ev_in = [torch.cuda.Event() for _ in range(E2E_CHUNKS)]
+    ev_cmp = [torch.cuda.Event() for _ in range(E2E_CHUNKS)]
 
     def e2e_step():
-        xd = xh.to(dev, non_blocking=True)
-        for i, ef in enumerate(efs):
-            yd = lg.virtual_mx_round(xd, MX_BLOCK, ef, e8)
-            yh[i].copy_(yd, non_blocking=True)
+        s_in.wait_stream(stream)
+        for c in range(E2E_CHUNKS):
+            sl = slice(c * rows, (c + 1) * rows)
+            with torch.cuda.stream(s_in):
+                xd_buf[sl].copy_(xh[sl], non_blocking=True)
+                ev_in[c].record(s_in)
+            s_cmp.wait_event(ev_in[c])
+            with torch.cuda.stream(s_cmp):
+                for i, ef in enumerate(efs):
+                    lg.virtual_mx_round(xd_buf[sl], MX_BLOCK, ef, e8, out=yd_buf[i][sl])
+                ev_cmp[c].record(s_cmp)
+            s_out.wait_event(ev_cmp[c])
+            with torch.cuda.stream(s_out):
+                for i in range(len(efs)):
+                    yh[i][sl].copy_(yd_buf[i][sl], non_blocking=True)
+        stream.wait_stream(s_out)
 
     for _ in range(2):
         e2e_step()
@@ -555,7 +605,8 @@ def run_ours(args, world, rank, local):
         "e2e": {"value": round(world * e2e_steps * step_bytes / e2e_s / 1e9, 2), "unit": "GB/s",
                 "h2d_bytes_per_step": MX_ROWS * MX_COLS * 4,
                 "d2h_bytes_per_step": len(efs) * MX_ROWS * MX_COLS * 4,
-                "api": "lofloat_gb300.virtual_mx_round (C ABI lofgb_mx_round_f32)"},
+                "api": "lofloat_gb300.virtual_mx_round (C ABI lofgb_mx_round_f32), "
+                       "16 row chunks streamed over copy-in / compute / copy-out streams"},
         "gpu_launches": args.steps * len(efs),
         "clocks": clk,
     }
@@ -605,6 +656,15 @@ def run_only(args):
         ys = torch.empty_like(xs)
         fn = lambda: lg.pwl_silu(xs, lut, 8.0, out=ys)  # noqa: E731
         work, unit = (1 << 26) * 8, "GB/s"
+    elif args.only in ("encode", "decode"):
+        n = 1 << 26
+        x = (torch.randn(n, device=dev) * torch.exp2(torch.randint(-20, 21, (n,), device=dev).float()))
+        fmt = lg.create_p3109_params(8, 4)
+        packed = lg.lof_encode(x, fmt)
+        y = torch.empty_like(x)
+        fn = (lambda: lg.lof_encode(x, fmt, out=packed)) if args.only == "encode" else \
+            (lambda: lg.lof_decode(packed, n, fmt, out=y))  # noqa: E731
+        work, unit = n * 5, "GB/s"
     else:
         n = GEMM_N if args.size == "full" else 1024
         g = torch.Generator().manual_seed(3)

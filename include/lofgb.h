@@ -166,6 +166,21 @@ int lofgb_gemm_f32(const float* A, int64_t lda, int trans_a, const float* B, int
                    void* workspace, size_t workspace_bytes, void* stream);
 size_t lofgb_gemm_tc_workspace_size(int M, int N, int K);
 
+/* Strided-batched form: `batch` independent products, GEMM b reading
+ * A + b*stride_a and B + b*stride_b and writing D + b*stride_d (element
+ * strides; 0 broadcasts an operand; D matrices may not overlap), each exactly
+ * as lofgb_gemm_f32 computes it. Replaces the per-matrix Python loop of
+ * _lof_gemm_2d (LoFloat/layers.py:136-150) through which
+ * LoF_MultiHeadAttention's score and context products run (:1331-1345).
+ * LOFGB_GEMM_TC needs lofgb_gemm_batched_tc_workspace_size(M, N, K, batch)
+ * bytes. */
+int lofgb_gemm_batched_f32(const float* A, int64_t lda, int64_t stride_a, int trans_a,
+                           const float* B, int64_t ldb, int64_t stride_b, int trans_b, float* D,
+                           int64_t ldd, int64_t stride_d, int M, int N, int K, int batch,
+                           int accum_mant_bits, int mode, float alpha, int variant, int chunk,
+                           void* workspace, size_t workspace_bytes, void* stream);
+size_t lofgb_gemm_batched_tc_workspace_size(int M, int N, int K, int batch);
+
 /* Tensor-core GEMM for callers that cannot allocate device memory.
  * No counterpart in the reference.
  *
@@ -341,6 +356,57 @@ int lofgb_pwl_silu_f64(const double* in, double* out, int64_t n, const float* lu
                        int segments, float R, void* stream);
 int lofgb_pwl_silu_f16(const uint16_t* in, uint16_t* out, int64_t n, const float* lut,
                        int segments, float R, void* stream);
+
+/* ---- low-precision storage codec -------------------------------------------
+ * Replaces LoF_encode_cuda / LoF_decode_cuda and their CPU twins
+ * (src/lo_pack.hpp:109-532): FP32 values are converted to n-bit codes of a
+ * runtime format (n in [1, 16]) and packed without waste, and back.
+ *
+ * Codes: convert_float_to_rep (src/lo_pack.hpp:109-287), the runtime twin of
+ * the typed float -> Templated_Float conversion: NaN -> the quiet-NaN code;
+ * ±inf -> the infinity code, or the largest finite code under SatFinite or
+ * without infinities; negative inputs of unsigned formats -> 0 or NaN
+ * (neg_to_nan); target-subnormal and normal ranges rounded with the
+ * reference's RoundMantissa (its RoundUp / RoundDown see a positive-sign flag
+ * of false, as there); overflow -> infinity under OvfInf with infinities,
+ * else the largest finite code; -0 of a format whose sign-only code is NaN
+ * encodes as +0. Stochastic modes draw R = SplitMix64(seed, offset + i) for
+ * element i, as the rounding entry points do. Values: convert_rep_to_float
+ * (:293-320): infinity and NaN codes by the format's predicates, else the
+ * exact value (in double) narrowed to float.
+ *
+ * Packing: a group of lcm(n, 8) bits (n <= 8) or lcm(n, 16) bits (n > 8)
+ * holds lcm / n codes; element i of a group sits at bit slot*n, slot = i
+ * (forward) or group_count - 1 - i (reverse), LSB-first within each byte;
+ * groups follow one another; the last group is zero padded.
+ *
+ * The special-value predicates of the reference's checker functors
+ * (P3109, IEEE-style, OCP, E8M0, trivial) all take one of these forms:
+ *   IsInf(rep) <=> (rep | inf_or) == inf_match   (inf_match 0xFFFFFFFF: never)
+ *   IsNaN(rep) <=> LOFGB_NAN_PATTERN: rep == qnan;
+ *                  LOFGB_NAN_IEEE:    rep without its sign bit > the code with
+ *                                     all exponent bits set and mantissa 0;
+ *                  LOFGB_NAN_NONE:    never.                                  */
+enum lofgb_sat_mode { LOFGB_OVF_INF = 0, LOFGB_SAT_FINITE = 1, LOFGB_SAT_PROPAGATE = 2 };
+enum lofgb_nan_kind { LOFGB_NAN_PATTERN = 0, LOFGB_NAN_IEEE = 1, LOFGB_NAN_NONE = 2 };
+
+typedef struct lofgb_codec_format {
+    lofgb_format fmt;            /* bitwidth 1..16 */
+    uint32_t inf_or, inf_match;  /* IsInf predicate, see above */
+    uint32_t pos_inf, neg_inf;   /* IsInf.minPosInf(), minNegInf() */
+    uint32_t qnan, snan;         /* IsNaN.qNanBitPattern(), sNanBitPattern() */
+    uint8_t nan_kind;            /* IsNaN form, lofgb_nan_kind */
+    uint8_t neg_to_nan;          /* unsigned formats: Unsigned_behavior NegtoNaN */
+    uint8_t reserved[2];
+} lofgb_codec_format;
+
+/* Bytes that `count` codes of `bitwidth` bits occupy (whole groups). */
+size_t lofgb_packed_size(int bitwidth, int64_t count);
+int lofgb_encode_f32(uint8_t* dst, const float* src, int64_t count, const lofgb_codec_format* fmt,
+                     int mode, int sat_mode, int stoch_len, int reverse, uint64_t seed,
+                     uint64_t offset, void* stream);
+int lofgb_decode_f32(float* dst, const uint8_t* src, int64_t count, const lofgb_codec_format* fmt,
+                     int reverse, void* stream);
 
 #ifdef __cplusplus
 }

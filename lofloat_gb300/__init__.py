@@ -16,13 +16,15 @@ All compute runs in liblofgb.so (include/lofgb.h) on CUDA tensors.
 """
 from . import _custom_ops  # noqa: F401  (registers torch.ops.lofloat.*)
 from .binding import (FloatFormatDescriptor, InfBehavior, NaNBehavior, RoundingMode, Signedness,
-                      conv2d, conv2d_alpha, gemm, gemm_alpha, gemm_f64_reference, get_rng_state,
-                      lof_conv2d, lof_gemm, pwl_silu, set_rng_state, set_seed, virtual_mx_round,
+                      SaturationMode, codec_format, conv2d, conv2d_alpha, gemm, gemm_alpha,
+                      gemm_f64_reference, get_rng_state, lof_conv2d, lof_decode, lof_encode, lof_gemm,
+                      packed_size, pwl_silu, set_rng_state, set_seed, virtual_mx_round,
                       virtual_round)
 from .formats import (create_e8m0_params, create_half_params, create_p3109_params,
                       create_single_params, make_format)
-from .layers import (LinearConfig, LoF_Conv2d, LoF_Linear, LoF_Quantize, LoFLinearFunction,
-                     PWLSiLU, STEMXRound, STERound, _fwht, _lof_gemm_2d, _lof_linear, lof_linear)
+from .layers import (LinearConfig, LoF_Conv2d, LoF_Linear, LoF_MultiHeadAttention, LoF_Quantize,
+                     LoFLinearFunction, PWLSiLU, STEMXRound, STERound, _fwht, _lof_gemm_2d,
+                     _lof_linear, lof_linear)
 from ._custom_ops import get_format, register_format
 from .grouped import GroupedRound
 from .autotune import GroupedGemm
@@ -34,5 +36,6 @@ __all__ = [
     "create_half_params", "create_single_params", "make_format", "STERound", "STEMXRound",
     "LoF_Quantize", "LoF_Linear", "LoFLinearFunction", "LinearConfig", "lof_linear",
     "register_format", "get_format", "GroupedRound", "GroupedGemm", "lof_conv2d", "conv2d",
-    "conv2d_alpha", "pwl_silu", "LoF_Conv2d", "PWLSiLU",
+    "conv2d_alpha", "pwl_silu", "LoF_Conv2d", "PWLSiLU", "LoF_MultiHeadAttention",
+    "SaturationMode", "codec_format", "packed_size", "lof_encode", "lof_decode",
 ]

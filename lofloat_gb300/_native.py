@@ -37,6 +37,14 @@ class LofgbGemmTask(C.Structure):
                 ("accum_mant_bits", C.c_int32), ("alpha", C.c_float), ("chunk", C.c_int32)]
 
 
+class LofgbCodecFormat(C.Structure):
+    """``lofgb_codec_format`` (include/lofgb.h)."""
+    _fields_ = [("fmt", LofgbFormat), ("inf_or", C.c_uint32), ("inf_match", C.c_uint32),
+                ("pos_inf", C.c_uint32), ("neg_inf", C.c_uint32), ("qnan", C.c_uint32),
+                ("snan", C.c_uint32), ("nan_kind", C.c_uint8), ("neg_to_nan", C.c_uint8),
+                ("reserved", C.c_uint8 * 2)]
+
+
 class LofgbConv2dShape(C.Structure):
     """``lofgb_conv2d_shape`` (include/lofgb.h)."""
     _fields_ = [(f, C.c_int32) for f in ("n", "c", "h", "w", "k", "r", "s", "pad_h", "pad_w",
@@ -62,6 +70,10 @@ SIGNATURES = [
     ("lofgb_gemm_f32", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32,
                               _i32, _i32, _f32, _i32, _i32, _vp, _sz, _vp]),
     ("lofgb_gemm_tc_workspace_size", _sz, [_i32, _i32, _i32]),
+    ("lofgb_gemm_batched_f32", _i32, [_vp, _i64, _i64, _i32, _vp, _i64, _i64, _i32, _vp, _i64, _i64,
+                                      _i32, _i32, _i32, _i32, _i32, _i32, _f32, _i32, _i32, _vp,
+                                      _sz, _vp]),
+    ("lofgb_gemm_batched_tc_workspace_size", _sz, [_i32, _i32, _i32, _i32]),
     ("lofgb_gemm_tc_noalloc_f32", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32,
                                          _i32, _i32, _f32, _i32, _vp]),
     ("lofgb_gemm_f64_ref", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32,
@@ -83,6 +95,10 @@ SIGNATURES = [
     ("lofgb_pwl_silu_f32", _i32, [_vp, _vp, _i64, _vp, _i32, _f32, _vp]),
     ("lofgb_pwl_silu_f64", _i32, [_vp, _vp, _i64, _vp, _i32, _f32, _vp]),
     ("lofgb_pwl_silu_f16", _i32, [_vp, _vp, _i64, _vp, _i32, _f32, _vp]),
+    ("lofgb_packed_size", _sz, [_i32, _i64]),
+    ("lofgb_encode_f32", _i32, [_vp, _vp, _i64, C.POINTER(LofgbCodecFormat), _i32, _i32, _i32, _i32,
+                                _u64, _u64, _vp]),
+    ("lofgb_decode_f32", _i32, [_vp, _vp, _i64, C.POINTER(LofgbCodecFormat), _i32, _vp]),
 ]
 
 

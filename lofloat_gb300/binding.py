@@ -281,34 +281,47 @@ def gemm(A: torch.Tensor, B: torch.Tensor, accum_mant_bits: int, *, trans_a: boo
     """Emulated-accumulation GEMM with explicit layouts.
 
     A is (M, K), or (K, M) when trans_a; B is (K, N), or (N, K) when trans_b;
-    both contiguous float32 CUDA tensors. variant "plain" is bit-exact to the
-    reference leaf; "tc" is the tcgen05 chunked form."""
+    both contiguous float32 CUDA tensors. A leading batch dimension on either
+    operand makes it a strided-batched GEMM (one launch; a 2-D operand, or a
+    batch of 1, is shared by every product) with D of shape (batch, M, N).
+    variant "plain" is bit-exact to the reference leaf; "tc" is the tcgen05
+    chunked form."""
     for t, nm in ((A, "A"), (B, "B")):
-        if t.dim() != 2:
-            raise RuntimeError(f"lof_gemm: {nm} must be 2-D")
+        if t.dim() not in (2, 3):
+            raise RuntimeError(f"lof_gemm: {nm} must be 2-D (or 3-D for a batch)")
         if t.dtype != torch.float32:
             raise RuntimeError("lof_gemm: only float32 inputs are supported")
         _require_cuda(t, "lof_gemm")
+    batched = A.dim() == 3 or B.dim() == 3
     A = A.contiguous()
     B = B.contiguous()
-    M, K = (A.shape[1], A.shape[0]) if trans_a else (A.shape[0], A.shape[1])
-    Kb, N = (B.shape[1], B.shape[0]) if trans_b else (B.shape[0], B.shape[1])
+    M, K = (A.shape[-1], A.shape[-2]) if trans_a else (A.shape[-2], A.shape[-1])
+    Kb, N = (B.shape[-1], B.shape[-2]) if trans_b else (B.shape[-2], B.shape[-1])
     if K != Kb:
         raise RuntimeError(f"LoF_gemm: A.cols ({K}) != B.rows ({Kb})")
-    D = torch.empty((M, N), dtype=torch.float32, device=A.device) if out is None else out
-    if D.shape != (M, N) or not D.is_contiguous() or D.dtype != torch.float32:
-        raise RuntimeError("lof_gemm: out must be a contiguous float32 (M, N) tensor")
+    ba = A.shape[0] if A.dim() == 3 else 1
+    bb = B.shape[0] if B.dim() == 3 else 1
+    if ba != bb and 1 not in (ba, bb):
+        raise RuntimeError(f"lof_gemm: batch sizes differ ({ba} vs {bb})")
+    batch = max(ba, bb)
+    shape = (batch, M, N) if batched else (M, N)
+    D = torch.empty(shape, dtype=torch.float32, device=A.device) if out is None else out
+    if tuple(D.shape) != shape or not D.is_contiguous() or D.dtype != torch.float32:
+        raise RuntimeError(f"lof_gemm: out must be a contiguous float32 {shape} tensor")
     v = {"plain": 0, "tc": 1}[variant]
     L = _native.lib()
+    sa = A.shape[-2] * A.shape[-1] if ba > 1 else 0
+    sb = B.shape[-2] * B.shape[-1] if bb > 1 else 0
     with torch.cuda.device(A.device):
         ws, wsb = None, 0
-        if v == 1:
-            buf = _tc_workspace(A.device, M, N, K)
+        if v == 1 and M and N and K:
+            buf = _workspace(A.device, int(L.lofgb_gemm_batched_tc_workspace_size(M, N, K, batch)))
             ws, wsb = buf.data_ptr(), buf.numel()
-        check(L.lofgb_gemm_f32(A.data_ptr(), A.shape[1], int(trans_a), B.data_ptr(), B.shape[1],
-                               int(trans_b), D.data_ptr(), N, M, N, K, int(accum_mant_bits),
-                               int(RoundingMode.RoundToNearestEven), float(alpha), v, int(chunk),
-                               ws, wsb, _stream(A)), "lof_gemm")
+        check(L.lofgb_gemm_batched_f32(A.data_ptr(), A.shape[-1], sa, int(trans_a), B.data_ptr(),
+                                       B.shape[-1], sb, int(trans_b), D.data_ptr(), N, M * N, M,
+                                       N, K, batch, int(accum_mant_bits),
+                                       int(RoundingMode.RoundToNearestEven), float(alpha), v,
+                                       int(chunk), ws, wsb, _stream(A)), "lof_gemm")
     return D
 
 
@@ -457,4 +470,114 @@ def pwl_silu(input: torch.Tensor, lut: torch.Tensor, R: float, *,
         check(getattr(_native.lib(), _PWL_FNS[x.dtype])(x.data_ptr(), y.data_ptr(), x.numel(),
                                                         lut_f.data_ptr(), nseg, float(R),
                                                         _stream(x)), "pwl_silu")
+    return y
+
+
+# ---- storage codec (src/lo_pack.hpp) ----------------------------------------------
+class SaturationMode(enum.IntEnum):
+    """Saturation_Mode (src/fp_tools.hpp:38-41): what an overflow encodes to."""
+    OvfInf = 0
+    SatFinite = 1
+    SatPropagate = 2
+
+
+def codec_format(params: FloatFormatDescriptor, neg_to_nan: bool = False):
+    """lofgb_codec_format for `params`: the checkers' predicates are evaluated
+    over every code of the format (at most 2^16) and matched to the forms the
+    kernels evaluate — IsInf(rep) <=> (rep | inf_or) == inf_match; IsNaN as a
+    single pattern, the IEEE exponent-all-ones range, or never. Raises for a
+    checker that fits neither (the reference's P3109, IEEE-style, OCP, E8M0
+    and trivial checkers all fit)."""
+    n, m = params.total_bits, params.mantissa_bits
+    if not 1 <= n <= 16:
+        raise RuntimeError(f"codec: bitwidth {n} outside [1, 16]")
+    signed = params.signedness == Signedness.Signed
+    codes = range(1 << n)
+    inf_set = {r for r in codes if params.is_inf_checker(r)}
+    nan_set = {r for r in codes if params.is_nan_checker(r)}
+    sign = (1 << (n - 1)) if signed else 0
+    inf_or, inf_match = 0, 0xFFFFFFFF
+    if inf_set:
+        for o in (0, sign, 1 << (n - 1)):
+            t = min(inf_set) | o
+            if {r for r in codes if (r | o) == t} == inf_set:
+                inf_or, inf_match = o, t
+                break
+        else:
+            raise RuntimeError("codec: the format's infinity checker has no supported form")
+    qnan = int(params.is_nan_checker.qNanBitPattern()) if hasattr(params.is_nan_checker, "qNanBitPattern") \
+        else int(params.is_nan_checker.sNanBitPattern())
+    snan = int(params.is_nan_checker.sNanBitPattern()) if hasattr(params.is_nan_checker, "sNanBitPattern") \
+        else qnan
+    ebits = n - m - (1 if signed else 0)
+    expall = ((1 << ebits) - 1) << m
+    if not nan_set:
+        kind = 2
+    elif nan_set == {qnan}:
+        kind = 0
+    elif nan_set == {r for r in codes if (r & ~sign) > expall}:
+        kind = 1
+    else:
+        raise RuntimeError("codec: the format's NaN checker has no supported form")
+    f = _native.LofgbCodecFormat()
+    f.fmt = params.c_format
+    f.inf_or, f.inf_match = inf_or & 0xFFFFFFFF, inf_match & 0xFFFFFFFF
+    f.pos_inf = int(params.is_inf_checker.minPosInf()) & 0xFFFFFFFF
+    f.neg_inf = int(params.is_inf_checker.minNegInf()) & 0xFFFFFFFF
+    f.qnan, f.snan, f.nan_kind, f.neg_to_nan = qnan, snan, kind, int(bool(neg_to_nan))
+    return f
+
+
+def packed_size(bitwidth: int, count: int) -> int:
+    """Bytes `count` codes of `bitwidth` bits occupy (LoF_packed_size,
+    src/lo_pack.hpp:374-377)."""
+    return int(_native.lib().lofgb_packed_size(int(bitwidth), int(count)))
+
+
+def lof_encode(input: torch.Tensor, params: FloatFormatDescriptor,
+               round_mode=RoundingMode.RoundToNearestEven, saturation=SaturationMode.OvfInf,
+               stoch_len: int = 0, *, reverse: bool = False, neg_to_nan: bool = False,
+               out: torch.Tensor | None = None, seed: int | None = None,
+               offset: int | None = None) -> torch.Tensor:
+    """Round float32 values to `params` codes and pack them (LoF_encode_cuda,
+    src/lo_pack.hpp:496-512). Returns a uint8 tensor of packed_size bytes."""
+    if input.dtype != torch.float32:
+        raise RuntimeError("lof_encode: float32 input only")
+    _require_cuda(input, "lof_encode")
+    x = input.contiguous()
+    f = codec_format(params, neg_to_nan)
+    nbytes = packed_size(params.total_bits, x.numel())
+    y = torch.empty(nbytes, dtype=torch.uint8, device=x.device) if out is None else out
+    if y.dtype != torch.uint8 or y.numel() < nbytes or not y.is_contiguous():
+        raise RuntimeError(f"lof_encode: out must be a contiguous uint8 tensor of {nbytes} bytes")
+    mode = int(round_mode)
+    if seed is None:
+        s, o = _take_counters(mode, x.numel())
+    else:
+        s, o = int(seed), int(offset or 0)
+    with torch.cuda.device(x.device):
+        check(_native.lib().lofgb_encode_f32(y.data_ptr(), x.data_ptr(), x.numel(), C.byref(f),
+                                             mode, int(saturation), int(stoch_len), int(reverse),
+                                             s, o, _stream(x)), "lof_encode")
+    return y
+
+
+def lof_decode(packed: torch.Tensor, count: int, params: FloatFormatDescriptor, *,
+               reverse: bool = False, out: torch.Tensor | None = None) -> torch.Tensor:
+    """Unpack `count` codes of `params` and convert them to float32
+    (LoF_decode_cuda, src/lo_pack.hpp:515-532)."""
+    if packed.dtype != torch.uint8:
+        raise RuntimeError("lof_decode: packed must be a uint8 tensor")
+    _require_cuda(packed, "lof_decode")
+    p = packed.contiguous()
+    need = packed_size(params.total_bits, count)
+    if p.numel() < need:
+        raise RuntimeError(f"lof_decode: {count} codes need {need} bytes, got {p.numel()}")
+    f = codec_format(params)
+    y = torch.empty(int(count), dtype=torch.float32, device=p.device) if out is None else out
+    if y.dtype != torch.float32 or y.numel() != count or not y.is_contiguous():
+        raise RuntimeError("lof_decode: out must be a contiguous float32 tensor of count values")
+    with torch.cuda.device(p.device):
+        check(_native.lib().lofgb_decode_f32(y.data_ptr(), p.data_ptr(), int(count), C.byref(f),
+                                             int(reverse), _stream(p)), "lof_decode")
     return y

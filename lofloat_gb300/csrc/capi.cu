@@ -316,10 +316,11 @@ static int check_gemm_args(const void* A, int64_t lda, int ta, const void* B, in
     return LOFGB_OK;
 }
 
-int lofgb_gemm_f32(const float* A, int64_t lda, int trans_a, const float* B, int64_t ldb,
-                   int trans_b, float* D, int64_t ldd, int M, int N, int K, int accum_mant_bits,
-                   int mode, float alpha, int variant, int chunk, void* workspace,
-                   size_t workspace_bytes, void* stream) {
+static int gemm_impl(const float* A, int64_t lda, int64_t sa, int trans_a, const float* B,
+                     int64_t ldb, int64_t sb, int trans_b, float* D, int64_t ldd, int64_t sd,
+                     int M, int N, int K, int batch, int accum_mant_bits, int mode, float alpha,
+                     int variant, int chunk, void* workspace, size_t workspace_bytes,
+                     void* stream) {
     g_detail[0] = 0;
     int st = check_gemm_args(A, lda, trans_a, B, ldb, trans_b, D, ldd, M, N, K);
     if (st) return st;
@@ -328,23 +329,52 @@ int lofgb_gemm_f32(const float* A, int64_t lda, int trans_a, const float* B, int
     if (mode != LOFGB_RNE)
         return set_error(LOFGB_ERR_MODE,
                          "accumulator rounding is RNE only (the reference leaf ignores the mode)");
-    if (M == 0 || N == 0) return LOFGB_OK;
+    if (batch < 0) return set_error(LOFGB_ERR_SIZE, "negative batch");
+    if (sa < 0 || sb < 0 || sd < 0) return set_error(LOFGB_ERR_SIZE, "negative batch stride");
+    if (batch > 1 && M > 0 && N > 0 && sd < (int64_t)(M - 1) * ldd + N)
+        return set_error(LOFGB_ERR_ALIAS, "batch stride of D smaller than one D matrix");
+    if (M == 0 || N == 0 || batch == 0) return LOFGB_OK;
     if (variant == LOFGB_GEMM_PLAIN)
-        return launch_gemm_plain(A, lda, trans_a, B, ldb, trans_b, D, ldd, M, N, K,
-                                 accum_mant_bits, alpha, stream);
+        return launch_gemm_plain(A, lda, sa, trans_a, B, ldb, sb, trans_b, D, ldd, sd, M, N, K,
+                                 batch, accum_mant_bits, alpha, stream);
     if (variant == LOFGB_GEMM_TC) {
         if (chunk <= 0 || chunk % 16 != 0 || chunk > 256)
             return set_error(LOFGB_ERR_SIZE, "chunk %d must be a multiple of 16 in [16, 256]",
                              chunk);
-        return launch_gemm_tc(A, lda, trans_a, B, ldb, trans_b, D, ldd, M, N, K,
-                              accum_mant_bits, alpha, chunk, workspace, workspace_bytes, stream);
+        return launch_gemm_tc(A, lda, sa, trans_a, B, ldb, sb, trans_b, D, ldd, sd, M, N, K,
+                              batch, accum_mant_bits, alpha, chunk, workspace, workspace_bytes,
+                              stream);
     }
     return set_error(LOFGB_ERR_UNSUPPORTED, "unknown GEMM variant %d", variant);
 }
 
+int lofgb_gemm_f32(const float* A, int64_t lda, int trans_a, const float* B, int64_t ldb,
+                   int trans_b, float* D, int64_t ldd, int M, int N, int K, int accum_mant_bits,
+                   int mode, float alpha, int variant, int chunk, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+    return gemm_impl(A, lda, 0, trans_a, B, ldb, 0, trans_b, D, ldd, 0, M, N, K, 1,
+                     accum_mant_bits, mode, alpha, variant, chunk, workspace, workspace_bytes,
+                     stream);
+}
+
 size_t lofgb_gemm_tc_workspace_size(int M, int N, int K) {
     if (M <= 0 || N <= 0 || K <= 0) return 0;
-    return gemm_tc_workspace(M, N, K);
+    return gemm_tc_workspace(M, N, K, 1);
+}
+
+int lofgb_gemm_batched_f32(const float* A, int64_t lda, int64_t stride_a, int trans_a,
+                           const float* B, int64_t ldb, int64_t stride_b, int trans_b, float* D,
+                           int64_t ldd, int64_t stride_d, int M, int N, int K, int batch,
+                           int accum_mant_bits, int mode, float alpha, int variant, int chunk,
+                           void* workspace, size_t workspace_bytes, void* stream) {
+    return gemm_impl(A, lda, stride_a, trans_a, B, ldb, stride_b, trans_b, D, ldd, stride_d, M,
+                     N, K, batch, accum_mant_bits, mode, alpha, variant, chunk, workspace,
+                     workspace_bytes, stream);
+}
+
+size_t lofgb_gemm_batched_tc_workspace_size(int M, int N, int K, int batch) {
+    if (M <= 0 || N <= 0 || K <= 0 || batch <= 0) return 0;
+    return gemm_tc_workspace(M, N, K, batch);
 }
 
 int lofgb_gemm_f64_ref(const float* A, int64_t lda, int trans_a, const float* B, int64_t ldb,

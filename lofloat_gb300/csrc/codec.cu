@@ -1,0 +1,430 @@
+// codec.cu — low-precision storage codec: FP32 <-> packed n-bit codes.
+//
+// Replaces LoF_encode_cuda / LoF_decode_cuda (src/lo_pack.hpp:474-532), which
+// run one thread per group, stage the group in a 64-float local array and
+// set or read the code bits one at a time through byte read-modify-writes.
+//
+// Here a warp owns a tile of 1024 consecutive values (32 per lane). A tile is
+// always a whole number of groups (32 n bits hold 4 gcd(n, 8) or 2 gcd(n, 16)
+// groups), so every lane packs its 32 codes into exactly n 32-bit words on its
+// own, with no cross-lane bit exchange. FP32 values and packed words move
+// between HBM and registers through shared memory so that every global access
+// is a coalesced 128-byte warp transaction; the stride of 33 words per lane in
+// shared memory keeps the per-lane accesses free of bank conflicts. The code
+// width n (1..16) and the group order are template parameters, so the bit
+// positions fold to constants.
+//
+// Per element (codec_encode / codec_decode below) the arithmetic is
+// convert_float_to_rep / convert_rep_to_float of src/lo_pack.hpp:109-320,
+// restated with the shared RoundMantissa (round_mantissa in lof_round.cuh).
+// HBM-bound: 4 + n/8 bytes per element either way.
+#include <cuda_runtime.h>
+
+#include "lof_round.cuh"
+
+namespace lofgb {
+
+namespace {
+
+constexpr int CT = 128;             // threads per CTA (4 warps)
+constexpr int TILE = 1024;          // values per warp tile
+
+struct CodecArg {
+    int n, m, bias, is_signed, has_inf, nan3109;
+    uint32_t inf_or, inf_match, pos_inf, qnan, snan;
+    int nan_kind, neg_to_nan;
+    int mode, sat, len;
+    uint64_t seed, offset;
+};
+
+__device__ __forceinline__ bool c_is_nan(uint32_t rep, const CodecArg& a) {
+    if (a.nan_kind == LOFGB_NAN_NONE) return false;
+    if (a.nan_kind == LOFGB_NAN_PATTERN) return rep == a.qnan;
+    const uint32_t mag = a.is_signed ? rep & ((1u << (a.n - 1)) - 1u) : rep;
+    const int ebits = a.n - a.m - (a.is_signed ? 1 : 0);
+    return mag > (((1u << ebits) - 1u) << a.m);
+}
+
+__device__ __forceinline__ int clz32(uint32_t v) { return __clz((int)v); }
+
+// convert_float_to_rep, src/lo_pack.hpp:109-287. RoundMantissa sees the
+// reference's default positive-sign flag (false).
+template <int MODE>
+__device__ uint32_t codec_encode(float from, const CodecArg& a, uint64_t r) {
+    const int n = a.n, toMant = a.m;
+    const int toExpBits = a.is_signed ? n - toMant - 1 : n - toMant;
+    const int kExponentOffset = a.bias - 127;
+    const int kDigitShift = toMant - 23;
+    const int toMinExp = 1 - a.bias;
+    const int toMaxExp = (1 << toExpBits) - 1 - a.bias;
+    const uint32_t signmask = a.is_signed ? (1u << (n - 1)) : 0u;
+    const uint32_t maxFinite = a.has_inf ? a.pos_inf - 1u
+                                         : (a.is_signed ? (((1u << n) - 1u) >> 1) : ((1u << n) - 1u));
+    const uint32_t infRep = a.has_inf ? a.pos_inf : maxFinite;
+    const uint32_t fb = __float_as_uint(from);
+    const bool neg = (fb >> 31) != 0;
+    auto with_sign = [&](uint32_t mag) -> uint32_t {
+        if (!neg || !a.is_signed) return mag;
+        if (mag == 0u && c_is_nan(signmask, a)) return 0u;
+        return mag | signmask;
+    };
+    if (!a.is_signed && neg) return a.neg_to_nan ? (a.nan3109 ? a.qnan : a.snan) : 0u;
+    const uint32_t from_bits = fb & 0x7FFFFFFFu;
+    if (from_bits == 0x7F800000u)
+        return with_sign((a.sat != LOFGB_SAT_FINITE && a.has_inf) ? infRep : maxFinite);
+    if (from_bits > 0x7F800000u) return a.qnan;
+    if (from_bits == 0u) return with_sign(0u);
+    const int bfe = (int)(from_bits >> 23);
+    if (toMinExp < -125 && bfe == 0) {  // branch 1
+        uint64_t bits = from_bits;
+        const int norm = clz32(from_bits) - (32 - 23) + 1;
+        const int bexp = kExponentOffset - norm + 1;
+        if (bexp <= 0) {
+            if (kExponentOffset < 64) bits <<= kExponentOffset;
+        } else {
+            bits <<= norm;
+            bits &= ~(1ull << 23);
+            bits |= (uint64_t)bexp << 23;
+        }
+        bits = round_mantissa<MODE, 64, uint64_t>(bits, -kDigitShift, a.mode, a.len, false, r);
+        bits >>= -kDigitShift;
+        return with_sign((uint32_t)bits);
+    }
+    if (toMinExp > -125) {  // branch 2: target-subnormal or zero
+        const int bte = (bfe - 127) + a.bias;
+        if (bte <= 0) {
+            const uint32_t lead = bfe > 0 ? 1u : 0u;
+            const int shift = -kDigitShift - bte + (int)lead;
+            uint32_t rfb = (from_bits & 0x7FFFFFu) | (lead << 23);
+            uint32_t bits = 0;
+            if (shift <= 24) {
+                rfb = round_mantissa<MODE, 32, uint32_t>(rfb, shift, a.mode, a.len, false, r);
+                bits = rfb >> shift;
+            } else {
+                const int mode = MODE >= 0 ? MODE : a.mode;
+                switch (mode) {
+                case LOFGB_RTO:
+                case LOFGB_RAFZ: bits = rfb > 0 ? 1u : 0u; break;
+                case LOFGB_RU: bits = (rfb && !neg) ? 1u : 0u; break;
+                case LOFGB_RD: bits = (rfb && neg) ? 1u : 0u; break;
+                case LOFGB_SR_A: case LOFGB_SR_B: case LOFGB_SR_C: case LOFGB_SR_D:
+                case LOFGB_TRUE_SR: case LOFGB_PROB: {
+                    // shifts of 64 or more are undefined in the reference: 0
+                    const uint64_t w = round_mantissa<MODE, 64, uint64_t>(rfb, shift, a.mode, a.len,
+                                                                          false, r);
+                    bits = shift >= 64 ? 0u : (uint32_t)(w >> shift);
+                    break;
+                }
+                default: bits = 0; break;
+                }
+            }
+            return with_sign(bits);
+        }
+    }
+    uint64_t rfb = from_bits;  // normal path
+    rfb = round_mantissa<MODE, 64, uint64_t>(rfb, -kDigitShift, a.mode, a.len, false, r);
+    rfb &= ~((1ull << (-kDigitShift)) - 1ull);
+    rfb += (uint64_t)(int64_t)kExponentOffset << 23;
+    const uint64_t aligned_highest = (uint64_t)maxFinite << (-kDigitShift);
+    const uint32_t bits = (uint32_t)(rfb >> (-kDigitShift));
+    const bool narrower = (toMaxExp < 128) || (toMaxExp == 128 && toMant + 1 < 24);
+    if (narrower && rfb > aligned_highest)
+        return with_sign((a.sat == LOFGB_OVF_INF && a.has_inf) ? infRep : maxFinite);
+    return with_sign(bits);
+}
+
+// convert_rep_to_float, src/lo_pack.hpp:293-320.
+__device__ __forceinline__ float codec_decode(uint32_t rep, const CodecArg& a) {
+    const int n = a.n;
+    rep &= (1u << n) - 1u;
+    const bool sign = a.is_signed ? ((rep >> (n - 1)) & 1u) != 0 : false;
+    const uint32_t mag = a.is_signed ? rep & ((1u << (n - 1)) - 1u) : rep;
+    if (a.has_inf && (rep | a.inf_or) == a.inf_match) return sign ? -INFINITY : INFINITY;
+    if (c_is_nan(rep, a)) return __uint_as_float(0x7FC00000u);
+    const uint32_t e = mag >> a.m, mf = mag & ((1u << a.m) - 1u);
+    double v;
+    if (e == 0) v = ldexp((double)mf, 1 - a.bias - a.m);
+    else v = ldexp(1.0 + (double)mf / (double)(1u << a.m), (int)e - a.bias);
+    return __double2float_rn(sign ? -v : v);
+}
+
+constexpr int cgcd(int x, int y) { return y == 0 ? x : cgcd(y, x % y); }
+
+// Codes per group for width N: lcm(N, 8) bits for N <= 8, lcm(N, 16) above.
+template <int N>
+struct Group {
+    static constexpr int AL = N <= 8 ? 8 : 16;
+    static constexpr int BITS = N / cgcd(N, AL) * AL;
+    static constexpr int GC = BITS / N;
+};
+
+// The chunk element whose code fills slot s of the lane's bit stream: slots
+// run in stream order; within a group they hold elements in order (forward)
+// or in reverse order (reverse).
+template <int N, bool REV>
+__device__ __forceinline__ int slot_element(int s) {
+    constexpr int GC = Group<N>::GC;
+    if (!REV) return s;
+    const int g = s / GC, k = s - g * GC;
+    return g * GC + (GC - 1 - k);
+}
+
+template <int N, bool REV, int MODE>
+__global__ void __launch_bounds__(CT)
+encode_kernel(const float* __restrict__ src, uint32_t* __restrict__ dst, int64_t count,
+              int64_t out_bytes, CodecArg a) {
+    __shared__ float sx[CT / 32][TILE + 32];
+    __shared__ uint32_t sw[CT / 32][32 * (N + 1)];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t ntiles = (count + TILE - 1) / TILE;
+    const int64_t wstride = (int64_t)gridDim.x * (CT / 32);
+    for (int64_t t = (int64_t)blockIdx.x * (CT / 32) + wib; t < ntiles; t += wstride) {
+        const int64_t e0 = t * TILE;
+        const bool full = e0 + TILE <= count;
+        // coalesced loads into the lane-major shared tile (element e at e + e/32)
+#pragma unroll
+        for (int j = 0; j < TILE / 32; ++j) {
+            const int e = j * 32 + lane;
+            float v = 0.0f;
+            if (full || e0 + e < count) v = __ldcs(src + e0 + e);
+            sx[wib][e + (e >> 5)] = v;
+        }
+        __syncwarp();
+        // this lane's 32 codes, appended to a bit stream of N words
+        uint64_t acc = 0;
+        int fill = 0, widx = 0;
+        uint32_t* out = &sw[wib][lane * (N + 1)];
+#pragma unroll 2
+        for (int s = 0; s < 32; ++s) {
+            const int i = slot_element<N, REV>(s);
+            const int e = lane * 32 + i;
+            const float x = sx[wib][e + lane];
+            const uint64_t r = mode_is_stochastic(MODE >= 0 ? MODE : a.mode)
+                                   ? rng64(a.seed, a.offset + (uint64_t)(e0 + e)) : 0ull;
+            const uint32_t code = codec_encode<MODE>(x, a, r) & ((1u << N) - 1u);
+            acc |= (uint64_t)code << fill;
+            fill += N;
+            if (fill >= 32) {
+                out[widx++] = (uint32_t)acc;
+                acc >>= 32;
+                fill -= 32;
+            }
+        }
+        __syncwarp();
+        // coalesced stores of the tile's 32 N words (bytes past out_bytes are not written)
+        const int64_t w0 = t * (32 * N);
+        for (int w = lane; w < 32 * N; w += 32) {
+            const uint32_t v = sw[wib][(w / N) * (N + 1) + (w % N)];
+            const int64_t byte = (w0 + w) * 4;
+            if (byte + 4 <= out_bytes) {
+                dst[w0 + w] = v;
+            } else if (byte < out_bytes) {
+                uint8_t* d8 = reinterpret_cast<uint8_t*>(dst) + byte;
+                for (int q = 0; q < 4 && byte + q < out_bytes; ++q) d8[q] = (uint8_t)(v >> (8 * q));
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <int N, bool REV>
+__global__ void __launch_bounds__(CT)
+decode_kernel(const uint32_t* __restrict__ src, float* __restrict__ dst, int64_t count,
+              int64_t in_bytes, CodecArg a) {
+    __shared__ float sx[CT / 32][TILE + 32];
+    __shared__ uint32_t sw[CT / 32][32 * (N + 1)];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t ntiles = (count + TILE - 1) / TILE;
+    const int64_t wstride = (int64_t)gridDim.x * (CT / 32);
+    for (int64_t t = (int64_t)blockIdx.x * (CT / 32) + wib; t < ntiles; t += wstride) {
+        const int64_t e0 = t * TILE;
+        const int64_t w0 = t * (32 * N);
+        for (int w = lane; w < 32 * N; w += 32) {
+            const int64_t byte = (w0 + w) * 4;
+            uint32_t v = 0;
+            if (byte + 4 <= in_bytes) {
+                v = __ldcs(src + w0 + w);
+            } else if (byte < in_bytes) {
+                const uint8_t* s8 = reinterpret_cast<const uint8_t*>(src) + byte;
+                for (int q = 0; q < 4 && byte + q < in_bytes; ++q) v |= (uint32_t)s8[q] << (8 * q);
+            }
+            sw[wib][(w / N) * (N + 1) + (w % N)] = v;
+        }
+        __syncwarp();
+        const uint32_t* in = &sw[wib][lane * (N + 1)];
+        uint64_t buf = 0;
+        int avail = 0, widx = 0;
+#pragma unroll 2
+        for (int s = 0; s < 32; ++s) {
+            if (avail < N) {
+                buf |= (uint64_t)in[widx++] << avail;
+                avail += 32;
+            }
+            const uint32_t code = (uint32_t)buf & ((1u << N) - 1u);
+            buf >>= N;
+            avail -= N;
+            const int e = lane * 32 + slot_element<N, REV>(s);
+            sx[wib][e + lane] = codec_decode(code, a);
+        }
+        __syncwarp();
+        const bool full = e0 + TILE <= count;
+#pragma unroll
+        for (int j = 0; j < TILE / 32; ++j) {
+            const int e = j * 32 + lane;
+            if (full || e0 + e < count) __stcs(dst + e0 + e, sx[wib][e + (e >> 5)]);
+        }
+        __syncwarp();
+    }
+}
+
+int64_t packed_bytes(int n, int64_t count) {
+    const int al = n <= 8 ? 8 : 16;
+    int x = n, y = al;
+    while (y) { const int t = x % y; x = y; y = t; }
+    const int gbits = n / x * al, gc = gbits / n;
+    return (count + gc - 1) / gc * (gbits / 8);
+}
+
+int make_codec_arg(CodecArg* a, const lofgb_codec_format* f, int mode, int sat, int len) {
+    if (!f) return set_error(LOFGB_ERR_NULL, "NULL codec format");
+    const lofgb_format& F = f->fmt;
+    if (F.bitwidth < 1 || F.bitwidth > 16)
+        return set_error(LOFGB_ERR_FORMAT, "codec bitwidth %d outside [1, 16]", F.bitwidth);
+    const int ebits = F.bitwidth - F.mantissa_bits - (F.signedness == LOFGB_SIGNED ? 1 : 0);
+    if (F.mantissa_bits < 0 || ebits < 0)
+        return set_error(LOFGB_ERR_FORMAT, "codec mantissa bits %d do not fit %d bits",
+                         F.mantissa_bits, F.bitwidth);
+    if (F.bias < -(1 << 20) || F.bias > (1 << 20))
+        return set_error(LOFGB_ERR_FORMAT, "bias %d outside [-2^20, 2^20]", F.bias);
+    if (f->nan_kind > LOFGB_NAN_NONE) return set_error(LOFGB_ERR_FORMAT, "unknown NaN kind");
+    if (mode < 0 || mode >= LOFGB_NUM_MODES) return set_error(LOFGB_ERR_MODE, "unknown mode %d", mode);
+    if (sat < 0 || sat > LOFGB_SAT_PROPAGATE) return set_error(LOFGB_ERR_MODE, "unknown saturation mode %d", sat);
+    if (len < 0 || len > 62) return set_error(LOFGB_ERR_MODE, "stoch_len %d outside [0, 62]", len);
+    a->n = F.bitwidth;
+    a->m = F.mantissa_bits;
+    a->bias = F.bias;
+    a->is_signed = F.signedness == LOFGB_SIGNED;
+    a->has_inf = F.inf_behavior != LOFGB_INF_SATURATING;
+    a->nan3109 = F.nan_behavior == LOFGB_NAN_3109;
+    a->inf_or = f->inf_or;
+    a->inf_match = f->inf_match;
+    a->pos_inf = f->pos_inf;
+    a->qnan = f->qnan;
+    a->snan = f->snan;
+    a->nan_kind = f->nan_kind;
+    a->neg_to_nan = f->neg_to_nan;
+    a->mode = mode;
+    a->sat = sat;
+    a->len = len;
+    return LOFGB_OK;
+}
+
+int grid_for(int64_t count) {
+    const int64_t tiles = (count + TILE - 1) / TILE;
+    int64_t g = (tiles + (CT / 32) - 1) / (CT / 32);
+    const int64_t maxg = (int64_t)sm_count() * (2048 / CT);
+    if (g < 1) g = 1;
+    return (int)(g < maxg ? g : maxg);
+}
+
+template <int N>
+int launch_encode_n(const float* src, uint8_t* dst, int64_t count, int reverse, const CodecArg& a,
+                    cudaStream_t st) {
+    const int grid = grid_for(count);
+    const int64_t ob = packed_bytes(N, count);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+#define LOFGB_ENC(R, M) encode_kernel<N, R, M><<<grid, CT, 0, st>>>(src, d, count, ob, a)
+    if (a.mode == LOFGB_RNE) {
+        if (reverse) LOFGB_ENC(true, LOFGB_RNE); else LOFGB_ENC(false, LOFGB_RNE);
+    } else {
+        if (reverse) LOFGB_ENC(true, -1); else LOFGB_ENC(false, -1);
+    }
+#undef LOFGB_ENC
+    return check_launch("encode_kernel");
+}
+
+template <int N>
+int launch_decode_n(const uint8_t* src, float* dst, int64_t count, int reverse, const CodecArg& a,
+                    cudaStream_t st) {
+    const int grid = grid_for(count);
+    const int64_t ib = packed_bytes(N, count);
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+    if (reverse) decode_kernel<N, true><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
+    else decode_kernel<N, false><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
+    return check_launch("decode_kernel");
+}
+
+#define LOFGB_BY_N(FN, ...)                                                                   \
+    switch (n) {                                                                              \
+    case 1: return FN<1>(__VA_ARGS__);   case 2: return FN<2>(__VA_ARGS__);                   \
+    case 3: return FN<3>(__VA_ARGS__);   case 4: return FN<4>(__VA_ARGS__);                   \
+    case 5: return FN<5>(__VA_ARGS__);   case 6: return FN<6>(__VA_ARGS__);                   \
+    case 7: return FN<7>(__VA_ARGS__);   case 8: return FN<8>(__VA_ARGS__);                   \
+    case 9: return FN<9>(__VA_ARGS__);   case 10: return FN<10>(__VA_ARGS__);                 \
+    case 11: return FN<11>(__VA_ARGS__); case 12: return FN<12>(__VA_ARGS__);                 \
+    case 13: return FN<13>(__VA_ARGS__); case 14: return FN<14>(__VA_ARGS__);                 \
+    case 15: return FN<15>(__VA_ARGS__); default: return FN<16>(__VA_ARGS__);                 \
+    }
+
+int codec_pointers(const void* a, const void* b, int64_t count) {
+    if (count < 0) return set_error(LOFGB_ERR_SIZE, "negative count");
+    if (count > 0 && (!a || !b)) return set_error(LOFGB_ERR_NULL, "NULL buffer");
+    if (count > 0 && ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 3))
+        return set_error(LOFGB_ERR_SIZE, "codec buffers must be 4-byte aligned");
+    return LOFGB_OK;
+}
+
+}  // namespace
+
+}  // namespace lofgb
+
+using namespace lofgb;
+
+extern "C" {
+
+size_t lofgb_packed_size(int bitwidth, int64_t count) {
+    if (bitwidth < 1 || bitwidth > 16 || count < 0) return 0;
+    return (size_t)packed_bytes(bitwidth, count);
+}
+
+int lofgb_encode_f32(uint8_t* dst, const float* src, int64_t count, const lofgb_codec_format* fmt,
+                     int mode, int sat_mode, int stoch_len, int reverse, uint64_t seed,
+                     uint64_t offset, void* stream) {
+    clear_error();
+    CodecArg a;
+    int st = make_codec_arg(&a, fmt, mode, sat_mode, stoch_len);
+    if (st) return st;
+    if ((st = codec_pointers(src, dst, count))) return st;
+    if (count == 0) return LOFGB_OK;
+    const int64_t ob = packed_bytes(a.n, count);
+    const char* s = reinterpret_cast<const char*>(src);
+    const char* d = reinterpret_cast<const char*>(dst);
+    if (s < d + ob && d < s + count * 4)
+        return set_error(LOFGB_ERR_ALIAS, "packed output overlaps the input");
+    a.seed = seed;
+    a.offset = offset;
+    const int n = a.n;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    LOFGB_BY_N(launch_encode_n, src, dst, count, reverse, a, cs)
+}
+
+int lofgb_decode_f32(float* dst, const uint8_t* src, int64_t count, const lofgb_codec_format* fmt,
+                     int reverse, void* stream) {
+    clear_error();
+    CodecArg a;
+    int st = make_codec_arg(&a, fmt, LOFGB_RNE, 0, 0);
+    if (st) return st;
+    if ((st = codec_pointers(src, dst, count))) return st;
+    if (count == 0) return LOFGB_OK;
+    const int64_t ib = packed_bytes(a.n, count);
+    const char* s = reinterpret_cast<const char*>(src);
+    const char* d = reinterpret_cast<const char*>(dst);
+    if (s < d + count * 4 && d < s + ib)
+        return set_error(LOFGB_ERR_ALIAS, "decoded output overlaps the input");
+    a.seed = a.offset = 0;
+    const int n = a.n;
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    LOFGB_BY_N(launch_decode_n, src, dst, count, reverse, a, cs)
+}
+
+}  // extern "C"

@@ -25,13 +25,13 @@ namespace lofgb {
 
 namespace {
 
+// One 128 x 128 output tile of one GEMM of the batch.
 template <bool ROUND>
-__global__ void __launch_bounds__(NT, 2)
-gemm_plain_kernel(const float* __restrict__ A, int64_t lda, int ta, const float* __restrict__ B,
-                  int64_t ldb, int tb, float* __restrict__ D, int64_t ldd, int M, int N, int K,
-                  int ro, float alpha) {
-    __shared__ __align__(16) float As[2][BK][BM + PAD];
-    __shared__ __align__(16) float Bs[2][BK][BN + PAD];
+__device__ __forceinline__ void plain_tile(float (*As)[BK][BM + PAD], float (*Bs)[BK][BN + PAD],
+                                           const float* __restrict__ A, int64_t lda, int ta,
+                                           const float* __restrict__ B, int64_t ldb, int tb,
+                                           float* __restrict__ D, int64_t ldd, int M, int N,
+                                           int K, int ro, float alpha) {
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
@@ -94,6 +94,22 @@ gemm_plain_kernel(const float* __restrict__ A, int64_t lda, int ta, const float*
     }
 }
 
+// blockIdx.z walks the batch (strided-batched GEMM; batch 1 for a single one).
+template <bool ROUND>
+__global__ void __launch_bounds__(NT, 2)
+gemm_plain_kernel(const float* __restrict__ A, int64_t lda, int64_t sa, int ta,
+                  const float* __restrict__ B, int64_t ldb, int64_t sb, int tb,
+                  float* __restrict__ D, int64_t ldd, int64_t sd, int M, int N, int K, int batch,
+                  int ro, float alpha) {
+    __shared__ __align__(16) float As[2][BK][BM + PAD];
+    __shared__ __align__(16) float Bs[2][BK][BN + PAD];
+    for (int z = blockIdx.z; z < batch; z += gridDim.z) {
+        plain_tile<ROUND>(As, Bs, A + (int64_t)z * sa, lda, ta, B + (int64_t)z * sb, ldb, tb,
+                          D + (int64_t)z * sd, ldd, M, N, K, ro, alpha);
+        __syncthreads();  // the next batch entry refills the shared tiles
+    }
+}
+
 // FP64 oracle: D = sum_k (double)A[i,k] * (double)B[k,j], 64x64 tiles,
 // 256 threads, 4x4 outputs per thread.
 __global__ void __launch_bounds__(256)
@@ -133,17 +149,19 @@ gemm_f64_kernel(const float* __restrict__ A, int64_t lda, int ta, const float* _
 
 }  // namespace
 
-int launch_gemm_plain(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
-                      float* D, int64_t ldd, int M, int N, int K, int mbits, float alpha,
-                      void* stream) {
+int launch_gemm_plain(const float* A, int64_t lda, int64_t sa, int ta, const float* B,
+                      int64_t ldb, int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M,
+                      int N, int K, int batch, int mbits, float alpha, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch < 65535 ? batch : 65535);
     if (grid.y > 65535) return set_error(LOFGB_ERR_SIZE, "M too large for the plain GEMM grid");
     const int ro = 23 - mbits;
     if (ro > 0)
-        gemm_plain_kernel<true><<<grid, NT, 0, st>>>(A, lda, ta, B, ldb, tb, D, ldd, M, N, K, ro, alpha);
+        gemm_plain_kernel<true><<<grid, NT, 0, st>>>(A, lda, sa, ta, B, ldb, sb, tb, D, ldd, sd, M,
+                                                     N, K, batch, ro, alpha);
     else
-        gemm_plain_kernel<false><<<grid, NT, 0, st>>>(A, lda, ta, B, ldb, tb, D, ldd, M, N, K, ro, alpha);
+        gemm_plain_kernel<false><<<grid, NT, 0, st>>>(A, lda, sa, ta, B, ldb, sb, tb, D, ldd, sd, M,
+                                                      N, K, batch, ro, alpha);
     return check_launch("gemm_plain_kernel");
 }
 

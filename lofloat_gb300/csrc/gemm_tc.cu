@@ -68,6 +68,9 @@ struct TcParams {
     int* status;           // workspace status word
     int64_t img_L;         // conv output: columns per image (0: plain row-major D)
     int64_t img_stride;    // conv output: elements per image
+    int batch;             // strided batch: GEMM b reads split rows b*Mp.. / b*Np..
+    int Mp, Np;            // padded rows of one GEMM's A / B split
+    int64_t stride_d;      // elements between consecutive D matrices
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -214,6 +217,7 @@ struct TileInfo {
     float* D;
     int64_t ldd;
     int M, N, m0, n0, Kp, chunk16, ro;
+    int a_r0, b_r0;             // first split rows of the A / B tiles (TMA coordinates)
     float alpha;
     // conv2d output (img_L > 0): column j = img * img_L + l of row i is
     // stored at D[img * img_stride + i * ldd + l]
@@ -224,17 +228,21 @@ struct TileInfo {
 struct SingleSrc {
     const CUtensorMap* m[4];
     TcParams prm;
-    __device__ __forceinline__ int count() const { return prm.tiles_m * prm.tiles_n; }
+    __device__ __forceinline__ int count() const { return prm.batch * prm.tiles_m * prm.tiles_n; }
     __device__ __forceinline__ TileInfo get(int t) const {
         TileInfo ti;
 #pragma unroll
         for (int i = 0; i < 4; ++i) ti.map[i] = m[i];
-        ti.D = prm.D;
+        const int per = prm.tiles_m * prm.tiles_n;
+        const int b = t / per, r = t - b * per;
+        ti.D = prm.D + (int64_t)b * prm.stride_d;
         ti.ldd = prm.ldd;
         ti.M = prm.M;
         ti.N = prm.N;
-        ti.m0 = (t / prm.tiles_n) * TBM;
-        ti.n0 = (t % prm.tiles_n) * TBN;
+        ti.m0 = (r / prm.tiles_n) * TBM;
+        ti.n0 = (r % prm.tiles_n) * TBN;
+        ti.a_r0 = b * prm.Mp + ti.m0;
+        ti.b_r0 = b * prm.Np + ti.n0;
         ti.Kp = prm.Kp;
         ti.chunk16 = prm.chunk16;
         ti.ro = prm.ro;
@@ -289,6 +297,8 @@ struct GroupedSrc {
         ti.N = g->N;
         ti.m0 = r.m0;
         ti.n0 = r.n0;
+        ti.a_r0 = r.m0;
+        ti.b_r0 = r.n0;
         ti.Kp = g->Kp;
         ti.chunk16 = g->chunk16;
         ti.ro = g->ro;
@@ -358,10 +368,10 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                     if (!mbar_wait(bar_empty + 8 * s, ph ^ 1u, abort_flag, status)) { ok = false; break; }
                     const uint32_t base = smem_u32(tiles + s * STAGE_BYTES);
                     mbar_arrive_expect_tx(bar_full + 8 * s, STAGE_BYTES);
-                    tma_load_2d(base + 0 * TILE_BYTES, ti.map[0], ks * SK, ti.m0, bar_full + 8 * s);
-                    tma_load_2d(base + 1 * TILE_BYTES, ti.map[1], ks * SK, ti.m0, bar_full + 8 * s);
-                    tma_load_2d(base + 2 * TILE_BYTES, ti.map[2], ks * SK, ti.n0, bar_full + 8 * s);
-                    tma_load_2d(base + 3 * TILE_BYTES, ti.map[3], ks * SK, ti.n0, bar_full + 8 * s);
+                    tma_load_2d(base + 0 * TILE_BYTES, ti.map[0], ks * SK, ti.a_r0, bar_full + 8 * s);
+                    tma_load_2d(base + 1 * TILE_BYTES, ti.map[1], ks * SK, ti.a_r0, bar_full + 8 * s);
+                    tma_load_2d(base + 2 * TILE_BYTES, ti.map[2], ks * SK, ti.b_r0, bar_full + 8 * s);
+                    tma_load_2d(base + 3 * TILE_BYTES, ti.map[3], ks * SK, ti.b_r0, bar_full + 8 * s);
                 }
             }
             if (!ok) {
@@ -542,11 +552,18 @@ __device__ __forceinline__ void split_tile(const float* __restrict__ src, int64_
     __syncthreads();
 }
 
+// blockIdx.z walks a strided batch: operand z at src + z * src_stride, its
+// split at hi / lo + z * R * Kp.
 __global__ void __launch_bounds__(256)
-split_bf16_kernel(const float* __restrict__ src, int64_t ld, int kmajor, int rows, int K, int R,
-                  int Kp, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+split_bf16_kernel(const float* __restrict__ src, int64_t ld, int64_t src_stride, int kmajor,
+                  int rows, int K, int R, int Kp, int batch, __nv_bfloat16* __restrict__ hi,
+                  __nv_bfloat16* __restrict__ lo) {
     __shared__ float tile[32][65];
-    split_tile(src, ld, kmajor, rows, K, R, Kp, hi, lo, blockIdx.y, blockIdx.x, tile);
+    for (int z = blockIdx.z; z < batch; z += gridDim.z) {
+        const int64_t off = (int64_t)z * R * Kp;
+        split_tile(src + (int64_t)z * src_stride, ld, kmajor, rows, K, R, Kp, hi + off, lo + off,
+                   blockIdx.y, blockIdx.x, tile);
+    }
 }
 
 // All operands of a grouped launch: items are 32 x 64 tiles, walked
@@ -586,12 +603,13 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 }  // namespace
 
-WsLayout ws_layout(int M, int N, int K) {
+WsLayout ws_layout(int M, int N, int K, int batch) {
     WsLayout w;
     w.Mp = (int)align_up((size_t)M, TBM);
     w.Np = (int)align_up((size_t)N, TBN);
     w.Kp = (int)align_up((size_t)K, SK);
-    const size_t a = (size_t)w.Mp * w.Kp * 2, b = (size_t)w.Np * w.Kp * 2;
+    w.batch = batch;
+    const size_t a = (size_t)batch * w.Mp * w.Kp * 2, b = (size_t)batch * w.Np * w.Kp * 2;
     w.status = 0;
     w.ahi = 1024;
     w.alo = align_up(w.ahi + a, 1024);
@@ -633,21 +651,24 @@ int make_map(CUtensorMap* map, void* base, int rows, int Kp) {
 
 }  // namespace
 
-size_t gemm_tc_workspace(int M, int N, int K) { return ws_layout(M, N, K).total; }
+size_t gemm_tc_workspace(int M, int N, int K, int batch) { return ws_layout(M, N, K, batch).total; }
 
-int launch_gemm_tc(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
-                   float* D, int64_t ldd, int M, int N, int K, int mbits, float alpha, int chunk,
-                   void* workspace, size_t workspace_bytes, void* stream) {
+int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float* B, int64_t ldb,
+                   int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M, int N, int K,
+                   int batch, int mbits, float alpha, int chunk, void* workspace,
+                   size_t workspace_bytes, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (K == 0) {
         // no products: D = alpha * (+0)
-        for (int i = 0; i < M; ++i) {
-            cudaError_t e = cudaMemsetAsync(D + (int64_t)i * ldd, 0, sizeof(float) * N, st);
-            if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
-        }
+        for (int z = 0; z < batch; ++z)
+            for (int i = 0; i < M; ++i) {
+                cudaError_t e = cudaMemsetAsync(D + (int64_t)z * sd + (int64_t)i * ldd, 0,
+                                                sizeof(float) * N, st);
+                if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+            }
         return LOFGB_OK;
     }
-    const WsLayout w = ws_layout(M, N, K);
+    const WsLayout w = ws_layout(M, N, K, batch);
     if (!workspace || workspace_bytes < w.total || (reinterpret_cast<uintptr_t>(workspace) & 255))
         return set_error(LOFGB_ERR_WORKSPACE, "need %zu bytes of 256-byte aligned workspace", w.total);
     uint8_t* ws = static_cast<uint8_t*>(workspace);
@@ -659,18 +680,21 @@ int launch_gemm_tc(const float* A, int64_t lda, int ta, const float* B, int64_t 
     cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), st);
     if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
 
-    dim3 sb(256);
-    split_bf16_kernel<<<dim3(w.Kp / 64, w.Mp / 32), sb, 0, st>>>(A, lda, ta ? 0 : 1, M, K, w.Mp, w.Kp, ahi, alo);
+    dim3 sb256(256);
+    const unsigned gz = batch < 65535 ? batch : 65535;
+    split_bf16_kernel<<<dim3(w.Kp / 64, w.Mp / 32, gz), sb256, 0, st>>>(A, lda, sa, ta ? 0 : 1, M, K,
+                                                                        w.Mp, w.Kp, batch, ahi, alo);
     int rc = check_launch("split_bf16_kernel(A)");
     if (rc) return rc;
-    split_bf16_kernel<<<dim3(w.Kp / 64, w.Np / 32), sb, 0, st>>>(B, ldb, tb ? 1 : 0, N, K, w.Np, w.Kp, bhi, blo);
+    split_bf16_kernel<<<dim3(w.Kp / 64, w.Np / 32, gz), sb256, 0, st>>>(B, ldb, sb, tb ? 1 : 0, N, K,
+                                                                        w.Np, w.Kp, batch, bhi, blo);
     if ((rc = check_launch("split_bf16_kernel(B)"))) return rc;
-    return launch_tc_presplit(ws, w, D, ldd, M, N, mbits, alpha, chunk, 0, 0, stream);
+    return launch_tc_presplit(ws, w, D, ldd, sd, M, N, mbits, alpha, chunk, 0, 0, stream);
 }
 
-int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int M, int N,
-                       int mbits, float alpha, int chunk, int64_t img_L, int64_t img_stride,
-                       void* stream) {
+int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int64_t sd, int M,
+                       int N, int mbits, float alpha, int chunk, int64_t img_L,
+                       int64_t img_stride, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     auto* ahi = reinterpret_cast<__nv_bfloat16*>(ws + w.ahi);
     auto* alo = reinterpret_cast<__nv_bfloat16*>(ws + w.alo);
@@ -678,10 +702,10 @@ int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, in
     auto* blo = reinterpret_cast<__nv_bfloat16*>(ws + w.blo);
     int rc;
     CUtensorMap m_ahi, m_alo, m_bhi, m_blo;
-    if ((rc = make_map(&m_ahi, ahi, w.Mp, w.Kp))) return rc;
-    if ((rc = make_map(&m_alo, alo, w.Mp, w.Kp))) return rc;
-    if ((rc = make_map(&m_bhi, bhi, w.Np, w.Kp))) return rc;
-    if ((rc = make_map(&m_blo, blo, w.Np, w.Kp))) return rc;
+    if ((rc = make_map(&m_ahi, ahi, w.batch * w.Mp, w.Kp))) return rc;
+    if ((rc = make_map(&m_alo, alo, w.batch * w.Mp, w.Kp))) return rc;
+    if ((rc = make_map(&m_bhi, bhi, w.batch * w.Np, w.Kp))) return rc;
+    if ((rc = make_map(&m_blo, blo, w.batch * w.Np, w.Kp))) return rc;
 
     TcParams p;
     p.D = D;
@@ -697,6 +721,10 @@ int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, in
     p.status = reinterpret_cast<int*>(ws + w.status);
     p.img_L = img_L;
     p.img_stride = img_stride;
+    p.batch = w.batch;
+    p.Mp = w.Mp;
+    p.Np = w.Np;
+    p.stride_d = sd;
 
     int dev = 0;
     cudaGetDevice(&dev);
@@ -706,8 +734,9 @@ int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, in
         if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
         if (dev >= 0 && dev < 64) attr_set[dev] = true;
     }
-    const int tiles = p.tiles_m * p.tiles_n;
-    const int grid = tiles < sm_count() ? tiles : sm_count();
+    const int64_t tiles = (int64_t)p.batch * p.tiles_m * p.tiles_n;
+    if (tiles >= ((int64_t)1 << 31)) return set_error(LOFGB_ERR_SIZE, "too many output tiles");
+    const int grid = tiles < sm_count() ? (int)tiles : sm_count();
     gemm_tc_kernel<<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
     return check_launch("gemm_tc_kernel");
 }
@@ -763,7 +792,7 @@ extern "C" int lofgb_gemm_tc_noalloc_f32(const float* A, int64_t lda, int trans_
                                          void* stream) {
     using namespace lofgb;
     if (M > 0 && N > 0 && K > 0) {
-        const size_t need = gemm_tc_workspace(M, N, K);
+        const size_t need = gemm_tc_workspace(M, N, K, 1);
         if (need > NOALLOC_SCRATCH_BYTES)
             return set_error(LOFGB_ERR_WORKSPACE,
                              "no-alloc GEMM needs %zu bytes of scratch; the built-in array holds %zu",

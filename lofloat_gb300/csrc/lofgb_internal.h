@@ -71,18 +71,21 @@ int check_launch(const char* what);
 // Tensor-core GEMM workspace (gemm_tc.cu): a status word, then the BF16 hi /
 // lo splits of A (Mp x Kp) and B (Np x Kp), K-major and zero padded
 // (Mp, Np multiples of 128, Kp of 64), each 1024-byte aligned.
+// A strided batch of GEMMs stacks `batch` such splits (A rows b*Mp.., B rows
+// b*Np..) in each operand region.
 struct WsLayout {
     size_t status, ahi, alo, bhi, blo, total;
-    int Mp, Np, Kp;
+    int Mp, Np, Kp, batch;
 };
-WsLayout ws_layout(int M, int N, int K);
+WsLayout ws_layout(int M, int N, int K, int batch = 1);
 // Runs the chunked tensor-core GEMM on operands already split into `ws`
 // (laid out by ws_layout) whose status word the caller has cleared.
 // img_L > 0 stores conv2d output: column j = img * img_L + l of row i goes to
 // D[img * img_stride + i * ldd + l].
-int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int M, int N,
-                       int mbits, float alpha, int chunk, int64_t img_L, int64_t img_stride,
-                       void* stream);
+// D of batch entry b starts at D + b * sd.
+int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int64_t sd, int M,
+                       int N, int mbits, float alpha, int chunk, int64_t img_L,
+                       int64_t img_stride, void* stream);
 
 // Kernel launchers (one translation unit each).
 int launch_round(int src_bits, bool fmt, const void* in, void* out, int64_t n,
@@ -91,15 +94,17 @@ int launch_round(int src_bits, bool fmt, const void* in, void* out, int64_t n,
 int launch_mx(const float* in, float* out, int64_t n, int block, const RoundPlan& pe,
               const RoundPlan& ps, float pmn, float inv_pmn, uint64_t seed, uint64_t offset,
               void* stream);
-int launch_gemm_plain(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
-                      float* D, int64_t ldd, int M, int N, int K, int mbits, float alpha,
-                      void* stream);
+// Strided batches: GEMM z reads A + z*sa, B + z*sb and writes D + z*sd.
+int launch_gemm_plain(const float* A, int64_t lda, int64_t sa, int ta, const float* B,
+                      int64_t ldb, int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M,
+                      int N, int K, int batch, int mbits, float alpha, void* stream);
 int launch_gemm_f64(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
                     double* D, int64_t ldd, int M, int N, int K, void* stream);
-int launch_gemm_tc(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
-                   float* D, int64_t ldd, int M, int N, int K, int mbits, float alpha,
-                   int chunk, void* workspace, size_t workspace_bytes, void* stream);
-size_t gemm_tc_workspace(int M, int N, int K);
+int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float* B, int64_t ldb,
+                   int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M, int N, int K,
+                   int batch, int mbits, float alpha, int chunk, void* workspace,
+                   size_t workspace_bytes, void* stream);
+size_t gemm_tc_workspace(int M, int N, int K, int batch);
 
 }  // namespace lofgb
 

@@ -84,19 +84,27 @@ class LoF_Quantize(nn.Module):
 
 
 def _lof_gemm_2d(A, B, accum_mant_bits, gemm_round_mode, stochastic_rounding_bits, scale_a=1.0,
-                 scale_b=1.0):
-    """(..., M, K) x (..., K, N) -> (..., M, N) (LoFloat/layers.py:121-150)."""
+                 scale_b=1.0, variant="plain", chunk=32):
+    """(..., M, K) x (..., K, N) -> (..., M, N) (LoFloat/layers.py:121-150), with
+    the batch in one strided-batched launch instead of a Python loop of
+    lof_gemm calls (same per-product bits). A B that is the transposed view of
+    a contiguous (..., N, K) tensor — attention's K^T — is read in place."""
+    del gemm_round_mode, stochastic_rounding_bits
+    alpha = lof.gemm_alpha(scale_a, scale_b)
     if A.dim() == 2 and B.dim() == 2:
-        return lof.lof_gemm(A.contiguous(), B.contiguous(), accum_mant_bits, gemm_round_mode,
-                            stochastic_rounding_bits, scale_a, scale_b)
+        return lof.gemm(A.contiguous(), B.contiguous(), accum_mant_bits, alpha=alpha,
+                        variant=variant, chunk=chunk)
     batch_shape = A.shape[:-2]
     M, K = A.shape[-2], A.shape[-1]
     N = B.shape[-1]
     A_flat = A.reshape(-1, M, K).contiguous()
-    B_flat = B.reshape(-1, K, N).contiguous()
-    out = torch.stack([lof.lof_gemm(A_flat[i], B_flat[i], accum_mant_bits, gemm_round_mode,
-                                    stochastic_rounding_bits, scale_a, scale_b)
-                       for i in range(A_flat.shape[0])])
+    Bt = B.transpose(-2, -1)
+    if Bt.is_contiguous():
+        B_flat, tb = Bt.reshape(-1, N, K), True
+    else:
+        B_flat, tb = B.reshape(-1, K, N).contiguous(), False
+    out = lof.gemm(A_flat, B_flat, accum_mant_bits, trans_b=tb, alpha=alpha, variant=variant,
+                   chunk=chunk)
     return out.reshape(*batch_shape, M, N)
 
 
@@ -656,3 +664,159 @@ class PWLSiLU(nn.Module):
         frac = u - idx.to(x.dtype)
         out = torch.lerp(self.lut[idx], self.lut[idx + 1], frac)
         return torch.where(x.abs() > r, torch.relu(x), out)
+
+
+# ---- attention -------------------------------------------------------------------
+class LoF_MultiHeadAttention(nn.Module):
+    """Multi-head attention whose four projections and two attention products
+    run on the emulated-accumulation GEMM, with the reference's constructor and
+    forward (LoFloat/layers.py:1152-1410). Inputs are batch-first (B, T, E).
+    The score product Q·Kᵀ and the context product P·V are strided-batched
+    launches over all (batch, head) pairs, Kᵀ read in place; softmax, masks and
+    dropout are torch ops as in the reference. `gemm_variant` "tc" moves every
+    product to the tensor-core form."""
+
+    def __init__(self, embed_dim, num_heads, act_params=None, weight_params=None, bias=True,
+                 bias_params=None, act_exp=None, act_mant=None, weight_exp=None, weight_mant=None,
+                 bias_exp=None, bias_mant=None, rounding_mode=None, dropout=0.0,
+                 accum_mant_bits=23, gemm_round_mode=None, stochastic_rounding_bits=0,
+                 scaling="per_tensor", mx_block_size=32, scale_format=None,
+                 gemm_variant="plain", chunk=32):
+        super().__init__()
+        assert embed_dim % num_heads == 0, "embed_dim must be divisible by num_heads"
+        if scaling not in ("per_tensor", "mx"):
+            raise ValueError(f"scaling must be 'per_tensor' or 'mx', got {scaling!r}")
+        self.embed_dim = embed_dim
+        self.num_heads = num_heads
+        self.head_dim = embed_dim // num_heads
+        self.scale = self.head_dim ** -0.5
+        self.dropout = dropout
+        self.rounding_mode = rounding_mode if rounding_mode is not None else lof.RoundingMode.RoundToNearestEven
+        self.scaling = scaling
+        self.mx_block_size = mx_block_size
+        self.scale_format = scale_format if scale_format is not None else create_e8m0_params()
+        if scaling == "mx" and embed_dim % mx_block_size != 0:
+            raise ValueError(f"mx scaling needs embed_dim ({embed_dim}) divisible by "
+                             f"mx_block_size ({mx_block_size})")
+        self.accum_mant_bits = accum_mant_bits
+        self.gemm_round_mode = gemm_round_mode if gemm_round_mode is not None else lof.RoundingMode.RoundToNearestEven
+        self.stochastic_rounding_bits = stochastic_rounding_bits
+        self.gemm_variant = gemm_variant
+        self.chunk = chunk
+        self.act_params = act_params if act_params is not None else create_p3109_params(
+            act_exp + act_mant + 1, act_mant + 1, True, True)
+        self.weight_params = weight_params if weight_params is not None else create_p3109_params(
+            weight_exp + weight_mant + 1, weight_mant + 1, True, True)
+        self.bias_params = bias_params if bias_params is not None else create_p3109_params(
+            bias_exp + bias_mant + 1, bias_mant + 1, True, True) if (
+                bias_exp is not None and bias_mant is not None) else None
+        for nm in ("q", "k", "v", "out"):
+            self.register_parameter(f"{nm}_weight", nn.Parameter(torch.empty(embed_dim, embed_dim)))
+            if bias:
+                self.register_parameter(f"{nm}_bias", nn.Parameter(torch.zeros(embed_dim)))
+            else:
+                self.register_parameter(f"{nm}_bias", None)
+        self._reset_parameters()
+
+    def _reset_parameters(self):
+        for w in (self.q_weight, self.k_weight, self.v_weight, self.out_weight):
+            nn.init.xavier_uniform_(w)
+
+    @classmethod
+    def from_mha(cls, mha: nn.MultiheadAttention, act_params, weight_params, bias_params=None,
+                 rounding_mode=None, accum_mant_bits=23, gemm_round_mode=None,
+                 stochastic_rounding_bits=0):
+        layer = cls(mha.embed_dim, mha.num_heads, act_params=act_params,
+                    weight_params=weight_params, bias=mha.in_proj_bias is not None,
+                    bias_params=bias_params, rounding_mode=rounding_mode, dropout=mha.dropout,
+                    accum_mant_bits=accum_mant_bits, gemm_round_mode=gemm_round_mode,
+                    stochastic_rounding_bits=stochastic_rounding_bits)
+        e = mha.embed_dim
+        w = mha.in_proj_weight.data
+        dev = w.device
+
+        def q(t, p):  # rounding runs on the GPU; the result goes back to t's device
+            return layer._quantize(t.detach().clone().to("cuda"), p).to(t.device)
+
+        layer.q_weight = nn.Parameter(q(w[:e], layer.weight_params))
+        layer.k_weight = nn.Parameter(q(w[e:2 * e], layer.weight_params))
+        layer.v_weight = nn.Parameter(q(w[2 * e:], layer.weight_params))
+        layer.out_weight = nn.Parameter(q(mha.out_proj.weight.data, layer.weight_params))
+        if mha.in_proj_bias is not None:
+            b = mha.in_proj_bias.data
+            layer.q_bias = nn.Parameter(q(b[:e], layer.bias_params))
+            layer.k_bias = nn.Parameter(q(b[e:2 * e], layer.bias_params))
+            layer.v_bias = nn.Parameter(q(b[2 * e:], layer.bias_params))
+            layer.out_bias = nn.Parameter(q(mha.out_proj.bias.data, layer.bias_params))
+        return layer.to(dev)
+
+    def __deepcopy__(self, memo):
+        new = LoF_MultiHeadAttention(
+            self.embed_dim, self.num_heads, act_params=self.act_params,
+            weight_params=self.weight_params, bias=self.q_bias is not None,
+            bias_params=self.bias_params, rounding_mode=self.rounding_mode, dropout=self.dropout,
+            accum_mant_bits=self.accum_mant_bits, gemm_round_mode=self.gemm_round_mode,
+            stochastic_rounding_bits=self.stochastic_rounding_bits, scaling=self.scaling,
+            mx_block_size=self.mx_block_size, scale_format=self.scale_format,
+            gemm_variant=self.gemm_variant, chunk=self.chunk)
+        new.load_state_dict(self.state_dict())
+        memo[id(self)] = new
+        return new
+
+    def _quantize(self, tensor, params):
+        if params is None:
+            return tensor
+        if self.scaling == "mx":
+            if tensor.shape[-1] % self.mx_block_size != 0:
+                raise ValueError(f"mx scaling needs the last dim ({tensor.shape[-1]}) divisible by "
+                                 f"mx_block_size ({self.mx_block_size})")
+            return STEMXRound.apply(tensor, params, self.scale_format, self.mx_block_size,
+                                    self.rounding_mode)
+        return STERound.apply(tensor, params, self.rounding_mode)
+
+    def _linear(self, x, w, b):
+        leading, k = x.shape[:-1], x.shape[-1]
+        out = lof.gemm(x.reshape(-1, k).contiguous(), w.contiguous(), self.accum_mant_bits,
+                       trans_b=True, variant=self.gemm_variant, chunk=self.chunk)
+        out = out.reshape(*leading, w.shape[0])
+        return out + b if b is not None else out
+
+    def forward(self, query, key, value, attn_mask=None, key_padding_mask=None,
+                need_weights=False):
+        bsz, t, e = query.shape
+        s_len = key.shape[1]
+        query = self._quantize(query, self.act_params)
+        key = self._quantize(key, self.act_params)
+        value = self._quantize(value, self.act_params)
+        wq, wk, wv, wo = (self._quantize(w, self.weight_params)
+                          for w in (self.q_weight, self.k_weight, self.v_weight, self.out_weight))
+        bq, bk, bv, bo = (self._quantize(b, self.bias_params) if b is not None else None
+                          for b in (self.q_bias, self.k_bias, self.v_bias, self.out_bias))
+        h, d = self.num_heads, self.head_dim
+        q = self._linear(query, wq, bq).view(bsz, t, h, d).transpose(1, 2)
+        k = self._linear(key, wk, bk).view(bsz, s_len, h, d).transpose(1, 2)
+        v = self._linear(value, wv, bv).view(bsz, s_len, h, d).transpose(1, 2)
+        attn = _lof_gemm_2d(q, k.transpose(-2, -1), self.accum_mant_bits, self.gemm_round_mode,
+                            self.stochastic_rounding_bits, variant=self.gemm_variant,
+                            chunk=self.chunk) * self.scale
+        if attn_mask is not None:
+            attn = attn + attn_mask
+        if key_padding_mask is not None:
+            attn = attn.masked_fill(key_padding_mask.unsqueeze(1).unsqueeze(2), float("-inf"))
+        attn = torch.softmax(attn, dim=-1)
+        if self.training and self.dropout > 0.0:
+            attn = torch.nn.functional.dropout(attn, p=self.dropout)
+        out = _lof_gemm_2d(attn, v, self.accum_mant_bits, self.gemm_round_mode,
+                           self.stochastic_rounding_bits, variant=self.gemm_variant,
+                           chunk=self.chunk)
+        out = out.transpose(1, 2).contiguous().view(bsz, t, e)
+        out = self._linear(out, wo, bo)
+        return (out, attn) if need_weights else (out, None)
+
+    def set_accumulation_precision(self, accum_mant_bits):
+        self.accum_mant_bits = accum_mant_bits
+
+    def extra_repr(self):
+        return (f"embed_dim={self.embed_dim}, num_heads={self.num_heads}, "
+                f"head_dim={self.head_dim}, dropout={self.dropout}, "
+                f"bias={self.q_bias is not None}, accum_mant_bits={self.accum_mant_bits}")

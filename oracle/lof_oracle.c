@@ -833,3 +833,204 @@ int orc_pwl_silu_f32(const float* in, float* out, int64_t n, const float* lut, i
     }
     return 0;
 }
+
+/* ---- storage codec -------------------------------------------------------------
+ * convert_float_to_rep (src/lo_pack.hpp:109-287) with SOURCE = float, the
+ * runtime format in `f`, restated branch by branch; RoundMantissa is the
+ * shared round_mantissa above with the reference's default positive-sign flag
+ * (false) and the word width of the reference's Bits type at each call. */
+static int codec_is_inf(uint32_t rep, const lofgb_codec_format* f) {
+    return (rep | f->inf_or) == f->inf_match;
+}
+
+static int codec_is_nan(uint32_t rep, const lofgb_codec_format* f) {
+    if (f->nan_kind == LOFGB_NAN_NONE) return 0;
+    if (f->nan_kind == LOFGB_NAN_PATTERN) return rep == f->qnan;
+    const int n = f->fmt.bitwidth, m = f->fmt.mantissa_bits;
+    const int sgn = f->fmt.signedness == LOFGB_SIGNED;
+    const uint32_t mag = sgn ? rep & ((1u << (n - 1)) - 1u) : rep;
+    const int ebits = n - m - (sgn ? 1 : 0);
+    const uint32_t expall = ((1u << ebits) - 1u) << m;
+    return mag > expall;
+}
+
+static int clz32(uint32_t v) {
+    int c = 0;
+    for (int b = 31; b >= 0 && !((v >> b) & 1u); --b) ++c;
+    return c;
+}
+
+uint32_t orc_codec_encode_rep(float from, const lofgb_codec_format* F, int mode, int sat,
+                              int len, uint64_t r, double u) {
+    const int n = F->fmt.bitwidth, toMant = F->fmt.mantissa_bits;
+    const int to_signed = F->fmt.signedness == LOFGB_SIGNED;
+    const int toExpBits = to_signed ? n - toMant - 1 : n - toMant;
+    const int toBias = F->fmt.bias;
+    const int kExponentOffset = toBias - 127;
+    const int kDigitShift = toMant - 23;
+    const int toMinExp = 1 - toBias;
+    const int toMaxExp = (1 << toExpBits) - 1 - toBias;
+    const int toDigits = toMant + 1;
+    const int has_inf = F->fmt.inf_behavior != LOFGB_INF_SATURATING;
+    const uint32_t signmask = to_signed ? (1u << (n - 1)) : 0u;
+    const uint32_t maxFiniteRep = has_inf ? F->pos_inf - 1u
+                                          : (to_signed ? (((1u << n) - 1u) >> 1) : ((1u << n) - 1u));
+    const uint32_t infRep = has_inf ? F->pos_inf : maxFiniteRep;
+    const uint32_t fb = f2u(from);
+    const int neg = (fb >> 31) != 0;
+#define WITH_SIGN(mag) ((!neg || !to_signed) ? (uint32_t)(mag)                                  \
+                        : (((uint32_t)(mag)) == 0u && codec_is_nan(signmask, F)) ? 0u           \
+                        : ((uint32_t)(mag) | signmask))
+    /* :164-168 negative value into an unsigned target */
+    if (!to_signed && neg) {
+        if (!F->neg_to_nan) return 0u;
+        return F->fmt.nan_behavior == LOFGB_NAN_3109 ? F->qnan : F->snan;
+    }
+    const uint32_t from_bits = fb & 0x7FFFFFFFu;
+    /* :172-177 inf, NaN, zero */
+    if (from_bits == 0x7F800000u) {
+        if (sat != LOFGB_SAT_FINITE && has_inf) return WITH_SIGN(infRep);
+        return WITH_SIGN(maxFiniteRep);
+    }
+    if (from_bits > 0x7F800000u) return F->qnan;
+    if (from_bits == 0u) return WITH_SIGN(0u);
+    const int bfe = (int)(from_bits >> 23);
+    /* :182-201 branch 1: the target reaches below FP32's normal range */
+    if (toMinExp < -125 && bfe == 0) {
+        uint64_t bits = from_bits;
+        const int norm = clz32(from_bits) - (32 - 23) + 1;
+        const int bexp = kExponentOffset - norm + 1;
+        if (bexp <= 0) {
+            if (kExponentOffset < 64) bits <<= kExponentOffset;
+        } else {
+            bits <<= norm;
+            bits &= ~(1ull << 23);
+            bits |= (uint64_t)bexp << 23;
+        }
+        if (kDigitShift > 0) {
+            bits <<= kDigitShift;
+        } else {
+            bits = round_mantissa(bits, -kDigitShift, mode, len, 0, r, u, 64);
+            bits >>= -kDigitShift;
+        }
+        return WITH_SIGN((uint32_t)bits);
+    }
+    /* :204-241 branch 2: target-subnormal or zero */
+    if (toMinExp > -125) {
+        const int bte = (bfe - 127) + toBias;
+        if (bte <= 0) {
+            const uint32_t lead = bfe > 0 ? 1u : 0u;
+            const int shift = -kDigitShift - bte + (int)lead;
+            uint32_t rfb = (from_bits & 0x7FFFFFu) | (lead << 23);
+            uint32_t bits = 0;
+            if (shift <= 24) {
+                rfb = (uint32_t)round_mantissa(rfb, shift, mode, len, 0, r, u, 32);
+                bits = rfb >> shift;
+            } else {
+                uint64_t w = rfb;
+                switch (mode) {
+                case LOFGB_RTO:
+                case LOFGB_RAFZ: bits = rfb > 0 ? 1u : 0u; break;
+                case LOFGB_RTZ: bits = 0; break;
+                case LOFGB_RU: bits = (rfb && !neg) ? 1u : 0u; break;
+                case LOFGB_RD: bits = (rfb && neg) ? 1u : 0u; break;
+                case LOFGB_SR_A: case LOFGB_SR_B: case LOFGB_SR_C: case LOFGB_SR_D:
+                case LOFGB_TRUE_SR: case LOFGB_PROB:
+                    /* shifts of 64 or more are undefined in the reference: 0 */
+                    w = round_mantissa(w, shift, mode, len, 0, r, u, 64);
+                    bits = shift >= 64 ? 0u : (uint32_t)(w >> shift);
+                    break;
+                default: bits = 0; break;
+                }
+            }
+            return WITH_SIGN(bits);
+        }
+    }
+    /* :244-272 normal path, then the overflow rule */
+    uint64_t rfb = from_bits;
+    if (kDigitShift < 0) {
+        rfb = round_mantissa(rfb, -kDigitShift, mode, len, 0, r, u, 64);
+        rfb &= ~((1ull << (-kDigitShift)) - 1ull);
+    }
+    rfb += (uint64_t)(int64_t)kExponentOffset << 23;
+    uint32_t bits;
+    uint64_t aligned_highest = maxFiniteRep;
+    if (kDigitShift < 0) {
+        aligned_highest <<= -kDigitShift;
+        bits = (uint32_t)(rfb >> (-kDigitShift));
+    } else {
+        rfb <<= kDigitShift;
+        bits = (uint32_t)rfb;
+    }
+    const int narrower = (toMaxExp < 128) || (toMaxExp == 128 && toDigits < 24);
+    if (narrower && rfb > aligned_highest) {
+        const int emit_inf = sat == LOFGB_OVF_INF && has_inf;
+        return WITH_SIGN(emit_inf ? infRep : maxFiniteRep);
+    }
+    return WITH_SIGN(bits);
+#undef WITH_SIGN
+}
+
+/* convert_rep_to_float, src/lo_pack.hpp:293-320 */
+float orc_codec_decode_rep(uint32_t rep, const lofgb_codec_format* F) {
+    const int n = F->fmt.bitwidth, mant = F->fmt.mantissa_bits, bias = F->fmt.bias;
+    const int is_signed = F->fmt.signedness == LOFGB_SIGNED;
+    const int has_inf = F->fmt.inf_behavior != LOFGB_INF_SATURATING;
+    rep &= n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
+    const int sign = is_signed ? (int)((rep >> (n - 1)) & 1u) : 0;
+    const uint32_t mag = is_signed ? rep & ((1u << (n - 1)) - 1u) : rep;
+    if (has_inf && codec_is_inf(rep, F)) return sign ? -INFINITY : INFINITY;
+    if (codec_is_nan(rep, F)) return u2f(0x7FC00000u);
+    const uint32_t e = mag >> mant, m = mag & ((1u << mant) - 1u);
+    double v;
+    if (e == 0) v = ldexp((double)m, 1 - bias - mant);
+    else v = ldexp(1.0 + (double)m / (double)(1u << mant), (int)e - bias);
+    return (float)(sign ? -v : v);
+}
+
+/* group geometry, src/lo_pack.hpp:56-81 */
+static int gcd_i(int a, int b) { return b == 0 ? a : gcd_i(b, a % b); }
+static int group_bits(int n) { const int al = n <= 8 ? 8 : 16; return n / gcd_i(n, al) * al; }
+
+int64_t orc_packed_size(int n, int64_t count) {
+    const int gc = group_bits(n) / n;
+    return (count + gc - 1) / gc * (int64_t)(group_bits(n) / 8);
+}
+
+/* element i of group g sits at bit g*group_bits + slot*n, slot = i or gc-1-i,
+ * LSB-first within each byte (put_bits / get_bits, :85-104) */
+static int64_t code_bit(int64_t i, int n, int reverse) {
+    const int gc = group_bits(n) / n;
+    const int64_t g = i / gc;
+    const int k = (int)(i % gc);
+    const int slot = reverse ? gc - 1 - k : k;
+    return g * group_bits(n) + (int64_t)slot * n;
+}
+
+int orc_encode_f32(uint8_t* dst, const float* src, int64_t count, const lofgb_codec_format* f,
+                   int mode, int sat, int len, int reverse, uint64_t seed, uint64_t offset) {
+    if (!f || f->fmt.bitwidth < 1 || f->fmt.bitwidth > 16) return LOFGB_ERR_FORMAT;
+    const int n = f->fmt.bitwidth;
+    memset(dst, 0, (size_t)orc_packed_size(n, count));
+    for (int64_t i = 0; i < count; ++i) {
+        const uint64_t rb = orc_rng(seed, offset + (uint64_t)i);
+        const uint32_t code = orc_codec_encode_rep(src[i], f, mode, sat, len, rb, usamp_of(rb));
+        const int64_t b0 = code_bit(i, n, reverse);
+        for (int b = 0; b < n; ++b)
+            if ((code >> b) & 1u) dst[(b0 + b) >> 3] |= (uint8_t)(1u << ((b0 + b) & 7));
+    }
+    return 0;
+}
+
+int orc_decode_f32(float* dst, const uint8_t* src, int64_t count, const lofgb_codec_format* f,
+                   int reverse) {
+    if (!f || f->fmt.bitwidth < 1 || f->fmt.bitwidth > 16) return LOFGB_ERR_FORMAT;
+    const int n = f->fmt.bitwidth;
+    for (int64_t i = 0; i < count; ++i) {
+        const int64_t b0 = code_bit(i, n, reverse);
+        uint32_t code = 0;
+        for (int b = 0; b < n; ++b) code |= (uint32_t)((src[(b0 + b) >> 3] >> ((b0 + b) & 7)) & 1u) << b;
+        dst[i] = orc_codec_decode_rep(code, f);
+    }
+    return 0;
+}

@@ -116,6 +116,18 @@ int orc_conv2d_f32(const float* x, const float* w, float* y, const lofgb_conv2d_
 int orc_pwl_silu_f32(const float* in, float* out, int64_t n, const float* lut, int segments,
                      float R);
 
+/* Storage codec (lofgb_encode_f32 / lofgb_decode_f32 semantics):
+ * convert_float_to_rep / convert_rep_to_float and the group packing of
+ * src/lo_pack.hpp:56-420. `rbits` / `usamp` feed the stochastic modes. */
+uint32_t orc_codec_encode_rep(float x, const lofgb_codec_format* f, int mode, int sat_mode,
+                              int len, uint64_t rbits, double usamp);
+float orc_codec_decode_rep(uint32_t rep, const lofgb_codec_format* f);
+int64_t orc_packed_size(int bitwidth, int64_t count);
+int orc_encode_f32(uint8_t* dst, const float* src, int64_t count, const lofgb_codec_format* f,
+                   int mode, int sat_mode, int len, int reverse, uint64_t seed, uint64_t offset);
+int orc_decode_f32(float* dst, const uint8_t* src, int64_t count, const lofgb_codec_format* f,
+                   int reverse);
+
 int orc_validate_format(const lofgb_format* f, int src_mant_bits);
 int orc_max_threads(void);
 

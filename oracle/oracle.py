@@ -32,6 +32,14 @@ class Format(C.Structure):
                 ("signedness", C.c_uint8), ("reserved", C.c_uint8)]
 
 
+class CodecFormat(C.Structure):
+    """Same layout as ``lofgb_codec_format`` in include/lofgb.h."""
+    _fields_ = [("fmt", Format), ("inf_or", C.c_uint32), ("inf_match", C.c_uint32),
+                ("pos_inf", C.c_uint32), ("neg_inf", C.c_uint32), ("qnan", C.c_uint32),
+                ("snan", C.c_uint32), ("nan_kind", C.c_uint8), ("neg_to_nan", C.c_uint8),
+                ("reserved", C.c_uint8 * 2)]
+
+
 def fmt(bitwidth, mantissa_bits, bias, saturating=True, signed=True, nan_754=False) -> Format:
     return Format(bitwidth, mantissa_bits, bias, 1 if saturating else 0, 1 if nan_754 else 0,
                   0 if signed else 1, 0)
@@ -68,6 +76,15 @@ def lib():
                                            i32, f32, i32]
         L.orc_conv2d_f32.argtypes = [vp, vp, vp, C.POINTER(ConvShape), i32, f32, i32, i64, i64, i32]
         L.orc_pwl_silu_f32.argtypes = [vp, vp, i64, vp, i32, f32]
+        CP = C.POINTER(CodecFormat)
+        L.orc_codec_encode_rep.restype = C.c_uint32
+        L.orc_codec_encode_rep.argtypes = [f32, CP, i32, i32, i32, u64, f64]
+        L.orc_codec_decode_rep.restype = f32
+        L.orc_codec_decode_rep.argtypes = [C.c_uint32, CP]
+        L.orc_packed_size.restype = i64
+        L.orc_packed_size.argtypes = [i32, i64]
+        L.orc_encode_f32.argtypes = [vp, vp, i64, CP, i32, i32, i32, i32, u64, u64]
+        L.orc_decode_f32.argtypes = [vp, vp, i64, CP, i32]
         L.orc_rto_fma.restype = f32
         L.orc_rto_fma.argtypes = [f32, f32, f32]
         L.orc_max_threads.restype = i32
@@ -92,6 +109,10 @@ def ref():
             getattr(R, name).argtypes = [vp, vp, i64, i32, i32, i32, vp, vp, vp]
         R.ref_mx_round_f32.argtypes = [vp, vp, i64, i32] + [i32] * 13
         R.ref_gemm_f32.argtypes = [vp, vp, vp, i32, i32, i32, i32, f32]
+        R.ref_encode_f32.argtypes = [vp, vp, i64, vp, i32, i32, i32, i32]
+        R.ref_decode_f32.argtypes = [vp, vp, i64, vp, i32]
+        R.ref_packed_size.restype = i64
+        R.ref_packed_size.argtypes = [i32, i64]
         _ref = R
     return _ref
 
@@ -236,3 +257,73 @@ def pwl_silu(x, lut, R: float) -> np.ndarray:
     y = np.empty_like(x)
     _check(lib().orc_pwl_silu_f32(_p(x), _p(y), x.size, _p(lut), lut.size - 1, R))
     return y
+
+
+# ---- storage codec ---------------------------------------------------------------
+def codec_fmt(bitwidth, mantissa_bits, bias, saturating=True, signed=True, nan_754=False,
+              inf_or=0, inf_match=0xFFFFFFFF, pos_inf=0, neg_inf=0, qnan=0, snan=0, nan_kind=0,
+              neg_to_nan=False) -> CodecFormat:
+    f = CodecFormat()
+    f.fmt = fmt(bitwidth, mantissa_bits, bias, saturating, signed, nan_754)
+    f.inf_or, f.inf_match, f.pos_inf, f.neg_inf = inf_or, inf_match, pos_inf, neg_inf
+    f.qnan, f.snan, f.nan_kind, f.neg_to_nan = qnan, snan, nan_kind, int(neg_to_nan)
+    return f
+
+
+def codec_p3109(k, p, signed=True, saturating=True, bias=None, neg_to_nan=False) -> CodecFormat:
+    """P3109 <k, p> with the reference's P_3109 checkers (src/lo_float.h:1679-1760)."""
+    bias = (1 << (k - p - 1)) if bias is None else bias
+    nan = (1 << (k - 1)) if signed else (1 << k) - 1
+    if saturating:
+        inf_or, inf_match, pos, neg = 0, 0xFFFFFFFF, ((1 << (k - 1)) - 1 if signed else (1 << k) - 2), \
+            ((1 << k) - 1 if signed else 0)
+    else:
+        inf_or, inf_match = 1 << (k - 1), ((1 << k) - 1 if signed else (1 << k) - 2)
+        pos, neg = ((1 << (k - 1)) - 1 if signed else (1 << k) - 2), ((1 << k) - 1 if signed else 0)
+    return codec_fmt(k, p - 1, bias, saturating, signed, False, inf_or, inf_match, pos, neg, nan,
+                     nan, 0, neg_to_nan)
+
+
+def codec_ieee(bitwidth, mantissa_bits, bias, qnan, snan) -> CodecFormat:
+    """IEEE-style format (FP16 / BF16 checkers, src/fp_tools.hpp:334-395):
+    infinity = exponent all ones, mantissa 0; NaN = exponent all ones, mantissa != 0."""
+    sign = 1 << (bitwidth - 1)
+    expall = ((1 << (bitwidth - 1 - mantissa_bits)) - 1) << mantissa_bits
+    return codec_fmt(bitwidth, mantissa_bits, bias, False, True, True, sign, sign | expall, expall,
+                     sign | expall, qnan, snan, 1)
+
+
+def codec_fields(f: CodecFormat) -> np.ndarray:
+    """The int64 vector the reference shim's make_codec takes."""
+    base = f.fmt
+    return np.array([base.bitwidth, base.mantissa_bits, base.bias, base.inf_behavior,
+                     base.nan_behavior, base.signedness, f.inf_or, f.inf_match, f.pos_inf,
+                     f.neg_inf, f.qnan, f.snan, f.nan_kind, f.neg_to_nan], np.int64)
+
+
+def packed_size(bitwidth: int, count: int) -> int:
+    return int(lib().orc_packed_size(bitwidth, count))
+
+
+def encode(x, f: CodecFormat, mode: int = 0, sat: int = 0, stoch_len: int = 0,
+           reverse: int = 0, seed: int = 0, offset: int = 0) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.zeros(packed_size(f.fmt.bitwidth, x.size), np.uint8)
+    _check(lib().orc_encode_f32(_p(out), _p(x), x.size, C.byref(f), mode, sat, stoch_len, reverse,
+                                seed, offset))
+    return out
+
+
+def decode(packed, count: int, f: CodecFormat, reverse: int = 0) -> np.ndarray:
+    packed = np.ascontiguousarray(packed, dtype=np.uint8)
+    out = np.empty(count, np.float32)
+    _check(lib().orc_decode_f32(_p(out), _p(packed), count, C.byref(f), reverse))
+    return out
+
+
+def encode_rep(x: float, f: CodecFormat, mode: int = 0, sat: int = 0) -> int:
+    return int(lib().orc_codec_encode_rep(x, C.byref(f), mode, sat, 0, 0, 0.0))
+
+
+def decode_rep(rep: int, f: CodecFormat) -> float:
+    return float(lib().orc_codec_decode_rep(rep, C.byref(f)))

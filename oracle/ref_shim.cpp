@@ -20,6 +20,7 @@
 #include <random>
 
 #include "lo_float.h"
+#include "lo_pack.hpp"
 
 using namespace lo_float;
 using Params = FloatingPointParams<DeviceInfChecker, DeviceNaNChecker>;
@@ -235,5 +236,60 @@ int ref_gemm_f32(const float* A, const float* B, float* D, int M, int N, int K, 
         }
     return 0;
 }
+
+// ---- storage codec (src/lo_pack.hpp) --------------------------------------------
+// Runtime checker functors with the two predicate forms the reference's
+// checkers take (masked compare for infinities; single pattern, IEEE-style or
+// none for NaN), so that one shim function covers every format.
+struct RtInf {
+    uint32_t inf_or, inf_match, pos, neg;
+    bool operator()(uint64_t bits) const { return ((uint32_t)bits | inf_or) == inf_match; }
+    uint64_t minNegInf() const { return neg; }
+    uint64_t minPosInf() const { return pos; }
+};
+struct RtNaN {
+    int kind;  // 0 pattern, 1 IEEE-style, 2 none
+    uint32_t qnan, snan, sign_mask, exp_all;
+    bool operator()(uint64_t bits) const {
+        if (kind == 2) return false;
+        if (kind == 0) return (uint32_t)bits == qnan;
+        return ((uint32_t)bits & ~sign_mask) > exp_all;
+    }
+    uint64_t qNanBitPattern() const { return qnan; }
+    uint64_t sNanBitPattern() const { return snan; }
+};
+using CodecParams = FloatingPointParams<RtInf, RtNaN>;
+
+// cf: bw, m, bias, inf(1 = saturating), nan(1 = 754), sgn(1 = unsigned),
+//     inf_or, inf_match, pos_inf, neg_inf, qnan, snan, nan_kind, neg_to_nan
+static CodecParams make_codec(const int64_t* cf) {
+    const int bw = (int)cf[0], m = (int)cf[1], sgn = (int)cf[5];
+    RtInf inf{(uint32_t)cf[6], (uint32_t)cf[7], (uint32_t)cf[8], (uint32_t)cf[9]};
+    const uint32_t sign_mask = sgn ? 0u : (1u << (bw - 1));
+    const int ebits = bw - m - (sgn ? 0 : 1);
+    RtNaN nan{(int)cf[12], (uint32_t)cf[10], (uint32_t)cf[11], sign_mask,
+              ((1u << ebits) - 1u) << m};
+    return CodecParams(bw, m, (int)cf[2], cf[3] ? Inf_Behaviors::Saturating : Inf_Behaviors::Extended,
+                       cf[4] ? NaN_Behaviors::_754 : NaN_Behaviors::_3109,
+                       sgn ? Signedness::Unsigned : Signedness::Signed, inf, nan,
+                       cf[13] ? Unsigned_behavior::NegtoNaN : Unsigned_behavior::NegtoZero);
+}
+
+int ref_encode_f32(uint8_t* dst, const float* src, int64_t count, const int64_t* cf, int mode,
+                   int sat, int len, int reverse) {
+    const CodecParams P = make_codec(cf);
+    const ProjSpec ps{(Rounding_Mode)mode, (Saturation_Mode)sat, len};
+    return reverse ? LoF_encode<PackEndian::Reverse>(dst, src, P, (size_t)count, ps)
+                   : LoF_encode<PackEndian::Forward>(dst, src, P, (size_t)count, ps);
+}
+
+int ref_decode_f32(float* dst, const uint8_t* src, int64_t count, const int64_t* cf,
+                   int reverse) {
+    const CodecParams P = make_codec(cf);
+    return reverse ? LoF_decode<PackEndian::Reverse>(dst, src, P, (size_t)count)
+                   : LoF_decode<PackEndian::Forward>(dst, src, P, (size_t)count);
+}
+
+int64_t ref_packed_size(int n, int64_t count) { return (int64_t)LoF_packed_size(n, (size_t)count); }
 
 }  // extern "C"

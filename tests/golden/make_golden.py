@@ -343,6 +343,83 @@ def gen_gemm(R, rng, out):
                                "alpha": np.float32(alpha)}
 
 
+CODEC_FORMATS = {
+    # P3109 <k, p> with the reference's P_3109 checkers
+    "p3109_8_4": dict(kind="p3109", k=8, p=4),
+    "p3109_8_4_ext": dict(kind="p3109", k=8, p=4, saturating=False),
+    "p3109_8_3": dict(kind="p3109", k=8, p=3),
+    "p3109_7_3": dict(kind="p3109", k=7, p=3),
+    "p3109_6_3": dict(kind="p3109", k=6, p=3),
+    "p3109_5_2_ext": dict(kind="p3109", k=5, p=2, saturating=False),
+    "p3109_4_2": dict(kind="p3109", k=4, p=2),
+    "p3109_3_2": dict(kind="p3109", k=3, p=2),
+    "p3109_2_1": dict(kind="p3109", k=2, p=1),
+    "p3109_8_4_unsigned": dict(kind="p3109", k=8, p=4, signed=False),
+    "p3109_8_4_unsigned_ext_negnan": dict(kind="p3109", k=8, p=4, signed=False, saturating=False,
+                                          neg_to_nan=True),
+    "p3109_10_4": dict(kind="p3109", k=10, p=4),
+    "p3109_12_6_ext": dict(kind="p3109", k=12, p=6, saturating=False),
+    "p3109_16_9": dict(kind="p3109", k=16, p=9),
+    # IEEE-style checkers (src/fp_tools.hpp:334-395)
+    "fp16": dict(kind="ieee", bw=16, m=10, bias=15, qnan=0x7E00, snan=0x7C01),
+    "bf16": dict(kind="ieee", bw=16, m=7, bias=127, qnan=0x7FC0, snan=0x7F81),
+    # OCP E8M0 (src/lo_float.h:1773-1790) and a format without specials
+    "e8m0": dict(kind="raw", args=(8, 0, 127, True, False, False, 0, 0xFFFFFFFF, 0, 0, 0xFF, 0xFF, 0, False)),
+    "nospecial_9_3": dict(kind="raw", args=(9, 3, 200, True, True, False, 0, 0xFFFFFFFF, 0, 0, 0, 0, 2, False)),
+}
+CODEC_DET_MODES = [0, 1, 2, 4, 5, 6, 7, 12, 13]
+
+
+def codec_format(spec):
+    if spec["kind"] == "p3109":
+        return O.codec_p3109(spec["k"], spec["p"], signed=spec.get("signed", True),
+                             saturating=spec.get("saturating", True),
+                             neg_to_nan=spec.get("neg_to_nan", False))
+    if spec["kind"] == "ieee":
+        return O.codec_ieee(spec["bw"], spec["m"], spec["bias"], spec["qnan"], spec["snan"])
+    return O.codec_fmt(*spec["args"])
+
+
+def codec_probes(f, rng):
+    """Every finite value of the format, its float neighbours and midpoints,
+    specials, FP32 subnormals and wide random values."""
+    n = f.fmt.bitwidth
+    vals = np.array([O.decode_rep(r, f) for r in range(1 << n)], np.float32)
+    fin = np.unique(vals[np.isfinite(vals)])
+    if fin.size > 600:
+        fin = fin[np.linspace(0, fin.size - 1, 600).astype(int)]
+    parts = [fin, np.nextafter(fin, np.float32(np.inf)), np.nextafter(fin, np.float32(-np.inf)),
+             (0.5 * (fin[1:].astype(np.float64) + fin[:-1])).astype(np.float32),
+             np.array([0.0, -0.0, 1e30, -1e30, np.inf, -np.inf, np.nan, -np.nan, 1e-40, -1e-40,
+                       1.4e-45, 3e38, -3e38, 2.0 ** -126, 2.0 ** -127], np.float32),
+             (rng.standard_normal(800) * 2.0 ** rng.integers(-40, 40, 800)).astype(np.float32)]
+    return np.concatenate(parts).astype(np.float32)
+
+
+def gen_codec(R, rng, out):
+    """convert_float_to_rep / convert_rep_to_float and the packing of
+    src/lo_pack.hpp, run through the reference's LoF_encode / LoF_decode."""
+    for name, spec in CODEC_FORMATS.items():
+        f = codec_format(spec)
+        cf = O.codec_fields(f)
+        n = f.fmt.bitwidth
+        x = codec_probes(f, rng)
+        rec = {"fields": cf, "x": x}
+        for mode in CODEC_DET_MODES:
+            for sat in ((0, 1, 2) if mode == 0 else (0,)):
+                for rev in ((0, 1) if mode == 0 else (0,)):
+                    buf = np.zeros(int(R.ref_packed_size(n, x.size)), np.uint8)
+                    R.ref_encode_f32(p(buf), p(x), x.size, p(cf), mode, sat, 0, rev)
+                    rec[f"enc_m{mode}_s{sat}_r{rev}"] = buf
+        raw = rng.integers(0, 256, int(R.ref_packed_size(n, 2048)), dtype=np.uint8)
+        rec["raw"] = raw
+        for rev in (0, 1):
+            dec = np.empty(2048, np.float32)
+            R.ref_decode_f32(p(dec), p(raw), 2048, p(cf), rev)
+            rec[f"dec_r{rev}"] = dec
+        out[f"codec_{name}"] = rec
+
+
 def main():
     R = O.ref()
     if R is None:
@@ -352,12 +429,13 @@ def main():
     gen_round(R, rng, out)
     gen_mx(R, rng, out)
     gen_gemm(R, rng, out)
-    groups = {"round": {}, "mant": {}, "mx": {}, "gemm": {}}
+    gen_codec(R, np.random.default_rng(20261204), out)
+    groups = {"round": {}, "mant": {}, "mx": {}, "gemm": {}, "codec": {}}
     for k, v in out.items():
         groups[k.split("_")[0]][k] = v
     manifest = {"generator": "python tests/golden/make_golden.py",
-                "reference": "SudhanvaKulkarni123/LoFloat src/lo_float.h scalar virtual_round "
-                             "(via oracle/ref_shim.cpp)", "files": {}}
+                "reference": "SudhanvaKulkarni123/LoFloat src/lo_float.h scalar virtual_round, "
+                             "src/lo_pack.hpp codec (via oracle/ref_shim.cpp)", "files": {}}
     for g, cases in groups.items():
         flat = {}
         for cname, rec in cases.items():

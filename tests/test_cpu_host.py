@@ -102,6 +102,51 @@ def test_gemm_validation_codes():
     assert L.lofgb_gemm_tc_workspace_size(0, 4, 4) == 0
 
 
+def test_batched_gemm_and_conv_validation_codes():
+    L = _native.lib()
+    A, B, D = C.c_void_p(0x1000), C.c_void_p(0x2000), C.c_void_p(0x3000)
+
+    def call(batch=4, sa=1024, sb=2048, sd=512, M=16, N=32, K=64, mode=0):
+        return L.lofgb_gemm_batched_f32(A, K, sa, 0, B, N, sb, 0, D, N, sd, M, N, K, batch, 10,
+                                        mode, 1.0, 0, 32, None, 0, None)
+    assert call(batch=-1) == -2
+    assert call(sa=-5) == -2
+    assert call(sd=100) == -6          # D matrices would overlap
+    assert call(batch=0) == 0          # nothing to do
+    assert call(M=0) == 0
+    assert call(mode=3) == -4
+    assert L.lofgb_gemm_batched_tc_workspace_size(16, 32, 64, 0) == 0
+    assert L.lofgb_gemm_batched_tc_workspace_size(128, 128, 64, 3) > \
+        3 * L.lofgb_gemm_batched_tc_workspace_size(128, 128, 64, 1) // 2
+
+    sh = _native.LofgbConv2dShape(2, 3, 5, 5, 4, 3, 3, 1, 1, 1, 1, 1, 1)
+    P, Q = C.c_int32(), C.c_int32()
+    assert L.lofgb_conv2d_out_size(C.byref(sh), C.byref(P), C.byref(Q)) == 0
+    assert (P.value, Q.value) == (5, 5)
+    bad = _native.LofgbConv2dShape(1, 3, 2, 2, 4, 3, 3, 0, 0, 1, 1, 1, 1)
+    assert L.lofgb_conv2d_out_size(C.byref(bad), None, None) == -2
+    zero_stride = _native.LofgbConv2dShape(1, 3, 5, 5, 4, 3, 3, 0, 0, 0, 1, 1, 1)
+    assert L.lofgb_conv2d_out_size(C.byref(zero_stride), None, None) == -2
+
+    def conv(order=0, variant=0, chunk=32, mode=0, mbits=10, y=0x9000):
+        return L.lofgb_conv2d_f32(C.c_void_p(0x1000), C.c_void_p(0x8000), C.c_void_p(y),
+                                  C.byref(sh), mbits, mode, 1.0, order, variant, chunk, None, 0,
+                                  None)
+    assert conv(mode=1) == -4
+    assert conv(mbits=30) == -3
+    assert conv(order=5) == -7
+    assert conv(variant=9) == -7
+    assert conv(variant=1, chunk=8) == -2
+    assert conv(y=0x1010) == -6        # output overlaps the input
+    assert L.lofgb_conv2d_workspace_size(C.byref(sh), 0, 0) == 0   # plain needs none
+    assert L.lofgb_conv2d_workspace_size(C.byref(sh), 1, 1) > 0
+    lut = C.c_void_p(0x5000)
+    assert L.lofgb_pwl_silu_f32(C.c_void_p(0x1000), C.c_void_p(0x2000), 8, lut, 6, 1.0, None) == -2
+    assert L.lofgb_pwl_silu_f32(C.c_void_p(0x1000), C.c_void_p(0x2000), 8, lut, 8, 0.0, None) == -2
+    assert L.lofgb_pwl_silu_f32(C.c_void_p(0x1000), C.c_void_p(0x1004), 8, lut, 8, 1.0, None) == -6
+    assert L.lofgb_pwl_silu_f32(None, None, 0, lut, 8, 1.0, None) == 0
+
+
 def test_python_surface_mirrors_reference():
     assert int(lg.RoundingMode.RoundToNearestEven) == 0
     assert int(lg.RoundingMode.StochasticRoundingA) == 3
@@ -189,3 +234,52 @@ def test_grouped_gemm_validation_host_only():
     assert prep(good, ws=0x100010) == -9                     # workspace misaligned
     assert prep(good, tbytes=tb_need - 1) == -9              # table too small
     assert prep(good, sched=5) == -7                         # unknown schedule
+
+
+def test_codec_validation_and_sizes():
+    from oracle import oracle as O
+    L = _native.lib()
+    for n in range(1, 17):
+        for cnt in (0, 1, 7, 8, 33, 1000, 12345):
+            assert L.lofgb_packed_size(n, cnt) == O.packed_size(n, cnt)
+    assert L.lofgb_packed_size(0, 10) == 0 and L.lofgb_packed_size(17, 10) == 0
+    f = lg.codec_format(lg.create_p3109_params(8, 4))
+    src, dst = C.c_void_p(0x1000), C.c_void_p(0x100000)
+    bad = lg.codec_format(lg.create_p3109_params(8, 4))
+    bad.fmt.bitwidth = 17
+    assert L.lofgb_encode_f32(dst, src, 16, C.byref(bad), 0, 0, 0, 0, 0, 0, None) == -3
+    assert L.lofgb_encode_f32(dst, src, 16, C.byref(f), 99, 0, 0, 0, 0, 0, None) == -4
+    assert L.lofgb_encode_f32(dst, src, 16, C.byref(f), 0, 7, 0, 0, 0, 0, None) == -4
+    assert L.lofgb_encode_f32(C.c_void_p(0x1001), src, 16, C.byref(f), 0, 0, 0, 0, 0, 0, None) == -2
+    assert L.lofgb_encode_f32(C.c_void_p(0x1008), src, 16, C.byref(f), 0, 0, 0, 0, 0, 0, None) == -6
+    assert L.lofgb_decode_f32(C.c_void_p(0x1000), C.c_void_p(0x1004), 16, C.byref(f), 0, None) == -6
+    assert L.lofgb_encode_f32(None, None, 0, C.byref(f), 0, 0, 0, 0, 0, 0, None) == 0
+
+
+def test_codec_format_fits_reference_checkers():
+    from oracle import oracle as O
+    assert bytes(lg.codec_format(lg.create_p3109_params(8, 4))) == bytes(O.codec_p3109(8, 4))
+    assert bytes(lg.codec_format(lg.create_p3109_params(6, 3, True, False))) == \
+        bytes(O.codec_p3109(6, 3, saturating=False))
+    assert bytes(lg.codec_format(lg.create_p3109_params(8, 3, False, False))) == \
+        bytes(O.codec_p3109(8, 3, signed=False, saturating=False))
+    h = lg.codec_format(lg.create_half_params())
+    assert (h.nan_kind, h.inf_or, h.inf_match, h.pos_inf) == (1, 0x8000, 0xFC00, 0x7C00)
+
+    class Weird:
+        def __call__(self, bits):
+            return bits in (3, 5)
+
+        def minNegInf(self):
+            return 0
+
+        def minPosInf(self):
+            return 3
+
+        def qNanBitPattern(self):
+            return 9
+    w = lg.FloatFormatDescriptor(8, 3, 7, lg.InfBehavior.Extended, lg.NaNBehavior._3109,
+                                 lg.Signedness.Signed, Weird(), Weird())
+    import pytest
+    with pytest.raises(RuntimeError):
+        lg.codec_format(w)

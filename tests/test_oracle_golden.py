@@ -72,3 +72,28 @@ def test_mx_scale_formula_agreement():
 def test_gemm(cname, rec):
     D = O.gemm(rec["A"], rec["B"], int(rec["mbits"]), alpha=float(rec["alpha"]))
     assert same_bits(D, rec["D"]), cname
+
+
+def codec_from_fields(cf):
+    bw, m, bias, inf, nan, sgn, inf_or, inf_match, pos, neg, qn, sn, kind, n2n = (int(v) for v in cf)
+    return O.codec_fmt(bw, m, bias, saturating=bool(inf), signed=not sgn, nan_754=bool(nan),
+                       inf_or=inf_or, inf_match=inf_match, pos_inf=pos, neg_inf=neg, qnan=qn,
+                       snan=sn, nan_kind=kind, neg_to_nan=bool(n2n))
+
+
+@pytest.mark.parametrize("cname,rec", list(cases("codec")), ids=lambda v: v if isinstance(v, str) else "")
+def test_codec(cname, rec):
+    """The codec oracle against the reference's own LoF_encode / LoF_decode
+    (src/lo_pack.hpp) for every deterministic mode, the three saturation modes
+    and both group orders: packed bytes identical, decoded bits identical."""
+    f = codec_from_fields(rec["fields"])
+    x = rec["x"]
+    for key, want in rec.items():
+        if not key.startswith("enc_"):
+            continue
+        _, m, s, r = key.split("_")
+        got = O.encode(x, f, mode=int(m[1:]), sat=int(s[1:]), reverse=int(r[1:]))
+        assert np.array_equal(got, want), (cname, key, int(np.sum(got != want)))
+    for rev in (0, 1):
+        got = O.decode(rec["raw"], 2048, f, reverse=rev)
+        assert same_bits(got, rec[f"dec_r{rev}"]), (cname, rev)
