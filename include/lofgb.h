@@ -181,6 +181,19 @@ int lofgb_gemm_batched_f32(const float* A, int64_t lda, int64_t stride_a, int tr
                            void* workspace, size_t workspace_bytes, void* stream);
 size_t lofgb_gemm_batched_tc_workspace_size(int M, int N, int K, int batch);
 
+/* Emulated GEMM whose accumulator lives in a whole floating-point format:
+ * after every multiply-add (plain) or every chunk (tensor cores)
+ *   acc = virtual_round(rto(acc + ...), accum_fmt, RNE)
+ * — the format's exponent range, subnormals and overflow rule included, as
+ * lofgb_round_f32 applies them. No counterpart in the reference, whose leaf
+ * rounds only the mantissa (src/cutlass_gemms.cuh:162-163); it gives the
+ * FP16-like (5 exponent, 10 mantissa bits) accumulator of the linear-layer
+ * workload. Arguments and workspace as lofgb_gemm_f32. */
+int lofgb_gemm_accfmt_f32(const float* A, int64_t lda, int trans_a, const float* B, int64_t ldb,
+                          int trans_b, float* D, int64_t ldd, int M, int N, int K,
+                          const lofgb_format* accum_fmt, float alpha, int variant, int chunk,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
 /* Tensor-core GEMM for callers that cannot allocate device memory.
  * No counterpart in the reference.
  *

@@ -27,6 +27,7 @@ from .layers import (LinearConfig, LoF_Conv2d, LoF_Linear, LoF_MultiHeadAttentio
                      _lof_linear, lof_linear)
 from ._custom_ops import get_format, register_format
 from .grouped import GroupedRound
+from .norms import FISRBatchNorm, L1BatchNorm, LinfBatchNorm, PWLBatchNorm
 from .autotune import GroupedGemm
 
 __all__ = [
@@ -38,4 +39,5 @@ __all__ = [
     "register_format", "get_format", "GroupedRound", "GroupedGemm", "lof_conv2d", "conv2d",
     "conv2d_alpha", "pwl_silu", "LoF_Conv2d", "PWLSiLU", "LoF_MultiHeadAttention",
     "SaturationMode", "codec_format", "packed_size", "lof_encode", "lof_decode",
+    "L1BatchNorm", "LinfBatchNorm", "FISRBatchNorm", "PWLBatchNorm",
 ]

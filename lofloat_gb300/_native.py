@@ -74,6 +74,8 @@ SIGNATURES = [
                                       _i32, _i32, _i32, _i32, _i32, _i32, _f32, _i32, _i32, _vp,
                                       _sz, _vp]),
     ("lofgb_gemm_batched_tc_workspace_size", _sz, [_i32, _i32, _i32, _i32]),
+    ("lofgb_gemm_accfmt_f32", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32,
+                                     _FP, _f32, _i32, _i32, _vp, _sz, _vp]),
     ("lofgb_gemm_tc_noalloc_f32", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32,
                                          _i32, _i32, _f32, _i32, _vp]),
     ("lofgb_gemm_f64_ref", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32,

@@ -277,7 +277,8 @@ def tc_device_status(device=None) -> int:
 
 def gemm(A: torch.Tensor, B: torch.Tensor, accum_mant_bits: int, *, trans_a: bool = False,
          trans_b: bool = False, alpha: float = 1.0, variant: str = "plain", chunk: int = 32,
-         out: torch.Tensor | None = None) -> torch.Tensor:
+         out: torch.Tensor | None = None,
+         accum_format: FloatFormatDescriptor | None = None) -> torch.Tensor:
     """Emulated-accumulation GEMM with explicit layouts.
 
     A is (M, K), or (K, M) when trans_a; B is (K, N), or (N, K) when trans_b;
@@ -285,7 +286,9 @@ def gemm(A: torch.Tensor, B: torch.Tensor, accum_mant_bits: int, *, trans_a: boo
     operand makes it a strided-batched GEMM (one launch; a 2-D operand, or a
     batch of 1, is shared by every product) with D of shape (batch, M, N).
     variant "plain" is bit-exact to the reference leaf; "tc" is the tcgen05
-    chunked form."""
+    chunked form. `accum_format` (2-D only) rounds the accumulator into a
+    whole format instead of to `accum_mant_bits` mantissa bits
+    (lofgb_gemm_accfmt_f32)."""
     for t, nm in ((A, "A"), (B, "B")):
         if t.dim() not in (2, 3):
             raise RuntimeError(f"lof_gemm: {nm} must be 2-D (or 3-D for a batch)")
@@ -317,6 +320,14 @@ def gemm(A: torch.Tensor, B: torch.Tensor, accum_mant_bits: int, *, trans_a: boo
         if v == 1 and M and N and K:
             buf = _workspace(A.device, int(L.lofgb_gemm_batched_tc_workspace_size(M, N, K, batch)))
             ws, wsb = buf.data_ptr(), buf.numel()
+        if accum_format is not None:
+            if batched:
+                raise RuntimeError("lof_gemm: accum_format takes 2-D operands")
+            check(L.lofgb_gemm_accfmt_f32(A.data_ptr(), A.shape[-1], int(trans_a), B.data_ptr(),
+                                          B.shape[-1], int(trans_b), D.data_ptr(), N, M, N, K,
+                                          C.byref(accum_format.c_format), float(alpha), v,
+                                          int(chunk), ws, wsb, _stream(A)), "lof_gemm")
+            return D
         check(L.lofgb_gemm_batched_f32(A.data_ptr(), A.shape[-1], sa, int(trans_a), B.data_ptr(),
                                        B.shape[-1], sb, int(trans_b), D.data_ptr(), N, M * N, M,
                                        N, K, batch, int(accum_mant_bits),

@@ -320,7 +320,7 @@ static int gemm_impl(const float* A, int64_t lda, int64_t sa, int trans_a, const
                      int64_t ldb, int64_t sb, int trans_b, float* D, int64_t ldd, int64_t sd,
                      int M, int N, int K, int batch, int accum_mant_bits, int mode, float alpha,
                      int variant, int chunk, void* workspace, size_t workspace_bytes,
-                     void* stream) {
+                     void* stream, const RoundPlan* acc_fmt = nullptr) {
     g_detail[0] = 0;
     int st = check_gemm_args(A, lda, trans_a, B, ldb, trans_b, D, ldd, M, N, K);
     if (st) return st;
@@ -336,14 +336,14 @@ static int gemm_impl(const float* A, int64_t lda, int64_t sa, int trans_a, const
     if (M == 0 || N == 0 || batch == 0) return LOFGB_OK;
     if (variant == LOFGB_GEMM_PLAIN)
         return launch_gemm_plain(A, lda, sa, trans_a, B, ldb, sb, trans_b, D, ldd, sd, M, N, K,
-                                 batch, accum_mant_bits, alpha, stream);
+                                 batch, accum_mant_bits, acc_fmt, alpha, stream);
     if (variant == LOFGB_GEMM_TC) {
         if (chunk <= 0 || chunk % 16 != 0 || chunk > 256)
             return set_error(LOFGB_ERR_SIZE, "chunk %d must be a multiple of 16 in [16, 256]",
                              chunk);
         return launch_gemm_tc(A, lda, sa, trans_a, B, ldb, sb, trans_b, D, ldd, sd, M, N, K,
-                              batch, accum_mant_bits, alpha, chunk, workspace, workspace_bytes,
-                              stream);
+                              batch, accum_mant_bits, acc_fmt, alpha, chunk, workspace,
+                              workspace_bytes, stream);
     }
     return set_error(LOFGB_ERR_UNSUPPORTED, "unknown GEMM variant %d", variant);
 }
@@ -370,6 +370,19 @@ int lofgb_gemm_batched_f32(const float* A, int64_t lda, int64_t stride_a, int tr
     return gemm_impl(A, lda, stride_a, trans_a, B, ldb, stride_b, trans_b, D, ldd, stride_d, M,
                      N, K, batch, accum_mant_bits, mode, alpha, variant, chunk, workspace,
                      workspace_bytes, stream);
+}
+
+int lofgb_gemm_accfmt_f32(const float* A, int64_t lda, int trans_a, const float* B, int64_t ldb,
+                          int trans_b, float* D, int64_t ldd, int M, int N, int K,
+                          const lofgb_format* accum_fmt, float alpha, int variant, int chunk,
+                          void* workspace, size_t workspace_bytes, void* stream) {
+    g_detail[0] = 0;
+    RoundPlan plan;
+    int st = make_round_plan(&plan, accum_fmt, 32, LOFGB_RNE, 0);
+    if (st) return st;
+    return gemm_impl(A, lda, 0, trans_a, B, ldb, 0, trans_b, D, ldd, 0, M, N, K, 1,
+                     23 - plan.d, LOFGB_RNE, alpha, variant, chunk, workspace, workspace_bytes,
+                     stream, &plan);
 }
 
 size_t lofgb_gemm_batched_tc_workspace_size(int M, int N, int K, int batch) {

@@ -50,7 +50,7 @@ __device__ __forceinline__ int clz32(uint32_t v) { return __clz((int)v); }
 // convert_float_to_rep, src/lo_pack.hpp:109-287. RoundMantissa sees the
 // reference's default positive-sign flag (false).
 template <int MODE>
-__device__ uint32_t codec_encode(float from, const CodecArg& a, uint64_t r) {
+__device__ __forceinline__ uint32_t codec_encode(float from, const CodecArg& a, uint64_t r) {
     const int n = a.n, toMant = a.m;
     const int toExpBits = a.is_signed ? n - toMant - 1 : n - toMant;
     const int kExponentOffset = a.bias - 127;
@@ -141,11 +141,14 @@ __device__ __forceinline__ float codec_decode(uint32_t rep, const CodecArg& a) {
     const uint32_t mag = a.is_signed ? rep & ((1u << (n - 1)) - 1u) : rep;
     if (a.has_inf && (rep | a.inf_or) == a.inf_match) return sign ? -INFINITY : INFINITY;
     if (c_is_nan(rep, a)) return __uint_as_float(0x7FC00000u);
+    // the value is an integer k < 2^16 times 2^x: k converts to float
+    // exactly and ldexpf rounds k * 2^x once, as the reference's exact double
+    // narrowed to float does
     const uint32_t e = mag >> a.m, mf = mag & ((1u << a.m) - 1u);
-    double v;
-    if (e == 0) v = ldexp((double)mf, 1 - a.bias - a.m);
-    else v = ldexp(1.0 + (double)mf / (double)(1u << a.m), (int)e - a.bias);
-    return __double2float_rn(sign ? -v : v);
+    const uint32_t k = e == 0 ? mf : (mf | (1u << a.m));
+    const int x = (e == 0 ? 1 : (int)e) - a.bias - a.m;
+    const float v = ldexpf(__uint2float_rn(k), x < -300 ? -300 : (x > 300 ? 300 : x));
+    return sign ? -v : v;
 }
 
 constexpr int cgcd(int x, int y) { return y == 0 ? x : cgcd(y, x % y); }

@@ -95,16 +95,14 @@ __device__ __forceinline__ void decode_col(const ConvGeo& g, int col, int& h0, i
     xbase = (int64_t)img * g.CHW;
 }
 
-template <bool ROUND, int ORDER>
+template <int ACC, int ORDER>
 __global__ void __launch_bounds__(NT, 2)
-conv_plain_kernel(ConvGeo g, int ro, float alpha) {
+conv_plain_kernel(ConvGeo g, AccRound r, float alpha) {
     __shared__ __align__(16) float As[2][BK][BM + PAD];
     __shared__ __align__(16) float Bs[2][BK][BN + PAD];
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    const uint32_t half_m1 = ROUND ? (1u << (ro - 1)) - 1u : 0u;
-    const uint32_t mask = ROUND ? ~((1u << ro) - 1u) : ~0u;
 
     float acc[8][8];
 #pragma unroll
@@ -165,7 +163,7 @@ conv_plain_kernel(ConvGeo g, int ro, float alpha) {
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
-        mac_ktile<ROUND>(As[buf], Bs[buf], acc, min(BK, g.kseq - kt * BK), tx, ty, ro, half_m1, mask);
+        mac_ktile<ACC>(As[buf], Bs[buf], acc, min(BK, g.kseq - kt * BK), tx, ty, r);
         __syncthreads();
     }
 
@@ -325,9 +323,9 @@ template <int ORDER>
 int launch_conv_plain(const ConvGeo& g, int mbits, float alpha, cudaStream_t st) {
     dim3 grid((g.ncols + BN - 1) / BN, (g.K + BM - 1) / BM);
     if (grid.y > 65535) return set_error(LOFGB_ERR_SIZE, "too many output channels for the grid");
-    const int ro = 23 - mbits;
-    if (ro > 0) conv_plain_kernel<true, ORDER><<<grid, NT, 0, st>>>(g, ro, alpha);
-    else conv_plain_kernel<false, ORDER><<<grid, NT, 0, st>>>(g, ro, alpha);
+    const AccRound r = acc_mant(mbits);
+    if (r.ro > 0) conv_plain_kernel<ACC_MANT, ORDER><<<grid, NT, 0, st>>>(g, r, alpha);
+    else conv_plain_kernel<ACC_NONE, ORDER><<<grid, NT, 0, st>>>(g, r, alpha);
     return check_launch("conv_plain_kernel");
 }
 

@@ -26,17 +26,15 @@ namespace lofgb {
 namespace {
 
 // One 128 x 128 output tile of one GEMM of the batch.
-template <bool ROUND>
+template <int ACC>
 __device__ __forceinline__ void plain_tile(float (*As)[BK][BM + PAD], float (*Bs)[BK][BN + PAD],
                                            const float* __restrict__ A, int64_t lda, int ta,
                                            const float* __restrict__ B, int64_t ldb, int tb,
                                            float* __restrict__ D, int64_t ldd, int M, int N,
-                                           int K, int ro, float alpha) {
+                                           int K, const AccRound& r, float alpha) {
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    const uint32_t half_m1 = ROUND ? (1u << (ro - 1)) - 1u : 0u;
-    const uint32_t mask = ROUND ? ~((1u << ro) - 1u) : ~0u;
 
     float acc[8][8];
 #pragma unroll
@@ -78,7 +76,7 @@ __device__ __forceinline__ void plain_tile(float (*As)[BK][BM + PAD], float (*Bs
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
-        mac_ktile<ROUND>(As[buf], Bs[buf], acc, min(BK, K - kt * BK), tx, ty, ro, half_m1, mask);
+        mac_ktile<ACC>(As[buf], Bs[buf], acc, min(BK, K - kt * BK), tx, ty, r);
         __syncthreads();  // buffer `buf` is refilled by the next iteration's issue()
     }
 
@@ -95,17 +93,17 @@ __device__ __forceinline__ void plain_tile(float (*As)[BK][BM + PAD], float (*Bs
 }
 
 // blockIdx.z walks the batch (strided-batched GEMM; batch 1 for a single one).
-template <bool ROUND>
+template <int ACC>
 __global__ void __launch_bounds__(NT, 2)
 gemm_plain_kernel(const float* __restrict__ A, int64_t lda, int64_t sa, int ta,
                   const float* __restrict__ B, int64_t ldb, int64_t sb, int tb,
                   float* __restrict__ D, int64_t ldd, int64_t sd, int M, int N, int K, int batch,
-                  int ro, float alpha) {
+                  const __grid_constant__ AccRound r, float alpha) {
     __shared__ __align__(16) float As[2][BK][BM + PAD];
     __shared__ __align__(16) float Bs[2][BK][BN + PAD];
     for (int z = blockIdx.z; z < batch; z += gridDim.z) {
-        plain_tile<ROUND>(As, Bs, A + (int64_t)z * sa, lda, ta, B + (int64_t)z * sb, ldb, tb,
-                          D + (int64_t)z * sd, ldd, M, N, K, ro, alpha);
+        plain_tile<ACC>(As, Bs, A + (int64_t)z * sa, lda, ta, B + (int64_t)z * sb, ldb, tb,
+                        D + (int64_t)z * sd, ldd, M, N, K, r, alpha);
         __syncthreads();  // the next batch entry refills the shared tiles
     }
 }
@@ -151,17 +149,24 @@ gemm_f64_kernel(const float* __restrict__ A, int64_t lda, int ta, const float* _
 
 int launch_gemm_plain(const float* A, int64_t lda, int64_t sa, int ta, const float* B,
                       int64_t ldb, int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M,
-                      int N, int K, int batch, int mbits, float alpha, void* stream) {
+                      int N, int K, int batch, int mbits, const RoundPlan* acc_fmt, float alpha,
+                      void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch < 65535 ? batch : 65535);
     if (grid.y > 65535) return set_error(LOFGB_ERR_SIZE, "M too large for the plain GEMM grid");
-    const int ro = 23 - mbits;
-    if (ro > 0)
-        gemm_plain_kernel<true><<<grid, NT, 0, st>>>(A, lda, sa, ta, B, ldb, sb, tb, D, ldd, sd, M,
-                                                     N, K, batch, ro, alpha);
-    else
-        gemm_plain_kernel<false><<<grid, NT, 0, st>>>(A, lda, sa, ta, B, ldb, sb, tb, D, ldd, sd, M,
-                                                      N, K, batch, ro, alpha);
+    AccRound r = acc_mant(mbits);
+#define LOFGB_PLAIN(ACC) \
+    gemm_plain_kernel<ACC><<<grid, NT, 0, st>>>(A, lda, sa, ta, B, ldb, sb, tb, D, ldd, sd, M, N, K, batch, r, alpha)
+    if (acc_fmt) {
+        r.plan = *acc_fmt;
+        if (acc_fmt->uni == 1) LOFGB_PLAIN(ACC_UNI);
+        else LOFGB_PLAIN(ACC_FMT);
+    } else if (r.ro > 0) {
+        LOFGB_PLAIN(ACC_MANT);
+    } else {
+        LOFGB_PLAIN(ACC_NONE);
+    }
+#undef LOFGB_PLAIN
     return check_launch("gemm_plain_kernel");
 }
 

@@ -13,21 +13,45 @@ namespace {
 constexpr int BM = 128, BN = 128, BK = 16, NT = 256;
 constexpr int PAD = 4;
 
+// How the accumulator is re-rounded after every MAC: ACC_NONE (23 mantissa
+// bits: the round-to-odd word itself), ACC_MANT (RNE to m mantissa bits, the
+// reference leaf), ACC_UNI / ACC_FMT (RNE into a whole format — exponent
+// range, subnormals, overflow — by the whole-range float rounding or by the
+// integer rounding core; an extension without a reference counterpart).
+enum { ACC_NONE = 0, ACC_MANT = 1, ACC_UNI = 2, ACC_FMT = 3 };
+
+struct AccRound {
+    int ro;                   // 23 - mantissa bits
+    uint32_t half_m1, mask;   // RNE constants for ACC_MANT
+    RoundPlan plan;           // the accumulator format for ACC_UNI / ACC_FMT
+};
+
 // One emulated MAC. The round-to-odd word v = rz | sticky: when the two
 // directed FMAs differ they are adjacent, so (rd | ru) & 1 is 1 exactly when
 // the sum was inexact or rz is already odd — the same word as rz | (rd != ru).
 // The RNE step works on the signed word: for finite values (and the GPU's
 // positive canonical NaN) adding < 2^ro never carries into the sign bit.
-template <bool ROUND>
-__device__ __forceinline__ float emac(float a, float b, float acc, int ro, uint32_t half_m1,
-                                      uint32_t mask) {
+// Round-to-odd keeps a sticky bit below FP32's last place, so rounding v to
+// the (narrower) accumulator equals rounding the exact a*b + acc.
+template <int ACC>
+__device__ __forceinline__ float emac(float a, float b, float acc, const AccRound& r) {
     const float rd = __fmaf_rd(a, b, acc);
     const float ru = __fmaf_ru(a, b, acc);
     const uint32_t rz = __float_as_uint(rd >= 0.0f ? rd : ru);
     const uint32_t v = rz | ((__float_as_uint(rd) | __float_as_uint(ru)) & 1u);
-    if (!ROUND) return __uint_as_float(v);
-    const uint32_t t = v + ((v >> ro) & 1u) + half_m1;
-    return __uint_as_float(t & mask);
+    if (ACC == ACC_NONE) return __uint_as_float(v);
+    if (ACC == ACC_UNI) return __uint_as_float(vr_uni_f32<LOFGB_RNE, 1>(v, r.plan));
+    if (ACC == ACC_FMT) return __uint_as_float(vr_format<LOFGB_RNE, 32>(v, r.plan, 0ull));
+    const uint32_t t = v + ((v >> r.ro) & 1u) + r.half_m1;
+    return __uint_as_float(t & r.mask);
+}
+
+AccRound acc_mant(int mbits) {
+    AccRound r = {};
+    r.ro = 23 - mbits;
+    r.half_m1 = r.ro > 0 ? (1u << (r.ro - 1)) - 1u : 0u;
+    r.mask = r.ro > 0 ? ~((1u << r.ro) - 1u) : ~0u;
+    return r;
 }
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -44,10 +68,10 @@ __device__ __forceinline__ void cp_async4(uint32_t dst, const float* src, bool v
 // owns rows {ty*4 .. ty*4+3, 64+ty*4 .. 64+ty*4+3} and the same columns of tx.
 // One 8x8 MAC block per k (640 instructions) stays resident in the
 // instruction cache; unrolling k as well overflows it.
-template <bool ROUND>
+template <int ACC>
 __device__ __forceinline__ void mac_ktile(const float (*As)[BM + PAD], const float (*Bs)[BN + PAD],
-                                          float (&acc)[8][8], int kmax, int tx, int ty, int ro,
-                                          uint32_t half_m1, uint32_t mask) {
+                                          float (&acc)[8][8], int kmax, int tx, int ty,
+                                          const AccRound& r) {
 #pragma unroll 1
     for (int kk = 0; kk < kmax; ++kk) {
         const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
@@ -59,8 +83,7 @@ __device__ __forceinline__ void mac_ktile(const float (*As)[BM + PAD], const flo
 #pragma unroll
         for (int i = 0; i < 8; ++i)
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
-                acc[i][j] = emac<ROUND>(av[i], bv[j], acc[i][j], ro, half_m1, mask);
+            for (int j = 0; j < 8; ++j) acc[i][j] = emac<ACC>(av[i], bv[j], acc[i][j], r);
     }
 }
 

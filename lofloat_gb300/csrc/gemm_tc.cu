@@ -38,6 +38,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "lof_round.cuh"
 #include "lofgb_internal.h"
 #include "tc_split.cuh"
 
@@ -71,6 +72,9 @@ struct TcParams {
     int batch;             // strided batch: GEMM b reads split rows b*Mp.. / b*Np..
     int Mp, Np;            // padded rows of one GEMM's A / B split
     int64_t stride_d;      // elements between consecutive D matrices
+    int acc_kind;          // 0: RNE to ro mantissa bits; 2 / 3: the format acc_plan
+                           // (whole-range float rounding / integer rounding core)
+    RoundPlan acc_plan;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -210,6 +214,19 @@ __device__ __forceinline__ float fold(float acc, float s, int ro, uint32_t half_
     return __uint_as_float(t & mask);
 }
 
+// acc = RNE_format(rto(acc + s)) for a whole-format accumulator: the
+// round-to-odd word keeps a sticky bit, so the format rounding of it equals
+// the format rounding of the exact sum.
+template <int KIND>
+__device__ __forceinline__ float fold_fmt(float acc, float s, const RoundPlan& p) {
+    const float rd = __fadd_rd(acc, s);
+    const float ru = __fadd_ru(acc, s);
+    const uint32_t rz = __float_as_uint(rd >= 0.0f ? rd : ru);
+    const uint32_t v = rz | ((__float_as_uint(rd) | __float_as_uint(ru)) & 1u);
+    if (KIND == 2) return __uint_as_float(vr_uni_f32<LOFGB_RNE, 1>(v, p));
+    return __uint_as_float(vr_format<LOFGB_RNE, 32>(v, p, 0ull));
+}
+
 // ---- tile sources ------------------------------------------------------------
 // Everything the three roles need to know about one 128 x 128 output tile.
 struct TileInfo {
@@ -310,8 +327,11 @@ struct GroupedSrc {
 };
 
 // ---- the persistent tensor-core body (shared by both launches) ---------------
-template <class Src>
-__device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* smem_raw) {
+// ACCK: 0 RNE to ro mantissa bits; 2 / 3 a whole-format accumulator (acc_plan)
+// by the whole-range float rounding / by the integer rounding core.
+template <int ACCK, class Src>
+__device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* smem_raw,
+                                       const RoundPlan* acc_plan = nullptr) {
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                ~uintptr_t(1023));
     uint8_t* tiles = smem;
@@ -455,10 +475,17 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                 tmem_ld_wait();
                 tc_fence_before();
                 mbar_arrive(bar_tempty + 8 * buf);
+                if constexpr (ACCK == 0) {
 #pragma unroll
-                for (int i = 0; i < 32; ++i) acc[i] = fold(acc[i], __uint_as_float(r0[i]), ro, half_m1, mask);
+                    for (int i = 0; i < 32; ++i) acc[i] = fold(acc[i], __uint_as_float(r0[i]), ro, half_m1, mask);
 #pragma unroll
-                for (int i = 0; i < 32; ++i) acc[32 + i] = fold(acc[32 + i], __uint_as_float(r1[i]), ro, half_m1, mask);
+                    for (int i = 0; i < 32; ++i) acc[32 + i] = fold(acc[32 + i], __uint_as_float(r1[i]), ro, half_m1, mask);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) acc[i] = fold_fmt<ACCK>(acc[i], __uint_as_float(r0[i]), *acc_plan);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) acc[32 + i] = fold_fmt<ACCK>(acc[32 + i], __uint_as_float(r1[i]), *acc_plan);
+                }
             }
             if (!ok) break;
             const int row = ti.m0 + quarter * 32 + lane;
@@ -503,10 +530,11 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
     }
 }
 
+template <int ACCK>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant__ CUtensorMap tm_alo,
                const __grid_constant__ CUtensorMap tm_bhi, const __grid_constant__ CUtensorMap tm_blo,
-               TcParams prm) {
+               const __grid_constant__ TcParams prm) {
     extern __shared__ uint8_t smem_raw[];
     SingleSrc src;
     src.m[0] = &tm_ahi;
@@ -514,14 +542,14 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
     src.m[2] = &tm_bhi;
     src.m[3] = &tm_blo;
     src.prm = prm;
-    tc_body(src, prm.status, smem_raw);
+    tc_body<ACCK>(src, prm.status, smem_raw, &prm.acc_plan);
 }
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 gemm_tc_grouped_kernel(const GroupHeader* __restrict__ h) {
     extern __shared__ uint8_t smem_raw[];
     GroupedSrc src{h};
-    tc_body(src, h->status, smem_raw);
+    tc_body<0>(src, h->status, smem_raw);
 }
 
 // ---- operand split: FP32 -> K-major BF16 hi/lo, zero padded -----------------
@@ -655,8 +683,8 @@ size_t gemm_tc_workspace(int M, int N, int K, int batch) { return ws_layout(M, N
 
 int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float* B, int64_t ldb,
                    int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M, int N, int K,
-                   int batch, int mbits, float alpha, int chunk, void* workspace,
-                   size_t workspace_bytes, void* stream) {
+                   int batch, int mbits, const RoundPlan* acc_fmt, float alpha, int chunk,
+                   void* workspace, size_t workspace_bytes, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (K == 0) {
         // no products: D = alpha * (+0)
@@ -689,12 +717,12 @@ int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float*
     split_bf16_kernel<<<dim3(w.Kp / 64, w.Np / 32, gz), sb256, 0, st>>>(B, ldb, sb, tb ? 1 : 0, N, K,
                                                                         w.Np, w.Kp, batch, bhi, blo);
     if ((rc = check_launch("split_bf16_kernel(B)"))) return rc;
-    return launch_tc_presplit(ws, w, D, ldd, sd, M, N, mbits, alpha, chunk, 0, 0, stream);
+    return launch_tc_presplit(ws, w, D, ldd, sd, M, N, mbits, alpha, chunk, 0, 0, stream, acc_fmt);
 }
 
 int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int64_t sd, int M,
                        int N, int mbits, float alpha, int chunk, int64_t img_L,
-                       int64_t img_stride, void* stream) {
+                       int64_t img_stride, void* stream, const RoundPlan* acc_fmt) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     auto* ahi = reinterpret_cast<__nv_bfloat16*>(ws + w.ahi);
     auto* alo = reinterpret_cast<__nv_bfloat16*>(ws + w.alo);
@@ -725,19 +753,33 @@ int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, in
     p.Mp = w.Mp;
     p.Np = w.Np;
     p.stride_d = sd;
+    p.acc_kind = 0;
+    memset(&p.acc_plan, 0, sizeof(p.acc_plan));
+    if (acc_fmt) {
+        p.acc_kind = acc_fmt->uni == 1 ? 2 : 3;
+        p.acc_plan = *acc_fmt;
+    }
 
     int dev = 0;
     cudaGetDevice(&dev);
-    static bool attr_set[64] = {false};
-    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    static bool attr_set[3][64] = {};
+    const int ki = p.acc_kind == 0 ? 0 : p.acc_kind - 1;
+    if (dev < 0 || dev >= 64 || !attr_set[ki][dev]) {
+        const void* fn = p.acc_kind == 0 ? (const void*)gemm_tc_kernel<0>
+                         : p.acc_kind == 2 ? (const void*)gemm_tc_kernel<2> : (const void*)gemm_tc_kernel<3>;
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
         if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
-        if (dev >= 0 && dev < 64) attr_set[dev] = true;
+        if (dev >= 0 && dev < 64) attr_set[ki][dev] = true;
     }
     const int64_t tiles = (int64_t)p.batch * p.tiles_m * p.tiles_n;
     if (tiles >= ((int64_t)1 << 31)) return set_error(LOFGB_ERR_SIZE, "too many output tiles");
     const int grid = tiles < sm_count() ? (int)tiles : sm_count();
-    gemm_tc_kernel<<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
+    if (p.acc_kind == 0)
+        gemm_tc_kernel<0><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
+    else if (p.acc_kind == 2)
+        gemm_tc_kernel<2><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
+    else
+        gemm_tc_kernel<3><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
     return check_launch("gemm_tc_kernel");
 }
 

@@ -83,9 +83,11 @@ WsLayout ws_layout(int M, int N, int K, int batch = 1);
 // img_L > 0 stores conv2d output: column j = img * img_L + l of row i goes to
 // D[img * img_stride + i * ldd + l].
 // D of batch entry b starts at D + b * sd.
+// acc_fmt (optional) rounds the accumulator into a whole format instead of
+// to mbits mantissa bits.
 int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int64_t sd, int M,
                        int N, int mbits, float alpha, int chunk, int64_t img_L,
-                       int64_t img_stride, void* stream);
+                       int64_t img_stride, void* stream, const RoundPlan* acc_fmt = nullptr);
 
 // Kernel launchers (one translation unit each).
 int launch_round(int src_bits, bool fmt, const void* in, void* out, int64_t n,
@@ -95,15 +97,18 @@ int launch_mx(const float* in, float* out, int64_t n, int block, const RoundPlan
               const RoundPlan& ps, float pmn, float inv_pmn, uint64_t seed, uint64_t offset,
               void* stream);
 // Strided batches: GEMM z reads A + z*sa, B + z*sb and writes D + z*sd.
+// acc_fmt (optional, RNE plan of an f32 source) rounds the accumulator into a
+// whole format after every MAC / chunk instead of to mbits mantissa bits.
 int launch_gemm_plain(const float* A, int64_t lda, int64_t sa, int ta, const float* B,
                       int64_t ldb, int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M,
-                      int N, int K, int batch, int mbits, float alpha, void* stream);
+                      int N, int K, int batch, int mbits, const RoundPlan* acc_fmt, float alpha,
+                      void* stream);
 int launch_gemm_f64(const float* A, int64_t lda, int ta, const float* B, int64_t ldb, int tb,
                     double* D, int64_t ldd, int M, int N, int K, void* stream);
 int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float* B, int64_t ldb,
                    int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M, int N, int K,
-                   int batch, int mbits, float alpha, int chunk, void* workspace,
-                   size_t workspace_bytes, void* stream);
+                   int batch, int mbits, const RoundPlan* acc_fmt, float alpha, int chunk,
+                   void* workspace, size_t workspace_bytes, void* stream);
 size_t gemm_tc_workspace(int M, int N, int K, int batch);
 
 }  // namespace lofgb

@@ -152,7 +152,7 @@ class LinearConfig:
                  round_mode=lof.RoundingMode.RoundToNearestEven, accum_mant_bits=10,
                  variant="plain", chunk=32, grad_format=None,
                  grad_round_mode=lof.RoundingMode.StochasticRoundingA, grad_stoch_len=8,
-                 grad_variant=None, alpha=1.0):
+                 grad_variant=None, alpha=1.0, accum_format=None):
         self.act_format = act_format
         self.weight_format = weight_format
         self.scale_format = scale_format if scale_format is not None else create_e8m0_params()
@@ -166,6 +166,9 @@ class LinearConfig:
         self.grad_stoch_len = grad_stoch_len
         self.grad_variant = grad_variant or variant
         self.alpha = float(alpha)  # forward output scale: D = alpha * acc
+        # a whole accumulator format (e.g. FP16-like 5e/10m) instead of
+        # accum_mant_bits mantissa bits with FP32's exponent range
+        self.accum_format = accum_format
 
 
 def _mx(t, fmt, cfg):
@@ -192,7 +195,7 @@ class LoFLinearFunction(torch.autograd.Function):
         xq = _mx(x32, cfg.act_format, cfg)
         wq = _mx(w32, cfg.weight_format, cfg)
         y = lof.gemm(xq, wq, cfg.accum_mant_bits, trans_b=True, alpha=cfg.alpha, variant=cfg.variant,
-                     chunk=cfg.chunk)
+                     chunk=cfg.chunk, accum_format=cfg.accum_format)
         ctx.save_for_backward(xq, wq)
         ctx.cfg = cfg
         ctx.dtypes = (x.dtype, w.dtype)
@@ -210,11 +213,12 @@ class LoFLinearFunction(torch.autograd.Function):
                                    stoch_len=cfg.grad_stoch_len)
         dx = dw = None
         if ctx.needs_input_grad[0]:
-            dx = lof.gemm(dy, wq, cfg.accum_mant_bits, variant=cfg.grad_variant, chunk=cfg.chunk)
+            dx = lof.gemm(dy, wq, cfg.accum_mant_bits, variant=cfg.grad_variant, chunk=cfg.chunk,
+                          accum_format=cfg.accum_format)
             dx = dx.to(ctx.dtypes[0])
         if ctx.needs_input_grad[1]:
             dw = lof.gemm(dy, xq, cfg.accum_mant_bits, trans_a=True, variant=cfg.grad_variant,
-                          chunk=cfg.chunk)
+                          chunk=cfg.chunk, accum_format=cfg.accum_format)
             dw = dw.to(ctx.dtypes[1])
         return dx, dw, None
 

@@ -713,6 +713,25 @@ int orc_gemm_f32(const float* A, int64_t lda, int ta, const float* B, int64_t ld
                              nthreads);
 }
 
+int orc_gemm_accfmt_f32(const float* A, int64_t lda, int ta, const float* B, int64_t ldb,
+                        int tb, float* D, int64_t ldd, int M, int N, int K,
+                        const lofgb_format* fmt, float alpha, int nthreads) {
+    int st = check_gemm(A, lda, ta, B, ldb, tb, D, ldd, M, N, K, 10);
+    if (st) return st;
+    if ((st = orc_validate_format(fmt, 23))) return st;
+    const int64_t total = (int64_t)M * N;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthr(nthreads))
+    for (int64_t t = 0; t < total; ++t) {
+        const int i = (int)(t / N), j = (int)(t % N);
+        float acc = 0.0f;
+        for (int k = 0; k < K; ++k)
+            acc = orc_vr_f32(orc_rto_fma(ldA(A, lda, ta, i, k), ldB(B, ldb, tb, k, j), acc), fmt,
+                             LOFGB_RNE, 0, 0, 0.0);
+        D[(int64_t)i * ldd + j] = alpha * acc;
+    }
+    return 0;
+}
+
 int orc_gemm_chunked_f32(const float* A, int64_t lda, int ta, const float* B,
                          int64_t ldb, int tb, float* D, int64_t ldd, int M, int N, int K,
                          int mbits, int chunk, float alpha, int nthreads) {

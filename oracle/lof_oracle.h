@@ -94,6 +94,11 @@ int orc_gemm_f32(const float* A, int64_t lda, int trans_a, const float* B, int64
 int orc_gemm_f32_rows(const float* A, int64_t lda, int trans_a, const float* B,
                       int64_t ldb, int trans_b, float* D, int64_t ldd, int M, int N,
                       int K, int mbits, float alpha, int row0, int rows, int nthreads);
+/* The same with the accumulator rounded into a whole format after every MAC:
+ * acc = vr(rto_fma(A[i,k], B[k,j], acc), fmt, RNE) (lofgb_gemm_accfmt_f32). */
+int orc_gemm_accfmt_f32(const float* A, int64_t lda, int trans_a, const float* B, int64_t ldb,
+                        int trans_b, float* D, int64_t ldd, int M, int N, int K,
+                        const lofgb_format* fmt, float alpha, int nthreads);
 /* The device leaf's round-to-odd FMA (src/cutlass_gemms.cuh:73-88). */
 float orc_rto_fma(float a, float b, float c);
 /* Chunked accumulation model of the tensor-core form with exact chunk sums:

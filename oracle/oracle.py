@@ -85,6 +85,8 @@ def lib():
         L.orc_packed_size.argtypes = [i32, i64]
         L.orc_encode_f32.argtypes = [vp, vp, i64, CP, i32, i32, i32, i32, u64, u64]
         L.orc_decode_f32.argtypes = [vp, vp, i64, CP, i32]
+        L.orc_gemm_accfmt_f32.argtypes = [vp, i64, i32, vp, i64, i32, vp, i64, i32, i32, i32, P,
+                                          f32, i32]
         L.orc_rto_fma.restype = f32
         L.orc_rto_fma.argtypes = [f32, f32, f32]
         L.orc_max_threads.restype = i32
@@ -327,3 +329,13 @@ def encode_rep(x: float, f: CodecFormat, mode: int = 0, sat: int = 0) -> int:
 
 def decode_rep(rep: int, f: CodecFormat) -> float:
     return float(lib().orc_codec_decode_rep(rep, C.byref(f)))
+
+
+def gemm_accfmt(A, B, f: Format, alpha: float = 1.0, trans_a: int = 0, trans_b: int = 0,
+                nthreads: int = 0) -> np.ndarray:
+    """Sequential-k emulated GEMM with the accumulator rounded into format f."""
+    A, B, M, N, K = _gemm_args(A, B, trans_a, trans_b)
+    D = np.empty((M, N), np.float32)
+    _check(lib().orc_gemm_accfmt_f32(_p(A), A.shape[1], trans_a, _p(B), B.shape[1], trans_b,
+                                     _p(D), N, M, N, K, C.byref(f), alpha, nthreads))
+    return D

@@ -112,3 +112,15 @@ def test_layer_constructor_validation():
     conv = torch.nn.Conv2d(8, 4, 3, padding=1, bias=True)
     lifted = lg.LoF_Conv2d.from_conv2d(conv, e4m3, e4m3, bias_params=e4m3)
     assert torch.equal(lifted.weight, conv.weight) and lifted.padding == (1, 1)
+
+
+def test_format_accumulator_oracle_reduces_to_mantissa_rounding():
+    """With FP32's exponent range (8 exponent bits, bias 127) and no
+    overflow or subnormal sums, rounding the accumulator into the format is
+    the mantissa-only rounding of the reference leaf."""
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((20, 300)).astype(np.float32)
+    B = rng.standard_normal((300, 16)).astype(np.float32)
+    for m in (7, 10, 12):
+        fmt = O.fmt(9 + m, m, 127, saturating=False)
+        assert same_bits(O.gemm_accfmt(A, B, fmt, alpha=0.25), O.gemm(A, B, m, alpha=0.25))

@@ -116,6 +116,19 @@ def test_ieee_and_special_formats():
         assert same_bits(gpu_decode(buf, n, f), O.decode(buf, n, f))
 
 
+def test_decode_rounds_into_float_subnormals():
+    """Codes whose values lie below FP32's normal range with more significant
+    bits than a float subnormal holds: one rounding of the exact value."""
+    f = O.codec_fmt(16, 10, 150, False, True, True, 0x8000, 0xFC00, 0x7C00, 0xFC00, 0x7E00, 0x7C01, 1)
+    codes = np.arange(1 << 16, dtype=np.uint16)
+    buf = codes.view(np.uint8)
+    got = gpu_decode(buf, codes.size, f)
+    want = O.decode(buf, codes.size, f)
+    assert same_bits(got, want)
+    sub = (np.abs(want) < 2.0 ** -126) & (want != 0)
+    assert sub.sum() > 1000
+
+
 def test_round_trip_of_representable_values():
     """encode(decode(c)) == c for every finite code of E4M3 / P3109<6,3> /
     FP16: the packed stream of all codes, decoded and re-encoded."""

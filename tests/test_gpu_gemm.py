@@ -105,3 +105,51 @@ def test_config3_sample_rows():
     ref = lg.gemm_f64_reference(Ag, Bg)
     rel = ((D.double() - ref).abs() / ref.abs().clamp_min(1e-3 * ref.abs().mean())).mean().item()
     assert rel < 5e-2
+
+
+def _half_fmt():
+    return O.fmt(16, 10, 15, saturating=False)
+
+
+@pytest.mark.parametrize("fmt_t", [(16, 10, 15, False), (8, 2, 15, True), (19, 10, 127, False),
+                                   (12, 6, 15, False)])
+@pytest.mark.parametrize("tb", [0, 1])
+def test_format_accumulator_vs_oracle(fmt_t, tb):
+    """Accumulator rounded into a whole format after every MAC (the FP16-like
+    5e/10m accumulator and others, incl. one outside the float-rounding
+    path): bit-exact to the oracle, overflow and underflow included."""
+    bw, m, bias, sat = fmt_t
+    rng = np.random.default_rng(bw * 100 + m + tb)
+    M, N, K = 96, 80, 200
+    A = (rng.standard_normal((M, K)) * 2.0 ** rng.integers(-12, 9, (M, K))).astype(np.float32)
+    B = rng.standard_normal((N, K) if tb else (K, N)).astype(np.float32)
+    desc = lg.FloatFormatDescriptor(bw, m, bias, lg.InfBehavior.Saturating if sat else lg.InfBehavior.Extended,
+                                    lg.NaNBehavior._754, lg.Signedness.Signed,
+                                    lg.formats.P3109_InfChecker(bw), lg.formats.P3109_NaNChecker(bw))
+    got = from_gpu(lg.gemm(to_gpu(A), to_gpu(B), 10, trans_b=bool(tb), alpha=0.5, accum_format=desc))
+    want = O.gemm_accfmt(A, B, O.fmt(bw, m, bias, saturating=sat), alpha=0.5, trans_b=tb)
+    ok, _ = same_bits_nan_class(got, want)
+    assert ok, mismatch_report(got, got, want)
+
+
+def test_format_accumulator_tc():
+    rng = np.random.default_rng(5)
+    A = _mx_e4m3(rng.standard_normal((256, 512)).astype(np.float32))
+    B = _mx_e4m3(rng.standard_normal((192, 512)).astype(np.float32))
+    half = lg.create_half_params()
+    Ag, Bg = to_gpu(A), to_gpu(B)
+    tc = from_gpu(lg.gemm(Ag, Bg, 10, trans_b=True, variant="tc", chunk=64, accum_format=half))
+    plain = from_gpu(lg.gemm(Ag, Bg, 10, trans_b=True, accum_format=half))
+    ref = from_gpu(lg.gemm_f64_reference(Ag, Bg, trans_b=True))
+    scale = np.abs(ref).mean()
+    assert np.abs(tc - ref).max() / scale <= 1.5 * np.abs(plain - ref).max() / scale + 1e-3
+    # exact small integers: both forms exact within FP16's range
+    Ai = rng.integers(-3, 4, (64, 128)).astype(np.float32)
+    Bi = rng.integers(-3, 4, (128, 48)).astype(np.float32)
+    tci = from_gpu(lg.gemm(to_gpu(Ai), to_gpu(Bi), 10, variant="tc", accum_format=half))
+    assert np.array_equal(tci, (Ai.astype(np.float64) @ Bi).astype(np.float32))
+    # overflow of the FP16 range: the extended format's +inf
+    big = np.full((4, 64), 3000.0, np.float32)  # 64 * 3000 > 65504
+    ob = from_gpu(lg.gemm(to_gpu(big), to_gpu(np.ones((64, 4), np.float32)), 10, accum_format=half))
+    assert np.all(np.isinf(ob))
+    assert lg.binding.tc_device_status() == 0
