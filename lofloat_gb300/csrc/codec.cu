@@ -20,6 +20,8 @@
 // HBM-bound: 4 + n/8 bytes per element either way.
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include "lof_round.cuh"
 
 namespace lofgb {
@@ -35,6 +37,20 @@ struct CodecArg {
     int nan_kind, neg_to_nan;
     int mode, sat, len;
     uint64_t seed, offset;
+    // Fast encode (enc_fast 1, RNE): the magnitude is
+    // rounded on the float grid (whole-range float rounding, uni_* as in
+    // RoundPlan) and its code read off the bits of the rounded value.
+    int enc_fast;
+    uint32_t uni_lo, uni_hi, uni_d;
+    uint32_t min_norm_bits;   // FP32 bits of the smallest target normal, 2^(1-bias)
+    uint32_t code_off;        // normal code = (bits >> (23 - m)) - code_off
+    float sub_scale;          // subnormal code = value * 2^(bias + m - 1)
+    uint32_t max_finite, ovf_code, inf_code, neg_zero_code, neg_code, sign_mask;
+    // Fast decode: every finite value is a normal FP32 number or an exact
+    // FP32 subnormal, so the bits are built directly.
+    int dec_fast;
+    float tiny;               // 2^(1 - bias - m)
+    uint32_t code_off_dec;    // normal value bits = (mag << (23 - m)) - code_off_dec
 };
 
 __device__ __forceinline__ bool c_is_nan(uint32_t rep, const CodecArg& a) {
@@ -133,6 +149,44 @@ __device__ __forceinline__ uint32_t codec_encode(float from, const CodecArg& a, 
     return with_sign(bits);
 }
 
+// convert_float_to_rep under RNE for formats whose subnormals sit inside
+// FP32's range (CodecArg::enc_fast): the same code as codec_encode,
+// branch-free. The float grid reproduces RoundMantissa's RNE on the normal
+// branch and on the target-subnormal branch alike (including the reference's
+// shift > 24 table, 0 for RNE).
+__device__ __forceinline__ uint32_t codec_encode_fast(float from, const CodecArg& a) {
+    const uint32_t fb = __float_as_uint(from);
+    const bool neg = (fb >> 31) != 0;
+    const uint32_t mb = fb & 0x7FFFFFFFu;
+    const uint32_t cb = min(max(fb & 0x7F800000u, a.uni_lo), a.uni_hi) + a.uni_d;
+    const float c = __uint_as_float(cb);
+    const float ax = __uint_as_float(mb);
+    const float v = __fsub_rn(__fadd_rn(ax, c), c);
+    const uint32_t vb = __float_as_uint(v);
+    uint32_t code = vb >= a.min_norm_bits ? (vb >> (23 - a.m)) - a.code_off
+                                          : __float2uint_rz(__fmul_rn(v, a.sub_scale));
+    code = code > a.max_finite ? a.ovf_code : code;
+    code = mb == 0x7F800000u ? a.inf_code : code;
+    code = (neg && a.is_signed) ? (code == 0u ? a.neg_zero_code : (code | a.sign_mask)) : code;
+    code = mb > 0x7F800000u ? a.qnan : code;
+    return (neg && !a.is_signed) ? a.neg_code : code;
+}
+
+// convert_rep_to_float for formats whose values FP32 holds exactly
+// (CodecArg::dec_fast).
+__device__ __forceinline__ float codec_decode_fast(uint32_t rep, const CodecArg& a) {
+    const uint32_t sbit = a.is_signed ? (rep >> (a.n - 1)) & 1u : 0u;
+    const uint32_t mag = rep & ~a.sign_mask;
+    const uint32_t e = mag >> a.m;
+    const float sub = __fmul_rn(__uint2float_rn(mag), a.tiny);
+    const uint32_t nb = (mag << (23 - a.m)) - a.code_off_dec;
+    uint32_t vb = e == 0 ? __float_as_uint(sub) : nb;
+    vb = c_is_nan(rep, a) ? 0x7FC00000u : (vb | (sbit << 31));
+    // infinity is tested first, as convert_rep_to_float does
+    vb = (a.has_inf && (rep | a.inf_or) == a.inf_match) ? (0x7F800000u | (sbit << 31)) : vb;
+    return __uint_as_float(vb);
+}
+
 // convert_rep_to_float, src/lo_pack.hpp:293-320.
 __device__ __forceinline__ float codec_decode(uint32_t rep, const CodecArg& a) {
     const int n = a.n;
@@ -172,7 +226,7 @@ __device__ __forceinline__ int slot_element(int s) {
     return g * GC + (GC - 1 - k);
 }
 
-template <int N, bool REV, int MODE>
+template <int N, bool REV, int MODE, int FAST>
 __global__ void __launch_bounds__(CT)
 encode_kernel(const float* __restrict__ src, uint32_t* __restrict__ dst, int64_t count,
               int64_t out_bytes, CodecArg a) {
@@ -194,23 +248,42 @@ encode_kernel(const float* __restrict__ src, uint32_t* __restrict__ dst, int64_t
         }
         __syncwarp();
         // this lane's 32 codes, appended to a bit stream of N words
-        uint64_t acc = 0;
-        int fill = 0, widx = 0;
         uint32_t* out = &sw[wib][lane * (N + 1)];
+        const float* xin = &sx[wib][lane * 33];
+        if constexpr (FAST != 0) {
+            // fully unrolled: every bit position and shared-memory offset is a constant
+            uint64_t acc = 0;
+            int fill = 0, widx = 0;
+#pragma unroll
+            for (int s = 0; s < 32; ++s) {
+                const uint32_t code = codec_encode_fast(xin[slot_element<N, REV>(s)], a) &
+                                      ((1u << N) - 1u);
+                acc |= (uint64_t)code << fill;
+                fill += N;
+                if (fill >= 32) {
+                    out[widx++] = (uint32_t)acc;
+                    acc >>= 32;
+                    fill -= 32;
+                }
+            }
+        } else {
+            uint64_t acc = 0;
+            int fill = 0, widx = 0;
 #pragma unroll 2
-        for (int s = 0; s < 32; ++s) {
-            const int i = slot_element<N, REV>(s);
-            const int e = lane * 32 + i;
-            const float x = sx[wib][e + lane];
-            const uint64_t r = mode_is_stochastic(MODE >= 0 ? MODE : a.mode)
-                                   ? rng64(a.seed, a.offset + (uint64_t)(e0 + e)) : 0ull;
-            const uint32_t code = codec_encode<MODE>(x, a, r) & ((1u << N) - 1u);
-            acc |= (uint64_t)code << fill;
-            fill += N;
-            if (fill >= 32) {
-                out[widx++] = (uint32_t)acc;
-                acc >>= 32;
-                fill -= 32;
+            for (int s = 0; s < 32; ++s) {
+                const int i = slot_element<N, REV>(s);
+                const int e = lane * 32 + i;
+                const float x = xin[i];
+                const uint64_t r = mode_is_stochastic(MODE >= 0 ? MODE : a.mode)
+                                       ? rng64(a.seed, a.offset + (uint64_t)(e0 + e)) : 0ull;
+                const uint32_t code = codec_encode<MODE>(x, a, r) & ((1u << N) - 1u);
+                acc |= (uint64_t)code << fill;
+                fill += N;
+                if (fill >= 32) {
+                    out[widx++] = (uint32_t)acc;
+                    acc >>= 32;
+                    fill -= 32;
+                }
             }
         }
         __syncwarp();
@@ -230,7 +303,7 @@ encode_kernel(const float* __restrict__ src, uint32_t* __restrict__ dst, int64_t
     }
 }
 
-template <int N, bool REV>
+template <int N, bool REV, bool FAST>
 __global__ void __launch_bounds__(CT)
 decode_kernel(const uint32_t* __restrict__ src, float* __restrict__ dst, int64_t count,
               int64_t in_bytes, CodecArg a) {
@@ -255,19 +328,33 @@ decode_kernel(const uint32_t* __restrict__ src, float* __restrict__ dst, int64_t
         }
         __syncwarp();
         const uint32_t* in = &sw[wib][lane * (N + 1)];
+        float* xout = &sx[wib][lane * 33];
         uint64_t buf = 0;
         int avail = 0, widx = 0;
-#pragma unroll 2
-        for (int s = 0; s < 32; ++s) {
-            if (avail < N) {
-                buf |= (uint64_t)in[widx++] << avail;
-                avail += 32;
+        if constexpr (FAST) {
+#pragma unroll
+            for (int s = 0; s < 32; ++s) {
+                if (avail < N) {
+                    buf |= (uint64_t)in[widx++] << avail;
+                    avail += 32;
+                }
+                const uint32_t code = (uint32_t)buf & ((1u << N) - 1u);
+                buf >>= N;
+                avail -= N;
+                xout[slot_element<N, REV>(s)] = codec_decode_fast(code, a);
             }
-            const uint32_t code = (uint32_t)buf & ((1u << N) - 1u);
-            buf >>= N;
-            avail -= N;
-            const int e = lane * 32 + slot_element<N, REV>(s);
-            sx[wib][e + lane] = codec_decode(code, a);
+        } else {
+#pragma unroll 2
+            for (int s = 0; s < 32; ++s) {
+                if (avail < N) {
+                    buf |= (uint64_t)in[widx++] << avail;
+                    avail += 32;
+                }
+                const uint32_t code = (uint32_t)buf & ((1u << N) - 1u);
+                buf >>= N;
+                avail -= N;
+                xout[slot_element<N, REV>(s)] = codec_decode(code, a);
+            }
         }
         __syncwarp();
         const bool full = e0 + TILE <= count;
@@ -319,6 +406,45 @@ int make_codec_arg(CodecArg* a, const lofgb_codec_format* f, int mode, int sat, 
     a->mode = mode;
     a->sat = sat;
     a->len = len;
+    // fast paths (see CodecArg)
+    const int n = a->n, m = a->m, bias = a->bias;
+    const int to_min = 1 - bias;
+    const int to_max = (1 << ebits) - 1 - bias;
+    a->sign_mask = a->is_signed ? (1u << (n - 1)) : 0u;
+    a->max_finite = a->has_inf ? a->pos_inf - 1u
+                               : (a->is_signed ? (((1u << n) - 1u) >> 1) : ((1u << n) - 1u));
+    const uint32_t inf_rep = a->has_inf ? a->pos_inf : a->max_finite;
+    a->inf_code = (sat != LOFGB_SAT_FINITE && a->has_inf) ? inf_rep : a->max_finite;
+    a->ovf_code = (sat == LOFGB_OVF_INF && a->has_inf) ? inf_rep : a->max_finite;
+    a->neg_code = a->neg_to_nan ? (a->nan3109 ? a->qnan : a->snan) : 0u;
+    bool sign_only_nan = false;  // IsNaN(sign-only code)
+    if (a->is_signed) {
+        const uint32_t sm = a->sign_mask;
+        if (a->nan_kind == LOFGB_NAN_PATTERN) sign_only_nan = sm == a->qnan;
+        else if (a->nan_kind == LOFGB_NAN_IEEE) sign_only_nan = false;  // magnitude 0
+    }
+    a->neg_zero_code = sign_only_nan ? 0u : a->sign_mask;
+    const bool narrower = to_max < 128 || (to_max == 128 && m + 1 < 24);
+    const int d = 23 - m;
+    const int hi = to_max + 1 + 127;
+    a->enc_fast = 0;
+    if (mode == LOFGB_RNE && narrower &&
+        to_min > -125 && bias >= -100 && bias + m - 1 <= 127 && hi + d <= 254 &&
+        to_min + 127 + d >= 1 && hi >= to_min + 127) {
+        a->enc_fast = 1;
+        a->uni_lo = (uint32_t)(to_min + 127) << 23;
+        a->uni_hi = (uint32_t)hi << 23;
+        a->uni_d = (uint32_t)d << 23;
+        a->min_norm_bits = (uint32_t)(to_min + 127) << 23;
+        a->code_off = (uint32_t)(127 - bias) << m;
+        a->sub_scale = std::ldexp(1.0f, bias + m - 1);
+    }
+    a->dec_fast = 0;
+    if (to_min + 127 >= 1 && to_max + 127 <= 254 && to_min - m >= -149) {
+        a->dec_fast = 1;
+        a->tiny = std::ldexp(1.0f, to_min - m);
+        a->code_off_dec = (uint32_t)(bias - 127) << 23;
+    }
     return LOFGB_OK;
 }
 
@@ -336,12 +462,13 @@ int launch_encode_n(const float* src, uint8_t* dst, int64_t count, int reverse, 
     const int grid = grid_for(count);
     const int64_t ob = packed_bytes(N, count);
     uint32_t* d = reinterpret_cast<uint32_t*>(dst);
-#define LOFGB_ENC(R, M) encode_kernel<N, R, M><<<grid, CT, 0, st>>>(src, d, count, ob, a)
-    if (a.mode == LOFGB_RNE) {
-        if (reverse) LOFGB_ENC(true, LOFGB_RNE); else LOFGB_ENC(false, LOFGB_RNE);
-    } else {
-        if (reverse) LOFGB_ENC(true, -1); else LOFGB_ENC(false, -1);
-    }
+#define LOFGB_ENC(R, M, F) encode_kernel<N, R, M, F><<<grid, CT, 0, st>>>(src, d, count, ob, a)
+#define LOFGB_ENC_R(M, F) do { if (reverse) LOFGB_ENC(true, M, F); else LOFGB_ENC(false, M, F); } while (0)
+    // the float-grid path for RNE (the codec's common mode); every other
+    // mode and format through the general restatement
+    if (a.enc_fast == 1) LOFGB_ENC_R(LOFGB_RNE, 1);
+    else LOFGB_ENC_R(-1, 0);
+#undef LOFGB_ENC_R
 #undef LOFGB_ENC
     return check_launch("encode_kernel");
 }
@@ -352,8 +479,13 @@ int launch_decode_n(const uint8_t* src, float* dst, int64_t count, int reverse, 
     const int grid = grid_for(count);
     const int64_t ib = packed_bytes(N, count);
     const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
-    if (reverse) decode_kernel<N, true><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
-    else decode_kernel<N, false><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
+    if (a.dec_fast) {
+        if (reverse) decode_kernel<N, true, true><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
+        else decode_kernel<N, false, true><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
+    } else {
+        if (reverse) decode_kernel<N, true, false><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
+        else decode_kernel<N, false, false><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
+    }
     return check_launch("decode_kernel");
 }
 

@@ -43,13 +43,12 @@ __device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
             const uint4 a = __ldcs(vin + v);
             const uint64_t i = (uint64_t)v * 4;
             uint32_t w[4] = {a.x, a.y, a.z, a.w};
-            uint64_t r[4];
+            uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
             const int mode = MODE >= 0 ? MODE : t.plan.mode;
+            if (mode_is_stochastic(mode)) rng64x4(t.seed, t.offset + i, r);
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < 4; ++q)
                 if (t.apply_scale) w[q] = __float_as_uint(__fmul_rn(t.scale, __uint_as_float(w[q])));
-                r[q] = mode_is_stochastic(mode) ? rng64(t.seed, t.offset + i + q) : 0ull;
-            }
             if constexpr (UNI != 0) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) w[q] = vr_uni_f32<MODE, UNI>(w[q], t.plan);

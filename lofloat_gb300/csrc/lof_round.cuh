@@ -28,11 +28,25 @@ namespace lofgb {
 
 // ---- counter-based RNG: SplitMix64 (Steele, Lea, Flood 2014) ---------------
 // The idx-th output of a SplitMix64 stream whose state starts at `seed`.
-__device__ __forceinline__ uint64_t rng64(uint64_t seed, uint64_t idx) {
-    uint64_t z = seed + (idx + 1ull) * 0x9E3779B97F4A7C15ull;
+constexpr uint64_t SM64_GAMMA = 0x9E3779B97F4A7C15ull;
+
+__device__ __forceinline__ uint64_t sm64_mix(uint64_t z) {
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ uint64_t rng64(uint64_t seed, uint64_t idx) {
+    return sm64_mix(seed + (idx + 1ull) * SM64_GAMMA);
+}
+
+// Outputs idx .. idx+3: the states step by the constant gamma.
+__device__ __forceinline__ void rng64x4(uint64_t seed, uint64_t idx, uint64_t (&r)[4]) {
+    const uint64_t z = seed + (idx + 1ull) * SM64_GAMMA;
+    r[0] = sm64_mix(z);
+    r[1] = sm64_mix(z + SM64_GAMMA);
+    r[2] = sm64_mix(z + 2ull * SM64_GAMMA);
+    r[3] = sm64_mix(z + 3ull * SM64_GAMMA);
 }
 
 __device__ __forceinline__ double usamp_of(uint64_t r) {

@@ -87,12 +87,11 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
                 o = make_uint4(w[0], w[1], w[2], w[3]);
             } else if constexpr (W == 32 && FMT) {
                 uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-                uint64_t r[4];
+                uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
+                if (needs_rng<MODE>(p)) rng64x4(seed, e0, r);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < 4; ++q)
                     if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
-                    r[q] = needs_rng<MODE>(p) ? rng64(seed, e0 + q) : 0ull;
-                }
                 if (full) vr_format_f32x4<MODE, true>(w, p, r);
                 else vr_format_f32x4<MODE, false>(w, p, r);
                 o = make_uint4(w[0], w[1], w[2], w[3]);
