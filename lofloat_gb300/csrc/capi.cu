@@ -178,12 +178,20 @@ int make_round_plan(RoundPlan* p, const lofgb_format* f, int src_bits, int mode,
     p->sat_and = p->saturating ? 0xFFFFFFFFu : 0u;
     p->sat_or = p->saturating ? 0u : 0x7F800000u;
     const int hi = p->to_max_field + 1;
-    if (p->grid != 0 && p->d >= 1 && p->tiny_thr >= 0x00800000ull && hi + p->d <= 254 &&
-        p->to_min_field >= 1 && hi >= p->to_min_field) {
-        p->uni = p->grid;
+    const bool uni_ok = src_bits == 32 && p->d >= 1 && p->tiny_thr >= 0x00800000ull &&
+                        hi + p->d <= 254 && p->to_min_field >= 1 && hi >= p->to_min_field;
+    if (uni_ok) {
         p->uni_lo = (uint32_t)p->to_min_field << 23;
         p->uni_hi = (uint32_t)hi << 23;
         p->uni_d = (uint32_t)p->d << 23;
+    }
+    if (uni_ok && p->grid != 0) p->uni = p->grid;
+    // tiny * 2^-len normal: (to_min - m) - len >= -126
+    p->sr_uni = 0;
+    if (uni_ok && mode == LOFGB_SR_A && len <= p->d && len <= 24 && gexp - len >= -126) {
+        p->sr_uni = 1;
+        p->sr_mask = len >= 32 ? 0xFFFFFFFFu : ((1u << len) - 1u);
+        p->sr_shift = (uint32_t)(23 + len) << 23;
     }
     return LOFGB_OK;
 }

@@ -49,7 +49,10 @@ __device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 if (t.apply_scale) w[q] = __float_as_uint(__fmul_rn(t.scale, __uint_as_float(w[q])));
-            if constexpr (UNI != 0) {
+            if constexpr (UNI == 3) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) w[q] = vr_uni_sra_f32(w[q], t.plan, r[q]);
+            } else if constexpr (UNI != 0) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) w[q] = vr_uni_f32<MODE, UNI>(w[q], t.plan);
             } else {
@@ -87,7 +90,7 @@ grouped_round_kernel(const GroupedTask* __restrict__ tasks, int ntasks, int64_t 
         __syncthreads();
         const int64_t e0 = (item - t.item_begin) * GROUPED_ITEM;
         const int64_t e1 = min(e0 + GROUPED_ITEM, t.n);
-        // uni is 1 only for RNE and 2 only for RTZ / RAFZ / RU / RD
+        // uni is 1 only for RNE and 2 only for RTZ / RAFZ / RU / RD; sr_uni only for SR-A
         switch (t.plan.mode) {
         case LOFGB_RNE:
             if (t.plan.uni) run_item<LOFGB_RNE, 1>(t, e0, e1);
@@ -98,7 +101,10 @@ grouped_round_kernel(const GroupedTask* __restrict__ tasks, int ntasks, int64_t 
             else run_item<LOFGB_RTZ, 0>(t, e0, e1);
             break;
         case LOFGB_RTO: run_item<LOFGB_RTO, 0>(t, e0, e1); break;
-        case LOFGB_SR_A: run_item<LOFGB_SR_A, 0>(t, e0, e1); break;
+        case LOFGB_SR_A:
+            if (t.plan.sr_uni) run_item<LOFGB_SR_A, 3>(t, e0, e1);
+            else run_item<LOFGB_SR_A, 0>(t, e0, e1);
+            break;
         default:
             if (t.plan.uni) run_item<-1, 2>(t, e0, e1);
             else run_item<-1, 0>(t, e0, e1);

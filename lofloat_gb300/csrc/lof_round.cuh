@@ -372,6 +372,23 @@ __device__ __forceinline__ uint32_t vr_uni_f32(uint32_t x, const RoundPlan& p) {
     return (x & 0x7FFFFFFFu) > 0x7F800000u ? 0x7FC00000u : res;
 }
 
+// virtual_round(x, params, {SR-A, len}) of an f32 word by float arithmetic
+// (RoundPlan::sr_uni); r is the element's random word.
+__device__ __forceinline__ uint32_t vr_uni_sra_f32(uint32_t x, const RoundPlan& p, uint64_t r) {
+    const uint32_t mag = x & 0x7FFFFFFFu;
+    const uint32_t cbx = min(max(x & 0x7F800000u, p.uni_lo), p.uni_hi) + p.uni_d;
+    const float noise = __fmul_rn(__uint2float_rn((uint32_t)r & p.sr_mask),
+                                  __uint_as_float(cbx - p.sr_shift));
+    const float y = __fadd_rz(__uint_as_float(mag), noise);
+    const uint32_t cby = min(max(__float_as_uint(y) & 0x7F800000u, p.uni_lo), p.uni_hi) + p.uni_d;
+    const float cy = __uint_as_float(cby);
+    const uint32_t v = __float_as_uint(__fsub_rn(__fadd_rz(y, cy), cy));
+    uint32_t res = v | (x & 0x80000000u);
+    res = v >= (uint32_t)p.ovf_thr ? ((x & p.sat_and) | p.sat_or) : res;
+    res = mag < (uint32_t)p.tiny_thr ? (x & 0x80000000u) : res;
+    return mag > 0x7F800000u ? 0x7FC00000u : res;
+}
+
 // virtual_round(x, ToMantissaBits, ps), src/lo_float.h:2715-2756.
 template <int MODE, int W>
 __device__ __forceinline__ typename Src<W>::U vr_mantissa(typename Src<W>::U x, int d,

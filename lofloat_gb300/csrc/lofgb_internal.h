@@ -56,7 +56,18 @@ struct RoundPlan {
     int32_t uni;
     uint32_t uni_lo, uni_hi, uni_d;  // FP32 exponent fields, shifted to bit 23
     uint32_t sat_and, sat_or;        // overflow result: (x & sat_and) | sat_or
-    int32_t pad2;
+    // Stochastic rounding A by float arithmetic (sr_uni): with the same C,
+    // the noise R' * spacing * 2^-len (R' = R & sr_mask, spacing = ulp(C)) is
+    // a multiple of ulp(|x|) when len <= d; y = fadd_rz(|x|, noise) then
+    // truncated to the spacing at y (fadd_rz(y, C_y) - C_y) is the reference's
+    // integer SR-A — within a binade the bit-pattern sum is the value sum, and
+    // a carry into the next binade truncates to 2^(e+1) either way; rounding y
+    // toward zero never crosses a multiple of the spacing. Magnitudes below
+    // tiny flush to +-0 (the stochastic modes' tiny branch). Valid when the
+    // uni conditions hold without a float grid and len <= min(d, 24) with
+    // tiny * 2^-len a normal float.
+    int32_t sr_uni;
+    uint32_t sr_mask, sr_shift;      // R' mask; (23 + len) << 23
 };
 
 // Host side.

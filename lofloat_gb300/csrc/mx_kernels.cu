@@ -57,12 +57,7 @@ struct BlockScale {
     bool pos, pow2;
 };
 
-template <int SMODE>
-__device__ __forceinline__ BlockScale block_scale(float amax, const RoundPlan& ps, float inv_pmn,
-                                                  uint64_t seed, uint64_t blk_elem) {
-    const float sin = __fmul_rn(amax, inv_pmn);
-    const uint64_t r = stoch<SMODE>(ps.mode) ? rng64(seed ^ SCALE_SALT, blk_elem) : 0ull;
-    const uint32_t sb = vr_format_f32_voted<SMODE>(__float_as_uint(sin), ps, r);
+__device__ __forceinline__ BlockScale scale_from_bits(uint32_t sb) {
     BlockScale b;
     b.scale = __uint_as_float(sb);
     b.pos = b.scale > 0.0f;
@@ -74,6 +69,15 @@ __device__ __forceinline__ BlockScale block_scale(float amax, const RoundPlan& p
     b.inv = __uint_as_float(0x7F000000u - (sb & 0x7F800000u));
     return b;
 }
+
+template <int SMODE>
+__device__ __forceinline__ BlockScale block_scale(float amax, const RoundPlan& ps, float inv_pmn,
+                                                  uint64_t seed, uint64_t blk_elem) {
+    const float sin = __fmul_rn(amax, inv_pmn);
+    const uint64_t r = stoch<SMODE>(ps.mode) ? rng64(seed ^ SCALE_SALT, blk_elem) : 0ull;
+    return scale_from_bits(vr_format_f32_voted<SMODE>(__float_as_uint(sin), ps, r));
+}
+
 
 // Four elements of one block: q = x / scale (x * (1/scale) for power-of-two
 // scales, chosen once per warp), round, rescale; a block whose scale is not
@@ -120,6 +124,9 @@ mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, fl
     constexpr int SLOT = 128 * VPT;  // elements per warp per slot
     constexpr int U = VPT == 1 ? 4 : 2;
     static_assert(L >= 1 && L <= 32 && (L & (L - 1)) == 0, "lanes per block");
+    constexpr int NB = 32 / L;                            // blocks per slot
+    constexpr int P = U * NB;                             // (slot, block) pairs per iteration
+    constexpr bool TRANSPOSED = VPT == 1 && P <= 32;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * MT + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * MT) >> 5;
@@ -134,22 +141,50 @@ mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, fl
 #pragma unroll
                 for (int j = 0; j < VPT; ++j)
                     v[u][j] = __ldcs(reinterpret_cast<const float4*>(in + (s0 + u) * SLOT + j * 128 + lane * 4));
+            float amax[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                float amax = 0.0f;
+                amax[u] = 0.0f;
 #pragma unroll
                 for (int j = 0; j < VPT; ++j)
-                    amax = fmaxf(amax, fmaxf(fmaxf(fabsf(v[u][j].x), fabsf(v[u][j].y)),
-                                             fmaxf(fabsf(v[u][j].z), fabsf(v[u][j].w))));
+                    amax[u] = fmaxf(amax[u], fmaxf(fmaxf(fabsf(v[u][j].x), fabsf(v[u][j].y)),
+                                                   fmaxf(fabsf(v[u][j].z), fabsf(v[u][j].w))));
 #pragma unroll
                 for (int off = L / 2; off > 0; off >>= 1)
-                    amax = fmaxf(amax, __shfl_xor_sync(0xFFFFFFFFu, amax, off));
-                const int64_t blk0 = (s0 + u) * SLOT + (int64_t)(lane / L) * BS;
-                const BlockScale b = block_scale<SMODE>(amax, ps, inv_pmn, seed, offset + blk0);
+                    amax[u] = fmaxf(amax[u], __shfl_xor_sync(0xFFFFFFFFu, amax[u], off));
+            }
+            if constexpr (TRANSPOSED) {
+                // one scale per lane for the U * NB (slot, block) pairs of this
+                // iteration instead of one per lane and slot: lane j takes pair
+                // j mod P, gathers its amax, rounds the scale, and every lane
+                // then fetches the scale bits of its own blocks
+                const int pj = lane % P;
+                const int uj = pj / NB, bj = pj % NB;
+                float aj = 0.0f;
 #pragma unroll
-                for (int j = 0; j < VPT; ++j) {
-                    const int64_t e = (s0 + u) * SLOT + j * 128 + lane * 4;
-                    __stcs(reinterpret_cast<float4*>(out + e), quant4<EMODE, true, UNI>(v[u][j], b, pe, seed, offset + (uint64_t)e));
+                for (int u = 0; u < U; ++u) {
+                    const float g = __shfl_sync(0xFFFFFFFFu, amax[u], bj * L);
+                    aj = u == uj ? g : aj;
+                }
+                const int64_t blkj = (s0 + uj) * SLOT + (int64_t)bj * BS;
+                const uint32_t sbj = __float_as_uint(block_scale<SMODE>(aj, ps, inv_pmn, seed, offset + blkj).scale);
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const uint32_t sb = __shfl_sync(0xFFFFFFFFu, sbj, u * NB + lane / L);
+                    const BlockScale b = scale_from_bits(sb);
+                    const int64_t e = (s0 + u) * SLOT + lane * 4;
+                    __stcs(reinterpret_cast<float4*>(out + e), quant4<EMODE, true, UNI>(v[u][0], b, pe, seed, offset + (uint64_t)e));
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int64_t blk0 = (s0 + u) * SLOT + (int64_t)(lane / L) * BS;
+                    const BlockScale b = block_scale<SMODE>(amax[u], ps, inv_pmn, seed, offset + blk0);
+#pragma unroll
+                    for (int j = 0; j < VPT; ++j) {
+                        const int64_t e = (s0 + u) * SLOT + j * 128 + lane * 4;
+                        __stcs(reinterpret_cast<float4*>(out + e), quant4<EMODE, true, UNI>(v[u][j], b, pe, seed, offset + (uint64_t)e));
+                    }
                 }
             }
             continue;

@@ -77,7 +77,18 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
             if (!full && vi >= nvec) continue;
             const uint64_t e0 = offset + (uint64_t)vi * EPV;
             uint4 o;
-            if constexpr (W == 32 && FMT && UNI != 0) {
+            if constexpr (W == 32 && FMT && UNI == 3) {
+                // SR-A by float arithmetic (RoundPlan::sr_uni)
+                uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+                uint64_t r[4];
+                rng64x4(seed, e0, r);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
+                    w[q] = vr_uni_sra_f32(w[q], p, r[q]);
+                }
+                o = make_uint4(w[0], w[1], w[2], w[3]);
+            } else if constexpr (W == 32 && FMT && UNI != 0) {
                 uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
@@ -194,6 +205,10 @@ int launch_w(const void* in, void* out, int64_t n, const RoundPlan& p, const Sca
         if (p.uni == 2) {
             if (p.mode == LOFGB_RTZ) LOFGB_RVU(LOFGB_RTZ, 2);
             else LOFGB_RVU(-1, 2);
+            return check_launch("round_vec_kernel");
+        }
+        if (p.sr_uni) {
+            LOFGB_RVU(LOFGB_SR_A, 3);
             return check_launch("round_vec_kernel");
         }
     }
