@@ -216,9 +216,21 @@ def cpu_baseline_sample():
         if time.perf_counter() - t0 > 10.0:
             break
     dt = time.perf_counter() - t0
+    # single-thread figure on a smaller sample (about 3 s)
+    x1 = x[: 1 << 19]
+    reps1, t1 = 0, time.perf_counter()
+    while True:
+        for ef in efs:
+            O.mx_round(x1, MX_BLOCK, ef, sf, nthreads=1)
+        reps1 += 1
+        if time.perf_counter() - t1 > 3.0:
+            break
+    dt1 = time.perf_counter() - t1
     return {"value": reps * len(efs) * x.size * 8 / dt / 1e9, "unit": "GB/s", "cores": threads,
             "kind": "port",
-            "sample": f"MX rounding of 2^22 of the 2^26 config elements, 3 formats x {reps} reps"}
+            "sample": f"MX rounding of 2^22 of the 2^26 config elements, 3 formats x {reps} reps",
+            "single_thread": {"value": reps1 * len(efs) * x1.size * 8 / dt1 / 1e9, "unit": "GB/s",
+                              "sample": f"2^19 elements, 3 formats x {reps1} reps"}}
 
 
 def time_events(torch, fn, reps, stream):

@@ -115,80 +115,118 @@ __device__ __forceinline__ float4 quant4(float4 x, const BlockScale& b, const Ro
 }
 
 // BS: block size; VPT float4s per lane per block; L lanes per block.
+// Geometry of one block size: BS elements per block, VPT float4s per lane per
+// block, L lanes per block, SLOT elements per warp per slot, U slots per warp
+// iteration; NB blocks per slot and P = U * NB (slot, block) pairs per
+// iteration. With P <= 32 the scales are computed transposed (one pair per
+// lane).
+template <int BS>
+struct MxGeo {
+    static constexpr int VPT = BS >= 256 ? BS / 128 : 1;
+    static constexpr int L = BS / (4 * VPT);
+    static constexpr int SLOT = 128 * VPT;
+    static constexpr int U = VPT == 1 ? 4 : 2;
+    static constexpr int NB = 32 / L;
+    static constexpr int P = U * NB;
+    static constexpr bool TRANSPOSED = VPT == 1 && P <= 32;
+    static_assert(L >= 1 && L <= 32 && (L & (L - 1)) == 0, "lanes per block");
+};
+
+template <int BS>
+__device__ __forceinline__ void load_slots(float4 (&v)[MxGeo<BS>::U][MxGeo<BS>::VPT],
+                                           const float* in, int64_t s0, int lane) {
+    using G = MxGeo<BS>;
+#pragma unroll
+    for (int u = 0; u < G::U; ++u)
+#pragma unroll
+        for (int j = 0; j < G::VPT; ++j)
+            v[u][j] = __ldcs(reinterpret_cast<const float4*>(in + (s0 + u) * G::SLOT + j * 128 + lane * 4));
+}
+
+// U full slots starting at slot s0, already in registers.
+template <int BS, int EMODE, int SMODE, int UNI>
+__device__ __forceinline__ void mx_full_slots(const float4 (&v)[MxGeo<BS>::U][MxGeo<BS>::VPT],
+                                              float* out, int64_t s0, int lane, const RoundPlan& pe,
+                                              const RoundPlan& ps, float inv_pmn, uint64_t seed,
+                                              uint64_t offset) {
+    using G = MxGeo<BS>;
+    constexpr int U = G::U, VPT = G::VPT, L = G::L, NB = G::NB, P = G::P, SLOT = G::SLOT;
+    float amax[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        amax[u] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < VPT; ++j)
+            amax[u] = fmaxf(amax[u], fmaxf(fmaxf(fabsf(v[u][j].x), fabsf(v[u][j].y)),
+                                           fmaxf(fabsf(v[u][j].z), fabsf(v[u][j].w))));
+#pragma unroll
+        for (int off = L / 2; off > 0; off >>= 1)
+            amax[u] = fmaxf(amax[u], __shfl_xor_sync(0xFFFFFFFFu, amax[u], off));
+    }
+    if constexpr (G::TRANSPOSED) {
+        // one scale per lane for the P (slot, block) pairs of this iteration
+        // instead of one per lane and slot: lane j takes pair j mod P, gathers
+        // its amax, rounds the scale, and every lane then fetches the scale
+        // bits of its own blocks
+        const int pj = lane % P;
+        const int uj = pj / NB, bj = pj % NB;
+        float aj = 0.0f;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const float g = __shfl_sync(0xFFFFFFFFu, amax[u], bj * L);
+            aj = u == uj ? g : aj;
+        }
+        const int64_t blkj = (s0 + uj) * SLOT + (int64_t)bj * BS;
+        const uint32_t sbj = __float_as_uint(block_scale<SMODE>(aj, ps, inv_pmn, seed, offset + blkj).scale);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t sb = __shfl_sync(0xFFFFFFFFu, sbj, u * NB + lane / L);
+            const BlockScale b = scale_from_bits(sb);
+            const int64_t e = (s0 + u) * SLOT + lane * 4;
+            __stcs(reinterpret_cast<float4*>(out + e), quant4<EMODE, true, UNI>(v[u][0], b, pe, seed, offset + (uint64_t)e));
+        }
+    } else {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t blk0 = (s0 + u) * SLOT + (int64_t)(lane / L) * BS;
+            const BlockScale b = block_scale<SMODE>(amax[u], ps, inv_pmn, seed, offset + blk0);
+#pragma unroll
+            for (int j = 0; j < VPT; ++j) {
+                const int64_t e = (s0 + u) * SLOT + j * 128 + lane * 4;
+                __stcs(reinterpret_cast<float4*>(out + e), quant4<EMODE, true, UNI>(v[u][j], b, pe, seed, offset + (uint64_t)e));
+            }
+        }
+    }
+}
+
+// The float-grid instantiations fit 5 CTAs of 256 threads per SM (<= 48
+// registers, the occupancy the HBM stream needs); the general ones would
+// spill under that bound.
 template <int BS, int EMODE, int SMODE, bool ALIGNED, int UNI = 0>
-__global__ void __launch_bounds__(MT)
+__global__ void __launch_bounds__(MT, UNI != 0 ? 5 : 1)
 mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, float inv_pmn,
           uint64_t seed, uint64_t offset) {
-    constexpr int VPT = BS >= 256 ? BS / 128 : 1;
-    constexpr int L = BS / (4 * VPT);
-    constexpr int SLOT = 128 * VPT;  // elements per warp per slot
-    constexpr int U = VPT == 1 ? 4 : 2;
-    static_assert(L >= 1 && L <= 32 && (L & (L - 1)) == 0, "lanes per block");
-    constexpr int NB = 32 / L;                            // blocks per slot
-    constexpr int P = U * NB;                             // (slot, block) pairs per iteration
-    constexpr bool TRANSPOSED = VPT == 1 && P <= 32;
+    using G = MxGeo<BS>;
+    constexpr int U = G::U, VPT = G::VPT, L = G::L, SLOT = G::SLOT;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * MT + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * MT) >> 5;
     const int64_t nslots = (n + SLOT - 1) / SLOT;
     const int64_t full_slots = n / SLOT;  // slots entirely inside the tensor
-    for (int64_t s0 = warp * U; s0 < nslots; s0 += nwarps * U) {
-        if (ALIGNED && s0 + U <= full_slots) {
-            // common case: U full slots, no bounds checks
+    const int64_t step = nwarps * U;
+    int64_t s0 = warp * U;
+    if (ALIGNED) {
+        // common case: runs of U full slots, no bounds checks (issuing the
+        // next run's loads early measured slower: the extra registers cost
+        // more occupancy than the overlap gained)
+        for (; s0 + U <= full_slots; s0 += step) {
             float4 v[U][VPT];
-#pragma unroll
-            for (int u = 0; u < U; ++u)
-#pragma unroll
-                for (int j = 0; j < VPT; ++j)
-                    v[u][j] = __ldcs(reinterpret_cast<const float4*>(in + (s0 + u) * SLOT + j * 128 + lane * 4));
-            float amax[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                amax[u] = 0.0f;
-#pragma unroll
-                for (int j = 0; j < VPT; ++j)
-                    amax[u] = fmaxf(amax[u], fmaxf(fmaxf(fabsf(v[u][j].x), fabsf(v[u][j].y)),
-                                                   fmaxf(fabsf(v[u][j].z), fabsf(v[u][j].w))));
-#pragma unroll
-                for (int off = L / 2; off > 0; off >>= 1)
-                    amax[u] = fmaxf(amax[u], __shfl_xor_sync(0xFFFFFFFFu, amax[u], off));
-            }
-            if constexpr (TRANSPOSED) {
-                // one scale per lane for the U * NB (slot, block) pairs of this
-                // iteration instead of one per lane and slot: lane j takes pair
-                // j mod P, gathers its amax, rounds the scale, and every lane
-                // then fetches the scale bits of its own blocks
-                const int pj = lane % P;
-                const int uj = pj / NB, bj = pj % NB;
-                float aj = 0.0f;
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const float g = __shfl_sync(0xFFFFFFFFu, amax[u], bj * L);
-                    aj = u == uj ? g : aj;
-                }
-                const int64_t blkj = (s0 + uj) * SLOT + (int64_t)bj * BS;
-                const uint32_t sbj = __float_as_uint(block_scale<SMODE>(aj, ps, inv_pmn, seed, offset + blkj).scale);
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const uint32_t sb = __shfl_sync(0xFFFFFFFFu, sbj, u * NB + lane / L);
-                    const BlockScale b = scale_from_bits(sb);
-                    const int64_t e = (s0 + u) * SLOT + lane * 4;
-                    __stcs(reinterpret_cast<float4*>(out + e), quant4<EMODE, true, UNI>(v[u][0], b, pe, seed, offset + (uint64_t)e));
-                }
-            } else {
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int64_t blk0 = (s0 + u) * SLOT + (int64_t)(lane / L) * BS;
-                    const BlockScale b = block_scale<SMODE>(amax[u], ps, inv_pmn, seed, offset + blk0);
-#pragma unroll
-                    for (int j = 0; j < VPT; ++j) {
-                        const int64_t e = (s0 + u) * SLOT + j * 128 + lane * 4;
-                        __stcs(reinterpret_cast<float4*>(out + e), quant4<EMODE, true, UNI>(v[u][j], b, pe, seed, offset + (uint64_t)e));
-                    }
-                }
-            }
-            continue;
+            load_slots<BS>(v, in, s0, lane);
+            mx_full_slots<BS, EMODE, SMODE, UNI>(v, out, s0, lane, pe, ps, inv_pmn, seed, offset);
         }
+    }
+    // partial runs (and every run of a misaligned tensor)
+    for (; s0 < nslots; s0 += step) {
         float4 v[U][VPT];
 #pragma unroll
         for (int u = 0; u < U; ++u)
