@@ -24,6 +24,19 @@ namespace lofgb {
 namespace {
 
 constexpr int MT = 256;
+constexpr int RING = 3;  // cp.async stages per thread (RING - 1 runs prefetched)
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 constexpr uint64_t SCALE_SALT = 0x5CA1E5CA1E5CA1E5ull;
 
 template <bool ALIGNED>
@@ -132,17 +145,6 @@ struct MxGeo {
     static_assert(L >= 1 && L <= 32 && (L & (L - 1)) == 0, "lanes per block");
 };
 
-template <int BS>
-__device__ __forceinline__ void load_slots(float4 (&v)[MxGeo<BS>::U][MxGeo<BS>::VPT],
-                                           const float* in, int64_t s0, int lane) {
-    using G = MxGeo<BS>;
-#pragma unroll
-    for (int u = 0; u < G::U; ++u)
-#pragma unroll
-        for (int j = 0; j < G::VPT; ++j)
-            v[u][j] = __ldcs(reinterpret_cast<const float4*>(in + (s0 + u) * G::SLOT + j * 128 + lane * 4));
-}
-
 // U full slots starting at slot s0, already in registers.
 template <int BS, int EMODE, int SMODE, int UNI>
 __device__ __forceinline__ void mx_full_slots(const float4 (&v)[MxGeo<BS>::U][MxGeo<BS>::VPT],
@@ -216,14 +218,40 @@ mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, fl
     const int64_t step = nwarps * U;
     int64_t s0 = warp * U;
     if (ALIGNED) {
-        // common case: runs of U full slots, no bounds checks (issuing the
-        // next run's loads early measured slower: the extra registers cost
-        // more occupancy than the overlap gained)
-        for (; s0 + U <= full_slots; s0 += step) {
-            float4 v[U][VPT];
-            load_slots<BS>(v, in, s0, lane);
-            mx_full_slots<BS, EMODE, SMODE, UNI>(v, out, s0, lane, pe, ps, inv_pmn, seed, offset);
+        // common case: runs of U full slots, no bounds checks. Each thread
+        // streams its own 16-byte pieces of the next RING - 1 runs into
+        // shared memory with cp.async while it rounds the current run, so the
+        // HBM reads in flight do not occupy registers; a thread only reads
+        // back what it copied itself, so no CTA barrier is needed.
+        __shared__ float4 ring[RING][U * VPT][MT];
+        auto issue = [&](int stage, int64_t s) {
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int j = 0; j < VPT; ++j)
+                    cp_async16(&ring[stage][u * VPT + j][threadIdx.x],
+                               in + (s + u) * SLOT + j * 128 + lane * 4);
+        };
+        int64_t sp = s0;  // next run to prefetch
+#pragma unroll
+        for (int k = 0; k < RING - 1; ++k, sp += step) {
+            if (sp + U <= full_slots) issue(k, sp);
+            cp_async_commit();
         }
+        int stage = 0;
+        for (; s0 + U <= full_slots; s0 += step, sp += step) {
+            if (sp + U <= full_slots) issue(stage == 0 ? RING - 1 : stage - 1, sp);
+            cp_async_commit();
+            cp_async_wait<RING - 1>();  // this run's group has landed
+            float4 v[U][VPT];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int j = 0; j < VPT; ++j) v[u][j] = ring[stage][u * VPT + j][threadIdx.x];
+            mx_full_slots<BS, EMODE, SMODE, UNI>(v, out, s0, lane, pe, ps, inv_pmn, seed, offset);
+            stage = stage == RING - 1 ? 0 : stage + 1;
+        }
+        cp_async_wait<0>();
     }
     // partial runs (and every run of a misaligned tensor)
     for (; s0 < nslots; s0 += step) {
