@@ -19,6 +19,19 @@ namespace {
 
 constexpr int RT = 256;  // threads per CTA
 constexpr int RU = 4;    // 16-byte vectors per thread per iteration
+constexpr int RING = 3;  // cp.async stages per thread (RING - 1 iterations prefetched)
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 struct ScaleArg {
     float f;      // f32 scale, or the f16 scale widened to float
@@ -63,75 +76,105 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
     constexpr int EPV = 128 / W;  // elements per 16-byte vector
     const int64_t nvec = n / EPV;
     const int64_t stride = (int64_t)gridDim.x * RT * RU;
-    for (int64_t base = (int64_t)blockIdx.x * RT * RU; base < nvec; base += stride) {
-        const bool full = base + RT * RU <= nvec;  // CTA-uniform: no per-vector checks
-        uint4 v[RU];
+    // one 16-byte vector: element index vi * EPV .. vi * EPV + EPV - 1; `full`:
+    // every lane of the warp is here (the voted rare-branch path may use the
+    // full mask)
+    auto round_vec = [&](const uint4& vv, int64_t vi, bool full) -> uint4 {
+        const uint64_t e0 = offset + (uint64_t)vi * EPV;
+        uint4 o;
+        if constexpr (W == 32 && FMT && UNI == 3) {
+            // SR-A by float arithmetic (RoundPlan::sr_uni)
+            uint32_t w[4] = {vv.x, vv.y, vv.z, vv.w};
+            uint64_t r[4];
+            rng64x4(seed, e0, r);
 #pragma unroll
-        for (int u = 0; u < RU; ++u) {
-            const int64_t vi = base + u * RT + threadIdx.x;
-            if (full || vi < nvec) v[u] = __ldcs(vin + vi);
-        }
-#pragma unroll
-        for (int u = 0; u < RU; ++u) {
-            const int64_t vi = base + u * RT + threadIdx.x;
-            if (!full && vi >= nvec) continue;
-            const uint64_t e0 = offset + (uint64_t)vi * EPV;
-            uint4 o;
-            if constexpr (W == 32 && FMT && UNI == 3) {
-                // SR-A by float arithmetic (RoundPlan::sr_uni)
-                uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-                uint64_t r[4];
-                rng64x4(seed, e0, r);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
-                    w[q] = vr_uni_sra_f32(w[q], p, r[q]);
-                }
-                o = make_uint4(w[0], w[1], w[2], w[3]);
-            } else if constexpr (W == 32 && FMT && UNI != 0) {
-                uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
-                    w[q] = vr_uni_f32<MODE, UNI>(w[q], p);
-                }
-                o = make_uint4(w[0], w[1], w[2], w[3]);
-            } else if constexpr (W == 32 && FMT) {
-                uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-                uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
-                if (needs_rng<MODE>(p)) rng64x4(seed, e0, r);
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
-                if (full) vr_format_f32x4<MODE, true>(w, p, r);
-                else vr_format_f32x4<MODE, false>(w, p, r);
-                o = make_uint4(w[0], w[1], w[2], w[3]);
-            } else if constexpr (W == 32) {
-                o.x = process<MODE, 32, FMT, SCALED>(v[u].x, p, s, seed, e0 + 0);
-                o.y = process<MODE, 32, FMT, SCALED>(v[u].y, p, s, seed, e0 + 1);
-                o.z = process<MODE, 32, FMT, SCALED>(v[u].z, p, s, seed, e0 + 2);
-                o.w = process<MODE, 32, FMT, SCALED>(v[u].w, p, s, seed, e0 + 3);
-            } else if constexpr (W == 64) {
-                const uint64_t a = ((uint64_t)v[u].y << 32) | v[u].x;
-                const uint64_t b = ((uint64_t)v[u].w << 32) | v[u].z;
-                const uint64_t ra = process<MODE, 64, FMT, SCALED>(a, p, s, seed, e0 + 0);
-                const uint64_t rb = process<MODE, 64, FMT, SCALED>(b, p, s, seed, e0 + 1);
-                o.x = (uint32_t)ra;
-                o.y = (uint32_t)(ra >> 32);
-                o.z = (uint32_t)rb;
-                o.w = (uint32_t)(rb >> 32);
-            } else {
-                const uint32_t in4[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
-                uint32_t out4[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const U lo = process<MODE, 16, FMT, SCALED>(in4[q] & 0xFFFFu, p, s, seed, e0 + 2 * q);
-                    const U hi = process<MODE, 16, FMT, SCALED>(in4[q] >> 16, p, s, seed, e0 + 2 * q + 1);
-                    out4[q] = (lo & 0xFFFFu) | (hi << 16);
-                }
-                o = make_uint4(out4[0], out4[1], out4[2], out4[3]);
+            for (int q = 0; q < 4; ++q) {
+                if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
+                w[q] = vr_uni_sra_f32(w[q], p, r[q]);
             }
-            __stcs(vout + vi, o);
+            o = make_uint4(w[0], w[1], w[2], w[3]);
+        } else if constexpr (W == 32 && FMT && UNI != 0) {
+            uint32_t w[4] = {vv.x, vv.y, vv.z, vv.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
+                w[q] = vr_uni_f32<MODE, UNI>(w[q], p);
+            }
+            o = make_uint4(w[0], w[1], w[2], w[3]);
+        } else if constexpr (W == 32 && FMT) {
+            uint32_t w[4] = {vv.x, vv.y, vv.z, vv.w};
+            uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
+            if (needs_rng<MODE>(p)) rng64x4(seed, e0, r);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
+            if (full) vr_format_f32x4<MODE, true>(w, p, r);
+            else vr_format_f32x4<MODE, false>(w, p, r);
+            o = make_uint4(w[0], w[1], w[2], w[3]);
+        } else if constexpr (W == 32) {
+            o.x = process<MODE, 32, FMT, SCALED>(vv.x, p, s, seed, e0 + 0);
+            o.y = process<MODE, 32, FMT, SCALED>(vv.y, p, s, seed, e0 + 1);
+            o.z = process<MODE, 32, FMT, SCALED>(vv.z, p, s, seed, e0 + 2);
+            o.w = process<MODE, 32, FMT, SCALED>(vv.w, p, s, seed, e0 + 3);
+        } else if constexpr (W == 64) {
+            const uint64_t a = ((uint64_t)vv.y << 32) | vv.x;
+            const uint64_t b = ((uint64_t)vv.w << 32) | vv.z;
+            const uint64_t ra = process<MODE, 64, FMT, SCALED>(a, p, s, seed, e0 + 0);
+            const uint64_t rb = process<MODE, 64, FMT, SCALED>(b, p, s, seed, e0 + 1);
+            o.x = (uint32_t)ra;
+            o.y = (uint32_t)(ra >> 32);
+            o.z = (uint32_t)rb;
+            o.w = (uint32_t)(rb >> 32);
+        } else {
+            const uint32_t in4[4] = {vv.x, vv.y, vv.z, vv.w};
+            uint32_t out4[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const U lo = process<MODE, 16, FMT, SCALED>(in4[q] & 0xFFFFu, p, s, seed, e0 + 2 * q);
+                const U hi = process<MODE, 16, FMT, SCALED>(in4[q] >> 16, p, s, seed, e0 + 2 * q + 1);
+                out4[q] = (lo & 0xFFFFu) | (hi << 16);
+            }
+            o = make_uint4(out4[0], out4[1], out4[2], out4[3]);
+        }
+        return o;
+    };
+    int64_t base = (int64_t)blockIdx.x * RT * RU;
+    {
+        // full iterations: each thread streams its own vectors of the next
+        // RING - 1 iterations into shared memory with cp.async while it
+        // rounds the current one (reads in flight without registers; a thread
+        // reads back only what it copied, so no CTA barrier)
+        __shared__ uint4 ring[RING][RU][RT];
+        auto issue = [&](int stage, int64_t b) {
+#pragma unroll
+            for (int u = 0; u < RU; ++u) cp_async16(&ring[stage][u][threadIdx.x], vin + b + u * RT + threadIdx.x);
+        };
+        int64_t bp = base;
+#pragma unroll
+        for (int k = 0; k < RING - 1; ++k, bp += stride) {
+            if (bp + RT * RU <= nvec) issue(k, bp);
+            cp_async_commit();
+        }
+        int stage = 0;
+        for (; base + RT * RU <= nvec; base += stride, bp += stride) {
+            if (bp + RT * RU <= nvec) issue(stage == 0 ? RING - 1 : stage - 1, bp);
+            cp_async_commit();
+            cp_async_wait<RING - 1>();
+#pragma unroll
+            for (int u = 0; u < RU; ++u) {
+                const int64_t vi = base + u * RT + threadIdx.x;
+                __stcs(vout + vi, round_vec(ring[stage][u][threadIdx.x], vi, true));
+            }
+            stage = stage == RING - 1 ? 0 : stage + 1;
+        }
+        cp_async_wait<0>();
+    }
+    // the last, partial iteration of this CTA
+    for (; base < nvec; base += stride) {
+#pragma unroll
+        for (int u = 0; u < RU; ++u) {
+            const int64_t vi = base + u * RT + threadIdx.x;
+            if (vi < nvec) __stcs(vout + vi, round_vec(__ldcs(vin + vi), vi, false));
         }
     }
     // tail of fewer than EPV elements
@@ -212,12 +255,18 @@ int launch_w(const void* in, void* out, int64_t n, const RoundPlan& p, const Sca
             return check_launch("round_vec_kernel");
         }
     }
-    switch (p.mode) {
-    case LOFGB_RNE: LOFGB_RV(LOFGB_RNE); break;
-    case LOFGB_RTZ: LOFGB_RV(LOFGB_RTZ); break;
-    case LOFGB_RTO: LOFGB_RV(LOFGB_RTO); break;
-    case LOFGB_SR_A: LOFGB_RV(LOFGB_SR_A); break;
-    default: LOFGB_RV(-1); break;
+    // mode-specialised element loops for f32 sources; f64 and f16 sources
+    // share the runtime-mode loop
+    if constexpr (W == 32) {
+        switch (p.mode) {
+        case LOFGB_RNE: LOFGB_RV(LOFGB_RNE); break;
+        case LOFGB_RTZ: LOFGB_RV(LOFGB_RTZ); break;
+        case LOFGB_RTO: LOFGB_RV(LOFGB_RTO); break;
+        case LOFGB_SR_A: LOFGB_RV(LOFGB_SR_A); break;
+        default: LOFGB_RV(-1); break;
+        }
+    } else {
+        LOFGB_RV(-1);
     }
 #undef LOFGB_RV
 #undef LOFGB_RVU
