@@ -7,7 +7,8 @@
 //   acc_0 = +0;  acc_{k+1} = RNE_m(rto_fma(A[i,k], B[k,j], acc_k)), k = 0..K-1
 //   D[i,j] = alpha * acc_K
 // with rto_fma the round-to-odd FMA of src/cutlass_gemms.cuh:73-88
-// (rd = fma.rm, ru = fma.rp, rz = rd >= 0 ? rd : ru, sticky = rd != ru).
+// (rd = fma.rm, ru = fma.rp, rz = rd >= 0 ? rd : ru, sticky = rd != ru;
+// computed here as the same word by rto_word).
 // Every output keeps that exact k order, so any M/N tiling is bit-exact;
 // K is never split.
 //

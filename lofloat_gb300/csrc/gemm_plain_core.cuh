@@ -21,34 +21,28 @@ constexpr int PAD = 4;
 enum { ACC_NONE = 0, ACC_MANT = 1, ACC_UNI = 2, ACC_FMT = 3 };
 
 struct AccRound {
-    int ro;                   // 23 - mantissa bits
-    uint32_t half_m1, mask;   // RNE constants for ACC_MANT
-    RoundPlan plan;           // the accumulator format for ACC_UNI / ACC_FMT
+    int ro;                       // 23 - mantissa bits
+    uint32_t sh, half_m1, mask;   // RNE constants for ACC_MANT (rne_word)
+    RoundPlan plan;               // the accumulator format for ACC_UNI / ACC_FMT
 };
 
-// One emulated MAC. The round-to-odd word v = rz | sticky: when the two
-// directed FMAs differ they are adjacent, so (rd | ru) & 1 is 1 exactly when
-// the sum was inexact or rz is already odd — the same word as rz | (rd != ru).
-// The RNE step works on the signed word: for finite values (and the GPU's
-// positive canonical NaN) adding < 2^ro never carries into the sign bit.
-// Round-to-odd keeps a sticky bit below FP32's last place, so rounding v to
-// the (narrower) accumulator equals rounding the exact a*b + acc.
+// One emulated MAC: the round-to-odd word of the two directed FMAs
+// (rto_word), then the accumulator rounding. Round-to-odd keeps a sticky bit
+// below FP32's last place, so rounding v to the (narrower) accumulator equals
+// rounding the exact a*b + acc.
 template <int ACC>
 __device__ __forceinline__ float emac(float a, float b, float acc, const AccRound& r) {
-    const float rd = __fmaf_rd(a, b, acc);
-    const float ru = __fmaf_ru(a, b, acc);
-    const uint32_t rz = __float_as_uint(rd >= 0.0f ? rd : ru);
-    const uint32_t v = rz | ((__float_as_uint(rd) | __float_as_uint(ru)) & 1u);
+    const uint32_t v = rto_word(__fmaf_rd(a, b, acc), __fmaf_ru(a, b, acc));
     if (ACC == ACC_NONE) return __uint_as_float(v);
     if (ACC == ACC_UNI) return __uint_as_float(vr_uni_f32<LOFGB_RNE, 1>(v, r.plan));
     if (ACC == ACC_FMT) return __uint_as_float(vr_format<LOFGB_RNE, 32>(v, r.plan, 0ull));
-    const uint32_t t = v + ((v >> r.ro) & 1u) + r.half_m1;
-    return __uint_as_float(t & r.mask);
+    return __uint_as_float(rne_word(v, r.sh, r.half_m1, r.mask));
 }
 
 AccRound acc_mant(int mbits) {
     AccRound r = {};
     r.ro = 23 - mbits;
+    r.sh = r.ro > 0 ? 1u << (32 - r.ro) : 0u;
     r.half_m1 = r.ro > 0 ? (1u << (r.ro - 1)) - 1u : 0u;
     r.mask = r.ro > 0 ? ~((1u << r.ro) - 1u) : ~0u;
     return r;

@@ -49,6 +49,28 @@ __device__ __forceinline__ void rng64x4(uint64_t seed, uint64_t idx, uint64_t (&
     r[3] = sm64_mix(z + 3ull * SM64_GAMMA);
 }
 
+// ---- round-to-odd word and RNE to m mantissa bits (the GEMM leaf) ----------
+// The round-to-odd result of one FP32 operation from its two directed
+// roundings rd (toward -inf) and ru (toward +inf). The reference form
+// (src/cutlass_gemms.cuh:73-88) is rz | (rd != ru) with rz = rd >= 0 ? rd : ru.
+// Inexact: rd and ru are adjacent words (also across 0 and at the overflow
+// edge), exactly one of them is odd, and that one is rz | 1. Exact: rd == ru,
+// or the zero pair rd = -0, ru = +0 where the reference keeps rd. NaN: both
+// are the canonical 0x7FFFFFFF. So "ru if ru is odd, else rd" gives the same
+// word for every input with one test and one select.
+__device__ __forceinline__ uint32_t rto_word(float rd, float ru) {
+    const uint32_t d = __float_as_uint(rd), u = __float_as_uint(ru);
+    return (u & 1u) ? u : d;
+}
+
+// RNE of the FP32 word v to 23 - ro mantissa bits, 1 <= ro <= 23, on the
+// signed word (adding < 2^ro never carries into the sign bit of a finite
+// value or of the canonical NaN). sh = 2^(32 - ro): the multiply-high is
+// v >> ro on the multiply pipe, leaving the logic pipe three operations.
+__device__ __forceinline__ uint32_t rne_word(uint32_t v, uint32_t sh, uint32_t half_m1, uint32_t mask) {
+    return (v + (__umulhi(v, sh) & 1u) + half_m1) & mask;
+}
+
 __device__ __forceinline__ double usamp_of(uint64_t r) {
     return (double)(r >> 11) * 0x1.0p-53;
 }
