@@ -96,7 +96,11 @@ int lofgb_version(void);
  * out[i] = virtual_round(scale * in[i], fmt, {mode, OvfInf, stoch_len}).
  * `scale` is applied in the source type, as the reference kernel does
  * (src/Lof_kernel.cu:52); scale == 1 skips the multiply.
- * Stochastic modes draw R = SplitMix64(seed, offset + i) per element i.
+ * Stochastic modes: element g = offset + i reads lane g mod 2^lg (from the
+ * low end, 64 >> lg bits) of SplitMix64 output g >> lg of the stream `seed`,
+ * lanes the narrowest of 8/16/32/64 bits holding what the mode reads
+ * (SR-A/B/C: stoch_len bits, SR-D: stoch_len + 1, Prob: 1, True SR: 64), so
+ * a stream split at any offset reproduces the single call.
  * f16 data is IEEE binary16 bit patterns (uint16_t). */
 int lofgb_round_f32(const float* in, float* out, int64_t n, const lofgb_format* fmt,
                     int mode, int stoch_len, float scale, uint64_t seed,
@@ -383,8 +387,8 @@ int lofgb_pwl_silu_f16(const uint16_t* in, uint16_t* out, int64_t n, const float
  * reference's RoundMantissa (its RoundUp / RoundDown see a positive-sign flag
  * of false, as there); overflow -> infinity under OvfInf with infinities,
  * else the largest finite code; -0 of a format whose sign-only code is NaN
- * encodes as +0. Stochastic modes draw R = SplitMix64(seed, offset + i) for
- * element i, as the rounding entry points do. Values: convert_rep_to_float
+ * encodes as +0. Stochastic modes draw element i's random lane from
+ * (seed, offset + i) as the rounding entry points do. Values: convert_rep_to_float
  * (:293-320): infinity and NaN codes by the format's predicates, else the
  * exact value (in double) narrowed to float.
  *

@@ -124,6 +124,7 @@ int make_round_plan(RoundPlan* p, const lofgb_format* f, int src_bits, int mode,
     const float t = tiny, h = half;
     p->mode = mode;
     p->len = len;
+    p->rng_lg = rng_lanes_log2(mode, len);
     p->d = srcM - m;
     p->to_min_field = to_min + srcBias;
     p->to_max_field = to_max + srcBias;
@@ -205,6 +206,7 @@ int make_mantissa_plan(RoundPlan* p, int src_bits, int mbits, int mode, int len)
     memset(p, 0, sizeof(*p));
     p->mode = mode;
     p->len = len;
+    p->rng_lg = rng_lanes_log2(mode, len);
     p->d = srcM - mbits;
     p->keep_mask = ~((1ull << p->d) - 1ull);
     return LOFGB_OK;

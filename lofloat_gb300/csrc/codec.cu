@@ -36,6 +36,7 @@ struct CodecArg {
     uint32_t inf_or, inf_match, pos_inf, qnan, snan;
     int nan_kind, neg_to_nan;
     int mode, sat, len;
+    int rng_lg;               // random lanes per SplitMix64 output (RoundPlan::rng_lg)
     uint64_t seed, offset;
     // Fast encode (enc_fast 1, RNE): the magnitude is
     // rounded on the float grid (whole-range float rounding, uni_* as in
@@ -275,7 +276,7 @@ encode_kernel(const float* __restrict__ src, uint32_t* __restrict__ dst, int64_t
                 const int e = lane * 32 + i;
                 const float x = xin[i];
                 const uint64_t r = mode_is_stochastic(MODE >= 0 ? MODE : a.mode)
-                                       ? rng64(a.seed, a.offset + (uint64_t)(e0 + e)) : 0ull;
+                                       ? rng_elem(a.seed, a.offset + (uint64_t)(e0 + e), a.rng_lg) : 0ull;
                 const uint32_t code = codec_encode<MODE>(x, a, r) & ((1u << N) - 1u);
                 acc |= (uint64_t)code << fill;
                 fill += N;
@@ -390,6 +391,7 @@ int make_codec_arg(CodecArg* a, const lofgb_codec_format* f, int mode, int sat, 
     if (mode < 0 || mode >= LOFGB_NUM_MODES) return set_error(LOFGB_ERR_MODE, "unknown mode %d", mode);
     if (sat < 0 || sat > LOFGB_SAT_PROPAGATE) return set_error(LOFGB_ERR_MODE, "unknown saturation mode %d", sat);
     if (len < 0 || len > 62) return set_error(LOFGB_ERR_MODE, "stoch_len %d outside [0, 62]", len);
+    a->rng_lg = rng_lanes_log2(mode, len);
     a->n = F.bitwidth;
     a->m = F.mantissa_bits;
     a->bias = F.bias;

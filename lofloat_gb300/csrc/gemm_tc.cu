@@ -24,8 +24,10 @@
 //   warp 1      TMEM owner and MMA issuer (one elected lane):
 //               tcgen05.mma.cta_group::1.kind::f16, M=128 N=128 K=16,
 //               chunk sums double-buffered in 2 x 128 TMEM columns;
-//   warps 2..9  epilogue: tcgen05.ld the chunk sum of one TMEM lane quarter
-//               and one 64-column half, fold it into 64 register
+//   warps 2..9  epilogue (two per TMEM lane quarter): tcgen05.ld the chunk
+//               sum of its lane quarter and one 64-column half, in four
+//               16-column loads pipelined with the folds (one piece loads
+//               while the previous one is folded), fold it into 64 register
 //               accumulators, release the TMEM buffer; store D at tile end.
 // Every wait is bounded (~2 s of %globaltimer): on expiry the CTA records
 // LOFGB_ERR_TIMEOUT in the workspace status word, drains its own in-flight
@@ -52,8 +54,10 @@ constexpr int SK = 64;            // k per pipeline stage (one 128-byte swizzle 
 constexpr int STAGES = 3;
 constexpr int TILE_BYTES = TBM * SK * 2;       // 16 KiB per operand tile
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;    // A hi, A lo, B hi, B lo
-constexpr int EPI_WARPS = 8;
+constexpr int EPI_WARPS = 8;                   // two per TMEM lane quarter
+constexpr int EPI_COLS = TBN * 4 / EPI_WARPS;  // accumulator columns per epilogue thread
 constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
+static_assert(EPI_COLS == 64, "the epilogue folds four pipelined 16-column pieces");
 constexpr int TMEM_COLS = 2 * TBN;             // two chunk buffers
 constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + STAGES * STAGE_BYTES + 256 /*barriers*/;
 constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;
@@ -185,33 +189,37 @@ __device__ __forceinline__ void tc_fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+// 16 consecutive TMEM columns of this warp's lane quarter, one per register.
+// The registers are valid only after tmem_ld_wait16 on them.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-          "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-          "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
 }
 
-__device__ __forceinline__ void tmem_ld_wait() {
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+// Wait for the outstanding TMEM loads; the registers of r are operands, so
+// no read of r is scheduled before the wait.
+__device__ __forceinline__ void tmem_ld_wait16(uint32_t (&r)[16]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                   "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                   "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+                 :
+                 : "memory");
 }
 
 // acc = RNE_m(rto(acc + s)) with directed adds, as the per-MAC leaf does with
-// directed FMAs (src/cutlass_gemms.cuh:73-88, 162-163).
-__device__ __forceinline__ float fold(float acc, float s, int ro, uint32_t half_m1, uint32_t mask) {
-    const float rd = __fadd_rd(acc, s);
-    const float ru = __fadd_ru(acc, s);
-    const uint32_t rz = __float_as_uint(rd >= 0.0f ? rd : ru);
-    const uint32_t v = rz | ((__float_as_uint(rd) | __float_as_uint(ru)) & 1u);
+// directed FMAs (src/cutlass_gemms.cuh:73-88, 162-163); rto_word / rne_word
+// are that leaf's round-to-odd and RNE steps.
+__device__ __forceinline__ float fold(float acc, float s, int ro, uint32_t sh, uint32_t half_m1,
+                                      uint32_t mask) {
+    const uint32_t v = rto_word(__fadd_rd(acc, s), __fadd_ru(acc, s));
     if (ro <= 0) return __uint_as_float(v);
-    const uint32_t t = v + ((v >> ro) & 1u) + half_m1;
-    return __uint_as_float(t & mask);
+    return __uint_as_float(rne_word(v, sh, half_m1, mask));
 }
 
 // acc = RNE_format(rto(acc + s)) for a whole-format accumulator: the
@@ -219,10 +227,7 @@ __device__ __forceinline__ float fold(float acc, float s, int ro, uint32_t half_
 // the format rounding of the exact sum.
 template <int KIND>
 __device__ __forceinline__ float fold_fmt(float acc, float s, const RoundPlan& p) {
-    const float rd = __fadd_rd(acc, s);
-    const float ru = __fadd_ru(acc, s);
-    const uint32_t rz = __float_as_uint(rd >= 0.0f ? rd : ru);
-    const uint32_t v = rz | ((__float_as_uint(rd) | __float_as_uint(ru)) & 1u);
+    const uint32_t v = rto_word(__fadd_rd(acc, s), __fadd_ru(acc, s));
     if (KIND == 2) return __uint_as_float(vr_uni_f32<LOFGB_RNE, 1>(v, p));
     return __uint_as_float(vr_format<LOFGB_RNE, 32>(v, p, 0ull));
 }
@@ -446,73 +451,96 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
         }
     } else {
         // ---------------- epilogue ----------------
-        const int ew = warp - 2;              // 0..7
+        const int ew = warp - 2;              // 0 .. EPI_WARPS-1
         const int quarter = warp & 3;         // TMEM lane quarter this warp may access
-        const int half = ew >> 2;             // column half
+        const int slice = ew >> 2;            // column slice of EPI_COLS columns
+        const uint32_t lane_base = tmem_base + ((uint32_t)(quarter * 32) << 16) + slice * EPI_COLS;
         uint32_t cg = 0;
         bool ok = true;
+        // every lane waits; the warp goes on only when all lanes saw the phase
+        // complete, reconverged for the .sync.aligned TMEM loads
+        auto wait_full = [&](uint32_t g) -> bool {
+            const bool got = mbar_wait(bar_tfull + 8 * (g & 1u), (g >> 1) & 1u, abort_flag, status);
+            if (!__all_sync(0xFFFFFFFFu, got)) return false;
+            __syncwarp();
+            tc_fence_after();
+            return true;
+        };
         for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
             const TileInfo ti = src.get(tile);
             const int nchunks = (ti.Kp / 16 + ti.chunk16 - 1) / ti.chunk16;
             const int ro = ti.ro;
+            const uint32_t sh = ro > 0 ? 1u << (32 - ro) : 0u;
             const uint32_t half_m1 = ro > 0 ? (1u << (ro - 1)) - 1u : 0u;
             const uint32_t mask = ro > 0 ? ~((1u << ro) - 1u) : ~0u;
-            float acc[64];
+            float acc[EPI_COLS];
 #pragma unroll
-            for (int i = 0; i < 64; ++i) acc[i] = 0.0f;
-            for (int c = 0; c < nchunks; ++c, ++cg) {
-                const uint32_t buf = cg & 1u;
-                // every lane waits; the warp proceeds only when all lanes saw the
-                // phase complete, reconverged for the .sync.aligned TMEM loads
-                const bool got = mbar_wait(bar_tfull + 8 * buf, (cg >> 1) & 1u, abort_flag, status);
-                if (!__all_sync(0xFFFFFFFFu, got)) { ok = false; break; }
-                __syncwarp();
-                tc_fence_after();
-                const uint32_t taddr = tmem_base + ((uint32_t)(quarter * 32) << 16) + buf * TBN + half * 64;
-                uint32_t r0[32], r1[32];
-                tmem_ld32(taddr, r0);
-                tmem_ld32(taddr + 32, r1);
-                tmem_ld_wait();
-                tc_fence_before();
-                mbar_arrive(bar_tempty + 8 * buf);
+            for (int i = 0; i < EPI_COLS; ++i) acc[i] = 0.0f;
+            auto fold16 = [&](int off, const uint32_t (&r)[16]) {
                 if constexpr (ACCK == 0) {
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) acc[i] = fold(acc[i], __uint_as_float(r0[i]), ro, half_m1, mask);
-#pragma unroll
-                    for (int i = 0; i < 32; ++i) acc[32 + i] = fold(acc[32 + i], __uint_as_float(r1[i]), ro, half_m1, mask);
+                    for (int i = 0; i < 16; ++i)
+                        acc[off + i] = fold(acc[off + i], __uint_as_float(r[i]), ro, sh, half_m1, mask);
                 } else {
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) acc[i] = fold_fmt<ACCK>(acc[i], __uint_as_float(r0[i]), *acc_plan);
-#pragma unroll
-                    for (int i = 0; i < 32; ++i) acc[32 + i] = fold_fmt<ACCK>(acc[32 + i], __uint_as_float(r1[i]), *acc_plan);
+                    for (int i = 0; i < 16; ++i)
+                        acc[off + i] = fold_fmt<ACCK>(acc[off + i], __uint_as_float(r[i]), *acc_plan);
                 }
+            };
+            // Four 16-column pieces per chunk, software-pipelined over two
+            // register sets: each piece loads while the previous one is
+            // folded, and piece 0 of chunk c+1 loads during piece 3 of chunk c.
+            uint32_t ra[16], rb[16];
+            if (!wait_full(cg)) { ok = false; break; }
+            tmem_ld16(lane_base + (cg & 1u) * TBN, ra);
+            tmem_ld_wait16(ra);
+            for (int c = 0; c < nchunks; ++c) {
+                const uint32_t col = lane_base + (cg & 1u) * TBN;
+                tmem_ld16(col + 16, rb);
+                fold16(0, ra);
+                tmem_ld_wait16(rb);
+                tmem_ld16(col + 32, ra);
+                fold16(16, rb);
+                tmem_ld_wait16(ra);
+                tmem_ld16(col + 48, rb);
+                fold16(32, ra);
+                tmem_ld_wait16(rb);
+                tc_fence_before();
+                mbar_arrive(bar_tempty + 8 * (cg & 1u));   // all of chunk c is in registers
+                ++cg;
+                const bool more = c + 1 < nchunks;
+                if (more) {
+                    if (!wait_full(cg)) { ok = false; break; }
+                    tmem_ld16(lane_base + (cg & 1u) * TBN, ra);
+                }
+                fold16(48, rb);
+                if (more) tmem_ld_wait16(ra);
             }
             if (!ok) break;
             const int row = ti.m0 + quarter * 32 + lane;
+            const int64_t col0 = ti.n0 + slice * EPI_COLS;
+            const int ncol = min(EPI_COLS, ti.N - (int)col0);
             if (row < ti.M && ti.img_L > 0) {
-                // conv2d output: walk (image, column-in-image) along the 64 columns
-                const int64_t col0 = ti.n0 + half * 64;
-                const int ncol = min(64, ti.N - (int)col0);
+                // conv2d output: walk (image, column-in-image) along the columns
                 int64_t img = col0 / ti.img_L;
                 int64_t l = col0 - img * ti.img_L;
 #pragma unroll
-                for (int i = 0; i < 64; ++i) {
+                for (int i = 0; i < EPI_COLS; ++i) {
                     if (i < ncol) ti.D[img * ti.img_stride + (int64_t)row * ti.ldd + l] = __fmul_rn(ti.alpha, acc[i]);
                     if (++l == ti.img_L) { l = 0; ++img; }
                 }
             } else if (row < ti.M) {
-                float* drow = ti.D + (int64_t)row * ti.ldd + ti.n0 + half * 64;
-                const int ncol = min(64, ti.N - (ti.n0 + half * 64));
-                if (ncol == 64 && ((reinterpret_cast<uintptr_t>(drow) & 15) == 0)) {
+                float* drow = ti.D + (int64_t)row * ti.ldd + col0;
+                if (ncol == EPI_COLS && ((reinterpret_cast<uintptr_t>(drow) & 15) == 0)) {
 #pragma unroll
-                    for (int i = 0; i < 64; i += 4) {
+                    for (int i = 0; i < EPI_COLS; i += 4) {
                         float4 v = make_float4(__fmul_rn(ti.alpha, acc[i]), __fmul_rn(ti.alpha, acc[i + 1]),
                                                __fmul_rn(ti.alpha, acc[i + 2]), __fmul_rn(ti.alpha, acc[i + 3]));
                         *reinterpret_cast<float4*>(drow + i) = v;
                     }
                 } else {
 #pragma unroll
-                    for (int i = 0; i < 64; ++i)
+                    for (int i = 0; i < EPI_COLS; ++i)
                         if (i < ncol) drow[i] = __fmul_rn(ti.alpha, acc[i]);
                 }
             }

@@ -26,7 +26,7 @@ template <int MODE>
 __device__ __forceinline__ uint32_t elem(uint32_t w, const GroupedTask& t, uint64_t idx) {
     if (t.apply_scale) w = __float_as_uint(__fmul_rn(t.scale, __uint_as_float(w)));
     const int mode = MODE >= 0 ? MODE : t.plan.mode;
-    const uint64_t r = mode_is_stochastic(mode) ? rng64(t.seed, t.offset + idx) : 0ull;
+    const uint64_t r = mode_is_stochastic(mode) ? rng_elem(t.seed, t.offset + idx, t.plan.rng_lg) : 0ull;
     return vr_format<MODE, 32>(w, t.plan, r);
 }
 
@@ -45,7 +45,7 @@ __device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
             uint32_t w[4] = {a.x, a.y, a.z, a.w};
             uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
             const int mode = MODE >= 0 ? MODE : t.plan.mode;
-            if (mode_is_stochastic(mode)) rng64x4(t.seed, t.offset + i, r);
+            if (mode_is_stochastic(mode)) rng_elem4(t.seed, t.offset + i, t.plan.rng_lg, r);
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 if (t.apply_scale) w[q] = __float_as_uint(__fmul_rn(t.scale, __uint_as_float(w[q])));

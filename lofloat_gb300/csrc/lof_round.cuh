@@ -12,8 +12,10 @@
 // exact because non-negative IEEE bit patterns order like their values.
 //
 // Defined behaviour where the reference's is undefined (shared with the
-// oracle): roundoff 0 leaves every mode unchanged; a random addend wider than
-// the dropped bits is shifted right instead of left by a negative count; SR-C
+// oracle): roundoff 0 leaves every mode unchanged; the random addend of
+// SR-A/B/C/D keeps the low min(len, W) bits of R (W the source word width);
+// an addend wider than the dropped bits is shifted right instead of left by a
+// negative count; SR-C
 // on 64-bit words uses 64-bit arithmetic; a subnormal-branch shift wider than
 // the word is clamped to width-1 (reachable only when the result is ±0).
 #pragma once
@@ -40,13 +42,39 @@ __device__ __forceinline__ uint64_t rng64(uint64_t seed, uint64_t idx) {
     return sm64_mix(seed + (idx + 1ull) * SM64_GAMMA);
 }
 
-// Outputs idx .. idx+3: the states step by the constant gamma.
-__device__ __forceinline__ void rng64x4(uint64_t seed, uint64_t idx, uint64_t (&r)[4]) {
-    const uint64_t z = seed + (idx + 1ull) * SM64_GAMMA;
-    r[0] = sm64_mix(z);
-    r[1] = sm64_mix(z + SM64_GAMMA);
-    r[2] = sm64_mix(z + 2ull * SM64_GAMMA);
-    r[3] = sm64_mix(z + 3ull * SM64_GAMMA);
+// Random word of element g: lane g mod 2^lg of output g >> lg, lanes of
+// 64 >> lg bits from the low end (RoundPlan::rng_lg). The bits above the
+// lane belong to the next elements; every mode masks to the bits it reads.
+__device__ __forceinline__ uint64_t rng_elem(uint64_t seed, uint64_t g, int lg) {
+    const uint64_t w = rng64(seed, g >> lg);
+    return w >> (((uint32_t)g & ((1u << lg) - 1u)) << (6 - lg));
+}
+
+// Elements g .. g+3. With lanes of 16 or 8 bits and g a multiple of 4 the
+// four lanes sit in one output, with 32-bit lanes and g even in two: one
+// or two SplitMix64 mixes for four elements instead of four. lg is uniform
+// across the launch, and so is g's alignment when the stream offset is.
+__device__ __forceinline__ void rng_elem4(uint64_t seed, uint64_t g, int lg, uint64_t (&r)[4]) {
+    if (lg >= 2 && (g & 3u) == 0) {
+        const int lb = 6 - lg;  // log2 of the lane width
+        const uint64_t w = rng64(seed, g >> lg) >> (((uint32_t)g & ((1u << lg) - 1u)) << lb);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) r[q] = w >> (q << lb);
+    } else if (lg == 1 && (g & 1u) == 0) {
+        const uint64_t z = seed + ((g >> 1) + 1ull) * SM64_GAMMA;
+        const uint64_t w0 = sm64_mix(z), w1 = sm64_mix(z + SM64_GAMMA);
+        r[0] = w0;
+        r[1] = w0 >> 32;
+        r[2] = w1;
+        r[3] = w1 >> 32;
+    } else if (lg == 0) {
+        const uint64_t z = seed + (g + 1ull) * SM64_GAMMA;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) r[q] = sm64_mix(z + (uint64_t)q * SM64_GAMMA);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) r[q] = rng_elem(seed, g + q, lg);
+    }
 }
 
 // ---- round-to-odd word and RNE to m mantissa bits (the GEMM leaf) ----------
@@ -102,6 +130,9 @@ __device__ __forceinline__ U round_mantissa(U bits, int ro, int rmode, int len, 
     const U low = one_ro - U(1);
     const U trunc = bits & ~low;
     const U tail = bits & low;
+    // the random addend keeps the low min(len, W) bits of r (the reference
+    // casts it to its W-bit Bits type before shifting)
+    const U rm = lowmask<U>(len < W ? len : W);
     U res;
     switch (mode) {
     case LOFGB_RNE: res = bits + ((bits >> ro) & U(1)) + (one_ro >> 1) - U(1); break;
@@ -113,17 +144,17 @@ __device__ __forceinline__ U round_mantissa(U bits, int ro, int rmode, int len, 
     case LOFGB_RTA: res = trunc + (((bits >> (ro - 1)) & U(1)) << ro); break;
     case LOFGB_SR_A: {
         if (len <= 0) { res = bits; break; }
-        res = bits + shl_s<U>(U(r) & lowmask<U>(len), ro - len);
+        res = bits + shl_s<U>(U(r) & rm, ro - len);
         break;
     }
     case LOFGB_SR_B: {
-        const U add = (U(r) & lowmask<U>(len)) + U(1);
+        const U add = (U(r) & rm) + U(1);
         res = bits + (tail ? shl_s<U>(add, ro - len) : U(0));
         break;
     }
     case LOFGB_SR_C: {
         if (len == 0 || tail == 0) { res = bits; break; }
-        const U samp = U(r) & lowmask<U>(len);
+        const U samp = U(r) & rm;
         U add = shl_s<U>((samp >> 1) + (samp & U(1)), ro - len + 1);
         if (W <= 32) add = U(uint32_t(add));
         res = bits + add;
@@ -131,7 +162,7 @@ __device__ __forceinline__ U round_mantissa(U bits, int ro, int rmode, int len, 
     }
     case LOFGB_SR_D: {
         if (len <= 0) { res = bits; break; }
-        const U add = (U(r) & lowmask<U>(len)) + (U(r >> len) & U(1));
+        const U add = (U(r) & rm) + (U(r >> len) & U(1));
         res = bits + shl_s<U>(add, ro - len);
         break;
     }

@@ -68,7 +68,27 @@ struct RoundPlan {
     // tiny * 2^-len a normal float.
     int32_t sr_uni;
     uint32_t sr_mask, sr_shift;      // R' mask; (23 + len) << 23
+    // Random words: element g of a stream reads lane g mod 2^rng_lg (from the
+    // low end) of the SplitMix64 output number g >> rng_lg; lanes are
+    // 64 >> rng_lg bits wide, the narrowest of 8/16/32/64 that holds every
+    // bit the mode reads (rng_lanes_log2).
+    int32_t rng_lg;
 };
+
+// log2 of the random lanes per 64-bit word for (mode, stoch_len): SR-A, SR-B
+// and SR-C read the low len bits, SR-D len + 1 bits, Prob one bit, True SR
+// 53 bits; the deterministic modes read none.
+inline int rng_lanes_log2(int mode, int len) {
+    int need = 0;
+    switch (mode) {
+    case LOFGB_SR_A: case LOFGB_SR_B: case LOFGB_SR_C: need = len; break;
+    case LOFGB_SR_D: need = len + 1; break;
+    case LOFGB_PROB: need = 1; break;
+    case LOFGB_TRUE_SR: need = 64; break;
+    default: need = 0;
+    }
+    return need <= 8 ? 3 : need <= 16 ? 2 : need <= 32 ? 1 : 0;
+}
 
 // Host side.
 int validate_format(const lofgb_format* f, int src_mant_bits);

@@ -114,7 +114,7 @@ __device__ __forceinline__ float4 quant4(float4 x, const BlockScale& b, const Ro
         for (int i = 0; i < 4; ++i) w[i] = vr_uni_f32<EMODE, UNI>(__float_as_uint(q[i]), pe);
     } else {
         uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
-        if (stoch<EMODE>(pe.mode)) rng64x4(seed, e, r);
+        if (stoch<EMODE>(pe.mode)) rng_elem4(seed, e, pe.rng_lg, r);
 #pragma unroll
         for (int i = 0; i < 4; ++i) w[i] = __float_as_uint(q[i]);
         vr_format_f32x4<EMODE, FULL>(w, pe, r);

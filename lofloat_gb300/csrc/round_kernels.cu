@@ -63,7 +63,7 @@ __device__ __forceinline__ typename Src<W>::U process(typename Src<W>::U w, cons
             w = (U)__half_as_ushort(__float2half_rn(prod));
         }
     }
-    const uint64_t r = needs_rng<MODE>(p) ? rng64(seed, idx) : 0ull;
+    const uint64_t r = needs_rng<MODE>(p) ? rng_elem(seed, idx, p.rng_lg) : 0ull;
     if constexpr (FMT) return vr_format<MODE, W>(w, p, r);
     else return vr_mantissa<MODE, W>(w, p.d, p.mode, p.len, r);
 }
@@ -86,7 +86,7 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
             // SR-A by float arithmetic (RoundPlan::sr_uni)
             uint32_t w[4] = {vv.x, vv.y, vv.z, vv.w};
             uint64_t r[4];
-            rng64x4(seed, e0, r);
+            rng_elem4(seed, e0, p.rng_lg, r);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
@@ -104,7 +104,7 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
         } else if constexpr (W == 32 && FMT) {
             uint32_t w[4] = {vv.x, vv.y, vv.z, vv.w};
             uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
-            if (needs_rng<MODE>(p)) rng64x4(seed, e0, r);
+            if (needs_rng<MODE>(p)) rng_elem4(seed, e0, p.rng_lg, r);
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));

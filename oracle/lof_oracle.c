@@ -12,6 +12,10 @@
  * share one defined choice:
  *   - roundoff == 0 (nothing dropped): every mode returns the bits unchanged
  *     (the reference's RTA, SR-A and SR-D would shift by a negative count);
+ *   - the random addend of SR-A/B/C/D keeps the low min(stoch_len, W) bits
+ *     of the random word, W the width of the word being rounded (the
+ *     reference casts it to its W-bit Bits type; its shifts are undefined
+ *     once stoch_len reaches W);
  *   - stochastic modes with stoch_len > roundoff: the len-bit random addend
  *     is shifted right by (len - roundoff) instead of left by a negative
  *     count (src/lo_float.h:664, 751, 810, 832);
@@ -95,6 +99,24 @@ uint64_t orc_rng(uint64_t seed, uint64_t idx) {
     return z ^ (z >> 31);
 }
 
+int orc_rng_lanes_log2(int mode, int len) {
+    int need = 0;
+    switch (mode) {
+    case LOFGB_SR_A: case LOFGB_SR_B: case LOFGB_SR_C: need = len; break;
+    case LOFGB_SR_D: need = len + 1; break;
+    case LOFGB_PROB: need = 1; break;
+    case LOFGB_TRUE_SR: need = 64; break;
+    default: need = 0;
+    }
+    return need <= 8 ? 3 : need <= 16 ? 2 : need <= 32 ? 1 : 0;
+}
+
+uint64_t orc_rng_elem(uint64_t seed, uint64_t g, int lg) {
+    const uint64_t w = orc_rng(seed, g >> lg);
+    const int lane = (int)(g & ((1ull << lg) - 1ull));
+    return w >> (lane * (64 >> lg));
+}
+
 static inline double usamp_of(uint64_t r) { return (double)(r >> 11) * 0x1.0p-53; }
 
 /* ------------------------------------------------------------------------ */
@@ -106,6 +128,9 @@ static inline double usamp_of(uint64_t r) { return (double)(r >> 11) * 0x1.0p-53
 static uint64_t round_mantissa(uint64_t bits, int ro, int mode, int len, int pos,
                                uint64_t r, double u, int W) {
     const uint64_t M = wmask(W);
+    /* the random addend keeps the low min(len, W) bits of r: the reference
+     * casts it to its W-bit Bits type before shifting (:662, :748, :811, :833) */
+    const uint64_t RM = wmask(len < W ? len : W);
     if (ro <= 0) return bits;
     if (ro > W - 1) ro = W - 1;
     const uint64_t one_ro = 1ull << ro;
@@ -137,18 +162,18 @@ static uint64_t round_mantissa(uint64_t bits, int ro, int mode, int len, int pos
         break;
     case LOFGB_SR_A: { /* Stochastic_Round_A, :653-696 */
         if (len <= 0) { res = bits; break; }
-        uint64_t add = r & wmask(len);
+        uint64_t add = r & RM;
         res = bits + shl_s(add, ro - len);
         break;
     }
     case LOFGB_SR_B: { /* Stochastic_Round_B, :699-756 */
-        uint64_t add = (r & wmask(len)) + 1ull;
+        uint64_t add = (r & RM) + 1ull;
         res = bits + (tail > 0 ? shl_s(add, ro - len) : 0ull);
         break;
     }
     case LOFGB_SR_C: { /* Stochastic_Round_C, :758-815 */
         if (len == 0 || tail == 0) { res = bits; break; }
-        uint64_t samp = r & wmask(len);
+        uint64_t samp = r & RM;
         uint64_t top = (samp >> 1) + (samp & 1ull);
         uint64_t add = shl_s(top, ro - len + 1);
         if (W <= 32) add &= 0xFFFFFFFFull; /* computed as unsigned int */
@@ -157,7 +182,7 @@ static uint64_t round_mantissa(uint64_t bits, int ro, int mode, int len, int pos
     }
     case LOFGB_SR_D: { /* Stochastic_Round_D, :820-861 */
         if (len <= 0) { res = bits; break; }
-        uint64_t add = (r & wmask(len)) + ((r >> len) & 1ull);
+        uint64_t add = (r & RM) + ((r >> len) & 1ull);
         res = bits + shl_s(add, ro - len);
         break;
     }
@@ -469,10 +494,11 @@ int orc_round_f32(const float* in, float* out, int64_t n, const lofgb_format* f,
     if (st) return st;
     fconst_t c = make_consts(f);
     const int sc = scale != 1.0f;
+    const int lg = orc_rng_lanes_log2(mode, len);
 #pragma omp parallel for schedule(static) num_threads(nthr(nthreads))
     for (int64_t i = 0; i < n; ++i) {
         float v = sc ? scale * in[i] : in[i];
-        uint64_t rb = orc_rng(seed, offset + (uint64_t)i);
+        uint64_t rb = orc_rng_elem(seed, offset + (uint64_t)i, lg);
         out[i] = u2f((uint32_t)vr_fmt(f2u(v), &SRC_F32, &c, mode, len, rb, usamp_of(rb)));
     }
     return 0;
@@ -486,10 +512,11 @@ int orc_round_f64(const double* in, double* out, int64_t n, const lofgb_format* 
     if (st) return st;
     fconst_t c = make_consts(f);
     const int sc = scale != 1.0;
+    const int lg = orc_rng_lanes_log2(mode, len);
 #pragma omp parallel for schedule(static) num_threads(nthr(nthreads))
     for (int64_t i = 0; i < n; ++i) {
         double v = sc ? scale * in[i] : in[i];
-        uint64_t rb = orc_rng(seed, offset + (uint64_t)i);
+        uint64_t rb = orc_rng_elem(seed, offset + (uint64_t)i, lg);
         out[i] = u2d(vr_fmt(d2u(v), &SRC_F64, &c, mode, len, rb, usamp_of(rb)));
     }
     return 0;
@@ -504,10 +531,11 @@ int orc_round_f16(const uint16_t* in, uint16_t* out, int64_t n, const lofgb_form
     fconst_t c = make_consts(f);
     const float sh = h2f(f2h(scale));
     const int sc = sh != 1.0f;
+    const int lg = orc_rng_lanes_log2(mode, len);
 #pragma omp parallel for schedule(static) num_threads(nthr(nthreads))
     for (int64_t i = 0; i < n; ++i) {
         uint16_t v = sc ? f2h(sh * h2f(in[i])) : in[i];
-        uint64_t rb = orc_rng(seed, offset + (uint64_t)i);
+        uint64_t rb = orc_rng_elem(seed, offset + (uint64_t)i, lg);
         out[i] = (uint16_t)vr_fmt(v, &SRC_F16, &c, mode, len, rb, usamp_of(rb));
     }
     return 0;
@@ -520,10 +548,11 @@ int orc_round_mantissa_f32(const float* in, float* out, int64_t n, int mbits, in
     if (!st) st = validate_mode(mode, len);
     if (st) return st;
     const int sc = scale != 1.0f;
+    const int lg = orc_rng_lanes_log2(mode, len);
 #pragma omp parallel for schedule(static) num_threads(nthr(nthreads))
     for (int64_t i = 0; i < n; ++i) {
         float v = sc ? scale * in[i] : in[i];
-        uint64_t rb = orc_rng(seed, offset + (uint64_t)i);
+        uint64_t rb = orc_rng_elem(seed, offset + (uint64_t)i, lg);
         out[i] = u2f((uint32_t)vr_mant(f2u(v), &SRC_F32, mbits, mode, len, rb, usamp_of(rb)));
     }
     return 0;
@@ -536,10 +565,11 @@ int orc_round_mantissa_f64(const double* in, double* out, int64_t n, int mbits,
     if (!st) st = validate_mode(mode, len);
     if (st) return st;
     const int sc = scale != 1.0;
+    const int lg = orc_rng_lanes_log2(mode, len);
 #pragma omp parallel for schedule(static) num_threads(nthr(nthreads))
     for (int64_t i = 0; i < n; ++i) {
         double v = sc ? scale * in[i] : in[i];
-        uint64_t rb = orc_rng(seed, offset + (uint64_t)i);
+        uint64_t rb = orc_rng_elem(seed, offset + (uint64_t)i, lg);
         out[i] = u2d(vr_mant(d2u(v), &SRC_F64, mbits, mode, len, rb, usamp_of(rb)));
     }
     return 0;
@@ -553,10 +583,11 @@ int orc_round_mantissa_f16(const uint16_t* in, uint16_t* out, int64_t n, int mbi
     if (st) return st;
     const float sh = h2f(f2h(scale));
     const int sc = sh != 1.0f;
+    const int lg = orc_rng_lanes_log2(mode, len);
 #pragma omp parallel for schedule(static) num_threads(nthr(nthreads))
     for (int64_t i = 0; i < n; ++i) {
         uint16_t v = sc ? f2h(sh * h2f(in[i])) : in[i];
-        uint64_t rb = orc_rng(seed, offset + (uint64_t)i);
+        uint64_t rb = orc_rng_elem(seed, offset + (uint64_t)i, lg);
         out[i] = (uint16_t)vr_mant(v, &SRC_F16, mbits, mode, len, rb, usamp_of(rb));
     }
     return 0;
@@ -585,6 +616,7 @@ int orc_mx_round_f32(const float* in, float* out, int64_t n, int block,
     const float pmn = ldexpf(1.0f, me) * (2.0f - ldexpf(1.0f, -ef->mantissa_bits));
     const float inv = 1.0f / pmn;
     const int64_t nb = (n + block - 1) / block;
+    const int lg = orc_rng_lanes_log2(mode, len);
 #pragma omp parallel for schedule(static) num_threads(nthr(nthreads))
     for (int64_t b = 0; b < nb; ++b) {
         const int64_t b0 = b * block;
@@ -601,7 +633,7 @@ int orc_mx_round_f32(const float* in, float* out, int64_t n, int block,
         }
         for (int64_t i = 0; i < cnt; ++i) {
             const float q = in[b0 + i] / scale;
-            uint64_t rb = orc_rng(seed, offset + (uint64_t)(b0 + i));
+            uint64_t rb = orc_rng_elem(seed, offset + (uint64_t)(b0 + i), lg);
             const float qr =
                 u2f((uint32_t)vr_fmt(f2u(q), &SRC_F32, &ce, mode, len, rb, usamp_of(rb)));
             out[b0 + i] = qr * scale;
@@ -1031,8 +1063,9 @@ int orc_encode_f32(uint8_t* dst, const float* src, int64_t count, const lofgb_co
     if (!f || f->fmt.bitwidth < 1 || f->fmt.bitwidth > 16) return LOFGB_ERR_FORMAT;
     const int n = f->fmt.bitwidth;
     memset(dst, 0, (size_t)orc_packed_size(n, count));
+    const int lg = orc_rng_lanes_log2(mode, len);
     for (int64_t i = 0; i < count; ++i) {
-        const uint64_t rb = orc_rng(seed, offset + (uint64_t)i);
+        const uint64_t rb = orc_rng_elem(seed, offset + (uint64_t)i, lg);
         const uint32_t code = orc_codec_encode_rep(src[i], f, mode, sat, len, rb, usamp_of(rb));
         const int64_t b0 = code_bit(i, n, reverse);
         for (int b = 0; b < n; ++b)

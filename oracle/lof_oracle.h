@@ -25,6 +25,14 @@ extern "C" {
  * idx-th output of a SplitMix64 stream whose state starts at `seed`. */
 uint64_t orc_rng(uint64_t seed, uint64_t idx);
 
+/* Per-element random words: element g reads lane g mod 2^lg (from the low
+ * end) of output g >> lg, lanes 64 >> lg bits wide; lg is the log2 of the
+ * lanes per output for (mode, stoch_len), the narrowest of 8/16/32/64 bits
+ * covering what the mode reads (SR-A/B/C: len, SR-D: len + 1, Prob: 1,
+ * True SR: 53). The MX block-scale stream keeps one output per block. */
+int orc_rng_lanes_log2(int mode, int len);
+uint64_t orc_rng_elem(uint64_t seed, uint64_t g, int lg);
+
 /* Scalar cores. `rbits` is the random word for stochastic modes; `usamp` is
  * the uniform [0,1) sample used by True_StochasticRounding (pass a negative
  * value to derive it from rbits as (rbits >> 11) * 2^-53). */

@@ -58,6 +58,10 @@ def lib():
         P = C.POINTER(Format)
         L.orc_rng.restype = u64
         L.orc_rng.argtypes = [u64, u64]
+        L.orc_rng_elem.restype = u64
+        L.orc_rng_elem.argtypes = [u64, u64, C.c_int]
+        L.orc_rng_lanes_log2.restype = C.c_int
+        L.orc_rng_lanes_log2.argtypes = [C.c_int, C.c_int]
         for name, sc in (("orc_round_f32", f32), ("orc_round_f64", f64), ("orc_round_f16", f32)):
             getattr(L, name).argtypes = [vp, vp, i64, P, i32, i32, sc, u64, u64, i32]
         for name, sc in (("orc_round_mantissa_f32", f32), ("orc_round_mantissa_f64", f64),
@@ -129,6 +133,15 @@ _DT = {np.dtype(np.float32): "f32", np.dtype(np.float64): "f64", np.dtype(np.uin
 
 def rng(seed: int, idx: int) -> int:
     return lib().orc_rng(seed, idx)
+
+
+def rng_lanes_log2(mode: int, stoch_len: int) -> int:
+    return lib().orc_rng_lanes_log2(mode, stoch_len)
+
+
+def rng_elem(seed: int, g: int, lg: int) -> int:
+    """Random word of element g (lane g mod 2^lg of output g >> lg)."""
+    return lib().orc_rng_elem(seed, g, lg)
 
 
 def round(x: np.ndarray, f: Format, mode: int, stoch_len: int = 0, scale: float = 1.0,

@@ -41,9 +41,10 @@ def test_round_beyond_2_31(big, mode, ln):
     del y
     f = O.fmt(8, 3, 8)
     # stochastic modes draw R from (seed, offset + global index): the oracle
-    # rounds each sampled element with its own index
+    # rounds each sampled element with its own index's random lane
     if mode == 3:
-        rbits = np.array([O.rng(5, 7 + int(i)) for i in idx], np.uint64)
+        lgl = O.rng_lanes_log2(mode, ln)
+        rbits = np.array([O.rng_elem(5, 7 + int(i), lgl) for i in idx], np.uint64)
         want = O.round_bits(xs, f, mode, ln, rbits=rbits)
     else:
         want = O.round(xs, f, mode, ln)
