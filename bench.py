@@ -545,26 +545,70 @@ def run_ours(args, world, rank, local):
     elapsed = t0.elapsed_time(t1) / 1e3
     per_launch = statistics.mean(s.elapsed_time(e) for s, e in launch_ms) / 1e3
 
-    # end to end through the public API with host buffers
+    # end to end through the public API with host buffers: every step copies
+    # its input from pinned host memory, rounds it to the three formats and
+    # copies the three results back to pinned host memory. Consecutive steps
+    # overlap: input copies run on their own stream into two device buffers,
+    # result copies alternate over two streams (two copy engines device to
+    # host), the roundings stay on the timed stream; events order the reuse
+    # of every device buffer.
     xh = x_host.pin_memory()
     yh = [torch.empty_like(xh).pin_memory() for _ in efs]
+    s_in = torch.cuda.Stream(dev)
+    s_out = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+    xd = [torch.empty(xh.shape, dtype=xh.dtype, device=dev) for _ in range(2)]
+    yd = [torch.empty(xh.shape, dtype=xh.dtype, device=dev) for _ in efs]
+    e2e = {"k": 0, "out_done": [None] * len(efs), "used": [None, None]}
 
     def e2e_step():
-        xd = xh.to(dev, non_blocking=True)
+        k = e2e["k"]
+        e2e["k"] += 1
+        buf = xd[k % 2]
+        with torch.cuda.stream(s_in):
+            if e2e["used"][k % 2] is not None:
+                s_in.wait_event(e2e["used"][k % 2])
+            buf.copy_(xh, non_blocking=True)
+            ev_in = torch.cuda.Event()
+            ev_in.record(s_in)
+        stream.wait_event(ev_in)
         for i, ef in enumerate(efs):
-            yd = lg.virtual_mx_round(xd, MX_BLOCK, ef, e8)
-            yh[i].copy_(yd, non_blocking=True)
+            if e2e["out_done"][i] is not None:
+                stream.wait_event(e2e["out_done"][i])
+            lg.virtual_mx_round(buf, MX_BLOCK, ef, e8, out=yd[i])
+            ev_c = torch.cuda.Event()
+            ev_c.record(stream)
+            so = s_out[i % 2]
+            so.wait_event(ev_c)
+            with torch.cuda.stream(so):
+                yh[i].copy_(yd[i], non_blocking=True)
+                ev_o = torch.cuda.Event()
+                ev_o.record(so)
+            e2e["out_done"][i] = ev_o
+        ev_u = torch.cuda.Event()
+        ev_u.record(stream)
+        e2e["used"][k % 2] = ev_u
+
+    def e2e_join():
+        for ev in e2e["out_done"]:
+            stream.wait_event(ev)
 
     for _ in range(2):
         e2e_step()
+    e2e_join()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2e_steps = max(3, min(args.steps, 10))
     e0.record(stream)
+    s_in.wait_event(e0)
     for _ in range(e2e_steps):
         e2e_step()
+    e2e_join()
     e1.record(stream)
     torch.cuda.synchronize()
+    # the host copies hold the device results (checked outside the timed region)
+    for i, ef in enumerate(efs):
+        if not torch.equal(yh[i].to(dev), lg.virtual_mx_round(xd[0], MX_BLOCK, ef, e8)):
+            raise RuntimeError(f"end-to-end result {i} differs from the device result")
     e2e_s = e0.elapsed_time(e1) / 1e3
     clk = clocks.stop()
 

@@ -189,10 +189,11 @@ int make_round_plan(RoundPlan* p, const lofgb_format* f, int src_bits, int mode,
     if (uni_ok && p->grid != 0) p->uni = p->grid;
     // tiny * 2^-len normal: (to_min - m) - len >= -126
     p->sr_uni = 0;
-    if (uni_ok && mode == LOFGB_SR_A && len <= p->d && len <= 24 && gexp - len >= -126) {
+    if (uni_ok && mode == LOFGB_SR_A && len <= p->d && len <= 23 && gexp - len >= -126 &&
+        p->grid_c > 0.0f) {
         p->sr_uni = 1;
         p->sr_mask = len >= 32 ? 0xFFFFFFFFu : ((1u << len) - 1u);
-        p->sr_shift = (uint32_t)(23 + len) << 23;
+        p->sr_shift = (uint32_t)len << 23;
     }
     return LOFGB_OK;
 }

@@ -23,7 +23,8 @@
 //               3 stages, 128-byte swizzle, one mbarrier per stage;
 //   warp 1      TMEM owner and MMA issuer (one elected lane):
 //               tcgen05.mma.cta_group::1.kind::f16, M=128 N=128 K=16,
-//               chunk sums double-buffered in 2 x 128 TMEM columns;
+//               chunk sums in four 128-column TMEM buffers (all 512
+//               columns), so the MMAs run up to three chunks ahead;
 //   warps 2..9  epilogue (two per TMEM lane quarter): tcgen05.ld the chunk
 //               sum of its lane quarter and one 64-column half, in four
 //               16-column loads pipelined with the folds (one piece loads
@@ -58,7 +59,9 @@ constexpr int EPI_WARPS = 8;                   // two per TMEM lane quarter
 constexpr int EPI_COLS = TBN * 4 / EPI_WARPS;  // accumulator columns per epilogue thread
 constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
 static_assert(EPI_COLS == 64, "the epilogue folds four pipelined 16-column pieces");
-constexpr int TMEM_COLS = 2 * TBN;             // two chunk buffers
+constexpr int NBUF = 4;                        // TMEM chunk buffers (all 512 columns)
+constexpr int TMEM_COLS = NBUF * TBN;
+static_assert((NBUF & (NBUF - 1)) == 0 && TMEM_COLS <= 512, "TMEM chunk buffers");
 constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + STAGES * STAGE_BYTES + 256 /*barriers*/;
 constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;
 
@@ -212,6 +215,20 @@ __device__ __forceinline__ void tmem_ld_wait16(uint32_t (&r)[16]) {
                  : "memory");
 }
 
+// Scheduling pin for the pipelined epilogue: an empty asm that takes 16
+// accumulators as in/out operands. Placed after a TMEM load it keeps the fold
+// of those accumulators after the load is issued; placed before a TMEM wait it
+// keeps their fold ahead of the wait. Emits no instruction.
+template <int OFF, int N>
+__device__ __forceinline__ void pin16(float (&a)[N]) {
+    static_assert(OFF + 16 <= N, "pin16 range");
+    asm volatile(""
+                 : "+f"(a[OFF + 0]), "+f"(a[OFF + 1]), "+f"(a[OFF + 2]), "+f"(a[OFF + 3]),
+                   "+f"(a[OFF + 4]), "+f"(a[OFF + 5]), "+f"(a[OFF + 6]), "+f"(a[OFF + 7]),
+                   "+f"(a[OFF + 8]), "+f"(a[OFF + 9]), "+f"(a[OFF + 10]), "+f"(a[OFF + 11]),
+                   "+f"(a[OFF + 12]), "+f"(a[OFF + 13]), "+f"(a[OFF + 14]), "+f"(a[OFF + 15]));
+}
+
 // acc = RNE_m(rto(acc + s)) with directed adds, as the per-MAC leaf does with
 // directed FMAs (src/cutlass_gemms.cuh:73-88, 162-163); rto_word / rne_word
 // are that leaf's round-to-odd and RNE steps.
@@ -341,8 +358,8 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                                                ~uintptr_t(1023));
     uint8_t* tiles = smem;
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
-    // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2], drain
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
+    // bars: full[STAGES], empty[STAGES], tfull[NBUF], tempty[NBUF], drain
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 2 * NBUF + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5;
@@ -350,15 +367,15 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
     const uint32_t bar_full = smem_u32(bars);
     const uint32_t bar_empty = smem_u32(bars + STAGES);
     const uint32_t bar_tfull = smem_u32(bars + 2 * STAGES);
-    const uint32_t bar_tempty = smem_u32(bars + 2 * STAGES + 2);
-    const uint32_t bar_drain = smem_u32(bars + 2 * STAGES + 4);
+    const uint32_t bar_tempty = smem_u32(bars + 2 * STAGES + NBUF);
+    const uint32_t bar_drain = smem_u32(bars + 2 * STAGES + 2 * NBUF);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(bar_full + 8 * s, 1);
             mbar_init(bar_empty + 8 * s, 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < NBUF; ++b) {
             mbar_init(bar_tfull + 8 * b, 1);
             mbar_init(bar_tempty + 8 * b, EPI_WARPS * 32);
         }
@@ -423,9 +440,9 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                     const uint32_t base = smem_u32(tiles + s * STAGE_BYTES);
                     for (int j = 0; j < SK / 16; ++j, ++kk16) {
                         const int pos = kk16 % ti.chunk16;
-                        const uint32_t buf = cg & 1u;
+                        const uint32_t buf = cg % NBUF;
                         if (pos == 0) {
-                            if (!mbar_wait(bar_tempty + 8 * buf, ((cg >> 1) & 1u) ^ 1u, abort_flag, status)) { ok = false; break; }
+                            if (!mbar_wait(bar_tempty + 8 * buf, ((cg / NBUF) & 1u) ^ 1u, abort_flag, status)) { ok = false; break; }
                             tc_fence_after();
                         }
                         const uint32_t d = tmem_base + buf * TBN;
@@ -460,7 +477,7 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
         // every lane waits; the warp goes on only when all lanes saw the phase
         // complete, reconverged for the .sync.aligned TMEM loads
         auto wait_full = [&](uint32_t g) -> bool {
-            const bool got = mbar_wait(bar_tfull + 8 * (g & 1u), (g >> 1) & 1u, abort_flag, status);
+            const bool got = mbar_wait(bar_tfull + 8 * (g % NBUF), (g / NBUF) & 1u, abort_flag, status);
             if (!__all_sync(0xFFFFFFFFu, got)) return false;
             __syncwarp();
             tc_fence_after();
@@ -492,28 +509,36 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
             // folded, and piece 0 of chunk c+1 loads during piece 3 of chunk c.
             uint32_t ra[16], rb[16];
             if (!wait_full(cg)) { ok = false; break; }
-            tmem_ld16(lane_base + (cg & 1u) * TBN, ra);
+            tmem_ld16(lane_base + (cg % NBUF) * TBN, ra);
             tmem_ld_wait16(ra);
             for (int c = 0; c < nchunks; ++c) {
-                const uint32_t col = lane_base + (cg & 1u) * TBN;
+                const uint32_t col = lane_base + (cg % NBUF) * TBN;
                 tmem_ld16(col + 16, rb);
+                pin16<0>(acc);
                 fold16(0, ra);
+                pin16<0>(acc);
                 tmem_ld_wait16(rb);
                 tmem_ld16(col + 32, ra);
+                pin16<16>(acc);
                 fold16(16, rb);
+                pin16<16>(acc);
                 tmem_ld_wait16(ra);
                 tmem_ld16(col + 48, rb);
+                pin16<32>(acc);
                 fold16(32, ra);
+                pin16<32>(acc);
                 tmem_ld_wait16(rb);
                 tc_fence_before();
-                mbar_arrive(bar_tempty + 8 * (cg & 1u));   // all of chunk c is in registers
+                mbar_arrive(bar_tempty + 8 * (cg % NBUF));   // all of chunk c is in registers
                 ++cg;
                 const bool more = c + 1 < nchunks;
                 if (more) {
                     if (!wait_full(cg)) { ok = false; break; }
-                    tmem_ld16(lane_base + (cg & 1u) * TBN, ra);
+                    tmem_ld16(lane_base + (cg % NBUF) * TBN, ra);
                 }
+                pin16<48>(acc);
                 fold16(48, rb);
+                pin16<48>(acc);
                 if (more) tmem_ld_wait16(ra);
             }
             if (!ok) break;

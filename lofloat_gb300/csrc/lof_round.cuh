@@ -55,11 +55,16 @@ __device__ __forceinline__ uint64_t rng_elem(uint64_t seed, uint64_t g, int lg) 
 // or two SplitMix64 mixes for four elements instead of four. lg is uniform
 // across the launch, and so is g's alignment when the stream offset is.
 __device__ __forceinline__ void rng_elem4(uint64_t seed, uint64_t g, int lg, uint64_t (&r)[4]) {
-    if (lg >= 2 && (g & 3u) == 0) {
-        const int lb = 6 - lg;  // log2 of the lane width
-        const uint64_t w = rng64(seed, g >> lg) >> (((uint32_t)g & ((1u << lg) - 1u)) << lb);
+    if (lg == 3 && (g & 3u) == 0) {
+        // four 8-bit lanes: the low or the high half of the output
+        const uint64_t w = rng64(seed, g >> 3);
+        const uint32_t h = (g & 4u) ? (uint32_t)(w >> 32) : (uint32_t)w;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) r[q] = w >> (q << lb);
+        for (int q = 0; q < 4; ++q) r[q] = h >> (8 * q);
+    } else if (lg == 2 && (g & 3u) == 0) {
+        const uint64_t w = rng64(seed, g >> 2);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) r[q] = w >> (16 * q);
     } else if (lg == 1 && (g & 1u) == 0) {
         const uint64_t z = seed + ((g >> 1) + 1ull) * SM64_GAMMA;
         const uint64_t w0 = sm64_mix(z), w1 = sm64_mix(z + SM64_GAMMA);
@@ -426,16 +431,23 @@ __device__ __forceinline__ uint32_t vr_uni_f32(uint32_t x, const RoundPlan& p) {
 }
 
 // virtual_round(x, params, {SR-A, len}) of an f32 word by float arithmetic
-// (RoundPlan::sr_uni); r is the element's random word.
-__device__ __forceinline__ uint32_t vr_uni_sra_f32(uint32_t x, const RoundPlan& p, uint64_t r) {
+// (RoundPlan::sr_uni); r holds the element's random bits in its low len bits.
+// The noise R' * spacing * 2^-len is built exactly as F - E with
+// E = 2^(e_C - len) (e_C the exponent of C) and F = E with R' in its low
+// mantissa bits (R' < 2^len, len <= d <= 23, so F = E + R' * ulp(E)). The
+// truncation of y to the target's spacing at y is y's word with the d low bits
+// cleared where y is at or above the target's smallest normal (every such y
+// then has spacing 2^(e_y - m), or overflows), and fadd_rz(y, Csub) - Csub with
+// Csub = 2^(to_min + d) (ulp = tiny) below it.
+__device__ __forceinline__ uint32_t vr_uni_sra_f32(uint32_t x, const RoundPlan& p, uint32_t r) {
     const uint32_t mag = x & 0x7FFFFFFFu;
     const uint32_t cbx = min(max(x & 0x7F800000u, p.uni_lo), p.uni_hi) + p.uni_d;
-    const float noise = __fmul_rn(__uint2float_rn((uint32_t)r & p.sr_mask),
-                                  __uint_as_float(cbx - p.sr_shift));
+    const uint32_t eb = cbx - p.sr_shift;
+    const float noise = __fsub_rn(__uint_as_float((r & p.sr_mask) | eb), __uint_as_float(eb));
     const float y = __fadd_rz(__uint_as_float(mag), noise);
-    const uint32_t cby = min(max(__float_as_uint(y) & 0x7F800000u, p.uni_lo), p.uni_hi) + p.uni_d;
-    const float cy = __uint_as_float(cby);
-    const uint32_t v = __float_as_uint(__fsub_rn(__fadd_rz(y, cy), cy));
+    const uint32_t yb = __float_as_uint(y);
+    const uint32_t vs = __float_as_uint(__fsub_rn(__fadd_rz(y, p.grid_c), p.grid_c));
+    const uint32_t v = yb >= (uint32_t)p.norm_thr ? (yb & (uint32_t)p.keep_mask) : vs;
     uint32_t res = v | (x & 0x80000000u);
     res = v >= (uint32_t)p.ovf_thr ? ((x & p.sat_and) | p.sat_or) : res;
     res = mag < (uint32_t)p.tiny_thr ? (x & 0x80000000u) : res;

@@ -59,15 +59,15 @@ struct RoundPlan {
     // Stochastic rounding A by float arithmetic (sr_uni): with the same C,
     // the noise R' * spacing * 2^-len (R' = R & sr_mask, spacing = ulp(C)) is
     // a multiple of ulp(|x|) when len <= d; y = fadd_rz(|x|, noise) then
-    // truncated to the spacing at y (fadd_rz(y, C_y) - C_y) is the reference's
-    // integer SR-A — within a binade the bit-pattern sum is the value sum, and
-    // a carry into the next binade truncates to 2^(e+1) either way; rounding y
-    // toward zero never crosses a multiple of the spacing. Magnitudes below
-    // tiny flush to +-0 (the stochastic modes' tiny branch). Valid when the
-    // uni conditions hold without a float grid and len <= min(d, 24) with
-    // tiny * 2^-len a normal float.
+    // truncated to the target's spacing at y is the reference's integer
+    // SR-A — within a binade the bit-pattern sum is the value sum, and a carry
+    // into the next binade truncates to 2^(e+1) either way; rounding y toward
+    // zero never crosses a multiple of the spacing. Magnitudes below tiny
+    // flush to +-0 (the stochastic modes' tiny branch). Valid when the uni
+    // conditions hold, the float grid constant grid_c exists, and
+    // len <= min(d, 24) with tiny * 2^-len a normal float.
     int32_t sr_uni;
-    uint32_t sr_mask, sr_shift;      // R' mask; (23 + len) << 23
+    uint32_t sr_mask, sr_shift;      // R' mask; len << 23
     // Random words: element g of a stream reads lane g mod 2^rng_lg (from the
     // low end) of the SplitMix64 output number g >> rng_lg; lanes are
     // 64 >> rng_lg bits wide, the narrowest of 8/16/32/64 that holds every
