@@ -161,3 +161,31 @@ def test_python_api_and_errors():
         lg.lof_decode(packed[:10], 1000, e4m3)
     with pytest.raises(RuntimeError):
         lg.lof_encode(x.cpu(), e4m3)
+
+
+@pytest.mark.parametrize("bits", [4, 8, 16])
+def test_direct_path_and_unaligned_fallback(bits):
+    """4-, 8- and 16-bit codes take the one-float4-per-thread kernels when the
+    buffers allow 16-byte loads; buffers that are only 4-byte aligned take the
+    staged kernels. Both write the oracle's bytes."""
+    f = O.codec_p3109(bits, max(1, bits // 2))
+    n = 70_003
+    x = _wide(n, bits)
+    want = O.encode(x, f, reverse=1)
+    nb = lg.packed_size(bits, n)
+    big = torch.from_numpy(np.concatenate([np.zeros(1, np.float32), x])).cuda()
+    for shift in (0, 1):                              # float offset: 16-byte or 4-byte aligned
+        xs = big[1:] if shift else torch.from_numpy(x).cuda()
+        out = torch.zeros(nb + 8, dtype=torch.uint8, device="cuda")
+        dptr = out.data_ptr() + 4 * shift              # packed output 4-byte aligned only
+        st = _native.lib().lofgb_encode_f32(dptr, xs.data_ptr(), n, C.byref(_native_fmt(f)), 0, 0, 0,
+                                            1, 0, 0, None)
+        assert st == 0
+        got = out.cpu().numpy()[4 * shift:4 * shift + nb]
+        assert np.array_equal(got, want), (shift, int(np.sum(got != want)))
+        assert not out.cpu().numpy()[4 * shift + nb:].any()   # nothing past the packed size
+        dec = torch.zeros(n + 4, dtype=torch.float32, device="cuda")
+        st = _native.lib().lofgb_decode_f32(dec.data_ptr() + 4 * shift, dptr, n,
+                                            C.byref(_native_fmt(f)), 1, None)
+        assert st == 0
+        assert same_bits(dec.cpu().numpy()[shift:shift + n], O.decode(want, n, f, 1))
