@@ -257,7 +257,9 @@ def secondary(torch, lg, dev, peaks):
         fn = lambda: lg.virtual_round(xg, e4m3, round_mode=mode, stoch_len=ln, seed=1, offset=0, out=yg)  # noqa: E731
         for _ in range(5):
             fn()
-        ms = time_events(torch, fn, 20, stream)
+        # 20 back-to-back launches between two events (per-launch events would
+        # also count the host's call overhead against a ~25 us kernel)
+        ms = [m / 20 for m in time_events(torch, lambda: [fn() for _ in range(20)], 5, stream)]
         gbs = C1_N * 8 / (statistics.median(ms) * 1e-3) / 1e9
         out[f"round_2^24_e4m3_{name}_GBs"] = round(gbs, 1)
         out[f"round_2^24_e4m3_{name}_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)

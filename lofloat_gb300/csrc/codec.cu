@@ -45,12 +45,13 @@ struct CodecArg {
     uint32_t uni_lo, uni_hi, uni_d;
     uint32_t min_norm_bits;   // FP32 bits of the smallest target normal, 2^(1-bias)
     uint32_t code_off;        // normal code = (bits >> (23 - m)) - code_off
-    float sub_scale;          // subnormal code = value * 2^(bias + m - 1)
+    float sub_c;              // 2^23 * tiny: subnormal code = bits(v + sub_c) - bits(sub_c)
     uint32_t max_finite, ovf_code, inf_code, neg_zero_code, neg_code, sign_mask;
     // Fast decode: every finite value is a normal FP32 number or an exact
     // FP32 subnormal, so the bits are built directly.
     int dec_fast;
     float tiny;               // 2^(1 - bias - m)
+    float sub_c_dec;          // 2^23 * tiny
     uint32_t code_off_dec;    // normal value bits = (mag << (23 - m)) - code_off_dec
 };
 
@@ -154,7 +155,13 @@ __device__ __forceinline__ uint32_t codec_encode(float from, const CodecArg& a, 
 // FP32's range (CodecArg::enc_fast): the same code as codec_encode,
 // branch-free. The float grid reproduces RoundMantissa's RNE on the normal
 // branch and on the target-subnormal branch alike (including the reference's
-// shift > 24 table, 0 for RNE).
+// shift > 24 table, 0 for RNE). A target-subnormal v is a multiple of tiny
+// below 2^to_min, so v + 2^23 tiny is exact and its word minus that of
+// 2^23 tiny is v / tiny, the code. Every code above the largest finite one
+// becomes ovf_code, which is that code or the next (infinity), so the
+// overflow test is a min. SPECIAL = false leaves out the infinity and NaN
+// inputs (the caller has checked that its warp holds none).
+template <bool SPECIAL>
 __device__ __forceinline__ uint32_t codec_encode_fast(float from, const CodecArg& a) {
     const uint32_t fb = __float_as_uint(from);
     const bool neg = (fb >> 31) != 0;
@@ -165,11 +172,11 @@ __device__ __forceinline__ uint32_t codec_encode_fast(float from, const CodecArg
     const float v = __fsub_rn(__fadd_rn(ax, c), c);
     const uint32_t vb = __float_as_uint(v);
     uint32_t code = vb >= a.min_norm_bits ? (vb >> (23 - a.m)) - a.code_off
-                                          : __float2uint_rz(__fmul_rn(v, a.sub_scale));
-    code = code > a.max_finite ? a.ovf_code : code;
-    code = mb == 0x7F800000u ? a.inf_code : code;
+                                          : __float_as_uint(__fadd_rn(v, a.sub_c)) - __float_as_uint(a.sub_c);
+    code = min(code, a.ovf_code);
+    if (SPECIAL) code = mb == 0x7F800000u ? a.inf_code : code;
     code = (neg && a.is_signed) ? (code == 0u ? a.neg_zero_code : (code | a.sign_mask)) : code;
-    code = mb > 0x7F800000u ? a.qnan : code;
+    if (SPECIAL) code = mb > 0x7F800000u ? a.qnan : code;
     return (neg && !a.is_signed) ? a.neg_code : code;
 }
 
@@ -179,7 +186,9 @@ __device__ __forceinline__ float codec_decode_fast(uint32_t rep, const CodecArg&
     const uint32_t sbit = a.is_signed ? (rep >> (a.n - 1)) & 1u : 0u;
     const uint32_t mag = rep & ~a.sign_mask;
     const uint32_t e = mag >> a.m;
-    const float sub = __fmul_rn(__uint2float_rn(mag), a.tiny);
+    // mag * tiny for a subnormal code (mag < 2^m): the word of 2^23 tiny plus
+    // mag is 2^23 tiny + mag * tiny exactly; subtracting 2^23 tiny is exact
+    const float sub = __fsub_rn(__uint_as_float(__float_as_uint(a.sub_c_dec) + mag), a.sub_c_dec);
     const uint32_t nb = (mag << (23 - a.m)) - a.code_off_dec;
     uint32_t vb = e == 0 ? __float_as_uint(sub) : nb;
     vb = c_is_nan(rep, a) ? 0x7FC00000u : (vb | (sbit << 31));
@@ -257,7 +266,7 @@ encode_kernel(const float* __restrict__ src, uint32_t* __restrict__ dst, int64_t
             int fill = 0, widx = 0;
 #pragma unroll
             for (int s = 0; s < 32; ++s) {
-                const uint32_t code = codec_encode_fast(xin[slot_element<N, REV>(s)], a) &
+                const uint32_t code = codec_encode_fast<true>(xin[slot_element<N, REV>(s)], a) &
                                       ((1u << N) - 1u);
                 acc |= (uint64_t)code << fill;
                 fill += N;
@@ -301,6 +310,150 @@ encode_kernel(const float* __restrict__ src, uint32_t* __restrict__ dst, int64_t
             }
         }
         __syncwarp();
+    }
+}
+
+// ---- direct kernels for 4-, 8- and 16-bit codes -----------------------------
+// With N in {4, 8, 16} the codes of four consecutive values fill exactly
+// 4N bits of the stream (two bytes, four bytes, eight bytes), so a thread
+// turns one float4 into one 16/32/64-bit store and back, with no staging:
+// for N = 8 and 16 a group holds one code (the group order changes
+// nothing); for N = 4 a byte holds two codes, low nibble first (forward) or
+// high nibble first (reverse). The last count % 4 values (and the padding
+// codes of +0.0 up to the group boundary, as the staged kernel writes them)
+// go through one thread that writes only the bytes below the packed size.
+template <int N>
+struct Chunk;
+template <> struct Chunk<4> { using T = uint16_t; };
+template <> struct Chunk<8> { using T = uint32_t; };
+template <> struct Chunk<16> { using T = uint2; };
+
+template <int N, bool REV>
+__device__ __forceinline__ uint64_t pack4(const uint32_t (&c)[4]) {
+    constexpr uint32_t M = (1u << N) - 1u;
+    if (N == 4 && REV)
+        return (uint64_t)((c[1] & M) | (c[0] & M) << 4 | (c[3] & M) << 8 | (c[2] & M) << 12);
+    return (uint64_t)(c[0] & M) | (uint64_t)(c[1] & M) << N | (uint64_t)(c[2] & M) << (2 * N) |
+           (uint64_t)(c[3] & M) << (3 * N);
+}
+
+template <int N, bool REV>
+__device__ __forceinline__ void unpack4(uint64_t w, uint32_t (&c)[4]) {
+    constexpr uint32_t M = (1u << N) - 1u;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) c[q] = (uint32_t)(w >> (q * N)) & M;
+    if (N == 4 && REV) {
+        const uint32_t t0 = c[0], t2 = c[2];
+        c[0] = c[1]; c[1] = t0; c[2] = c[3]; c[3] = t2;
+    }
+}
+
+template <int N, int MODE, int FAST>
+__device__ __forceinline__ void encode4(const float (&x)[4], uint32_t (&c)[4], const CodecArg& a,
+                                        uint64_t e) {
+    if constexpr (FAST != 0) {
+        // infinities and NaNs are rare: their checks run only in warps that hold one
+        bool sp = false;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) sp |= (__float_as_uint(x[q]) & 0x7FFFFFFFu) >= 0x7F800000u;
+        if (__any_sync(__activemask(), sp)) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) c[q] = codec_encode_fast<true>(x[q], a);
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) c[q] = codec_encode_fast<false>(x[q], a);
+        }
+    } else {
+        uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
+        if (mode_is_stochastic(MODE >= 0 ? MODE : a.mode)) rng_elem4(a.seed, a.offset + e, a.rng_lg, r);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) c[q] = codec_encode<MODE>(x[q], a, r[q]);
+    }
+}
+
+template <int N, bool REV, int MODE, int FAST>
+__global__ void __launch_bounds__(256)
+encode_direct_kernel(const float4* __restrict__ src, uint8_t* __restrict__ dst, int64_t count,
+                     int64_t out_bytes, CodecArg a) {
+    using T = typename Chunk<N>::T;
+    constexpr int U = 2;  // float4 loads in flight per thread
+    const int64_t nvec = count >> 2;
+    const int64_t stride = (int64_t)gridDim.x * 256;
+    T* out = reinterpret_cast<T*>(dst);
+    for (int64_t v0 = (int64_t)blockIdx.x * 256 + threadIdx.x; v0 < nvec; v0 += U * stride) {
+        float4 f[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (v0 + u * stride < nvec) f[u] = __ldcs(src + v0 + u * stride);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t v = v0 + u * stride;
+            if (v >= nvec) break;
+            const float x[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
+            uint32_t c[4];
+            encode4<N, MODE, FAST>(x, c, a, (uint64_t)v * 4);
+            const uint64_t w = pack4<N, REV>(c);
+            if constexpr (N == 16) __stcs(out + v, make_uint2((uint32_t)w, (uint32_t)(w >> 32)));
+            else out[v] = (T)w;
+        }
+    }
+    if ((count & 3) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const float* s = reinterpret_cast<const float*>(src);
+        float x[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) x[q] = nvec * 4 + q < count ? s[nvec * 4 + q] : 0.0f;
+        uint32_t c[4];
+        encode4<N, MODE, FAST>(x, c, a, (uint64_t)nvec * 4);
+        const uint64_t w = pack4<N, REV>(c);
+        const int64_t b0 = nvec * (N / 2);
+        for (int q = 0; q < N / 2 && b0 + q < out_bytes; ++q) dst[b0 + q] = (uint8_t)(w >> (8 * q));
+    }
+}
+
+template <int N, bool REV, bool FAST>
+__global__ void __launch_bounds__(256)
+decode_direct_kernel(const uint8_t* __restrict__ src, float4* __restrict__ dst, int64_t count,
+                     int64_t in_bytes, CodecArg a) {
+    using T = typename Chunk<N>::T;
+    constexpr int U = 1;  // code loads in flight per thread (four measured no faster)
+    const int64_t nvec = count >> 2;
+    const int64_t stride = (int64_t)gridDim.x * 256;
+    const T* in = reinterpret_cast<const T*>(src);
+    for (int64_t v0 = (int64_t)blockIdx.x * 256 + threadIdx.x; v0 < nvec; v0 += U * stride) {
+        uint64_t w[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            w[u] = 0;
+            if (v0 + u * stride < nvec) {
+                if constexpr (N == 16) {
+                    const uint2 t = __ldcs(in + v0 + u * stride);
+                    w[u] = (uint64_t)t.x | (uint64_t)t.y << 32;
+                } else {
+                    w[u] = __ldcs(in + v0 + u * stride);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t v = v0 + u * stride;
+            if (v >= nvec) break;
+            uint32_t c[4];
+            unpack4<N, REV>(w[u], c);
+            float y[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) y[q] = FAST ? codec_decode_fast(c[q], a) : codec_decode(c[q], a);
+            __stcs(dst + v, make_float4(y[0], y[1], y[2], y[3]));
+        }
+    }
+    if ((count & 3) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const int64_t b0 = nvec * (N / 2);
+        uint64_t w = 0;
+        for (int q = 0; q < N / 2 && b0 + q < in_bytes; ++q) w |= (uint64_t)src[b0 + q] << (8 * q);
+        uint32_t c[4];
+        unpack4<N, REV>(w, c);
+        float* d = reinterpret_cast<float*>(dst);
+        for (int q = 0; nvec * 4 + q < count; ++q)
+            d[nvec * 4 + q] = FAST ? codec_decode_fast(c[q], a) : codec_decode(c[q], a);
     }
 }
 
@@ -432,19 +585,21 @@ int make_codec_arg(CodecArg* a, const lofgb_codec_format* f, int mode, int sat, 
     a->enc_fast = 0;
     if (mode == LOFGB_RNE && narrower &&
         to_min > -125 && bias >= -100 && bias + m - 1 <= 127 && hi + d <= 254 &&
-        to_min + 127 + d >= 1 && hi >= to_min + 127) {
+        to_min + 127 + d >= 1 && hi >= to_min + 127 &&
+        (a->ovf_code == a->max_finite || a->ovf_code == a->max_finite + 1u)) {
         a->enc_fast = 1;
         a->uni_lo = (uint32_t)(to_min + 127) << 23;
         a->uni_hi = (uint32_t)hi << 23;
         a->uni_d = (uint32_t)d << 23;
         a->min_norm_bits = (uint32_t)(to_min + 127) << 23;
         a->code_off = (uint32_t)(127 - bias) << m;
-        a->sub_scale = std::ldexp(1.0f, bias + m - 1);
+        a->sub_c = std::ldexp(1.0f, to_min - m + 23);
     }
     a->dec_fast = 0;
-    if (to_min + 127 >= 1 && to_max + 127 <= 254 && to_min - m >= -149) {
+    if (to_min + 127 >= 1 && to_max + 127 <= 254 && to_min - m >= -149 && to_min - m + 23 <= 127) {
         a->dec_fast = 1;
         a->tiny = std::ldexp(1.0f, to_min - m);
+        a->sub_c_dec = std::ldexp(1.0f, to_min - m + 23);
         a->code_off_dec = (uint32_t)(bias - 127) << 23;
     }
     return LOFGB_OK;
@@ -458,11 +613,34 @@ int grid_for(int64_t count) {
     return (int)(g < maxg ? g : maxg);
 }
 
+// grid of the direct kernels: one float4 per thread per step, at most
+// 8 CTAs of 256 threads per SM
+int grid_direct(int64_t count) {
+    const int64_t need = ((count >> 2) + 255) / 256;
+    const int64_t maxg = (int64_t)sm_count() * 8;
+    return (int)(need < 1 ? 1 : (need < maxg ? need : maxg));
+}
+
 template <int N>
 int launch_encode_n(const float* src, uint8_t* dst, int64_t count, int reverse, const CodecArg& a,
                     cudaStream_t st) {
     const int grid = grid_for(count);
     const int64_t ob = packed_bytes(N, count);
+    if constexpr (N == 4 || N == 8 || N == 16) {
+        if ((reinterpret_cast<uintptr_t>(src) & 15) == 0 &&
+            (reinterpret_cast<uintptr_t>(dst) & (N / 2 - 1)) == 0) {
+            const float4* s4 = reinterpret_cast<const float4*>(src);
+            const int gd = grid_direct(count);
+#define LOFGB_ENCD(R, M, F) encode_direct_kernel<N, R, M, F><<<gd, 256, 0, st>>>(s4, dst, count, ob, a)
+            if (a.enc_fast == 1) {
+                if (reverse) LOFGB_ENCD(true, LOFGB_RNE, 1); else LOFGB_ENCD(false, LOFGB_RNE, 1);
+            } else {
+                if (reverse) LOFGB_ENCD(true, -1, 0); else LOFGB_ENCD(false, -1, 0);
+            }
+#undef LOFGB_ENCD
+            return check_launch("encode_direct_kernel");
+        }
+    }
     uint32_t* d = reinterpret_cast<uint32_t*>(dst);
 #define LOFGB_ENC(R, M, F) encode_kernel<N, R, M, F><<<grid, CT, 0, st>>>(src, d, count, ob, a)
 #define LOFGB_ENC_R(M, F) do { if (reverse) LOFGB_ENC(true, M, F); else LOFGB_ENC(false, M, F); } while (0)
@@ -480,6 +658,21 @@ int launch_decode_n(const uint8_t* src, float* dst, int64_t count, int reverse, 
                     cudaStream_t st) {
     const int grid = grid_for(count);
     const int64_t ib = packed_bytes(N, count);
+    if constexpr (N == 4 || N == 8 || N == 16) {
+        if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0 &&
+            (reinterpret_cast<uintptr_t>(src) & (N / 2 - 1)) == 0) {
+            float4* d4 = reinterpret_cast<float4*>(dst);
+            const int gd = grid_direct(count);
+#define LOFGB_DECD(R, F) decode_direct_kernel<N, R, F><<<gd, 256, 0, st>>>(src, d4, count, ib, a)
+            if (a.dec_fast) {
+                if (reverse) LOFGB_DECD(true, true); else LOFGB_DECD(false, true);
+            } else {
+                if (reverse) LOFGB_DECD(true, false); else LOFGB_DECD(false, false);
+            }
+#undef LOFGB_DECD
+            return check_launch("decode_direct_kernel");
+        }
+    }
     const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
     if (a.dec_fast) {
         if (reverse) decode_kernel<N, true, true><<<grid, CT, 0, st>>>(s, dst, count, ib, a);

@@ -232,11 +232,11 @@ __device__ __forceinline__ void pin16(float (&a)[N]) {
 // acc = RNE_m(rto(acc + s)) with directed adds, as the per-MAC leaf does with
 // directed FMAs (src/cutlass_gemms.cuh:73-88, 162-163); rto_word / rne_word
 // are that leaf's round-to-odd and RNE steps.
-__device__ __forceinline__ float fold(float acc, float s, int ro, uint32_t sh, uint32_t half_m1,
-                                      uint32_t mask) {
+__device__ __forceinline__ float fold(float acc, float s, int ro, uint32_t sh, uint32_t two,
+                                      uint32_t half_m1, uint32_t mask) {
     const uint32_t v = rto_word(__fadd_rd(acc, s), __fadd_ru(acc, s));
     if (ro <= 0) return __uint_as_float(v);
-    return __uint_as_float(rne_word(v, sh, half_m1, mask));
+    return __uint_as_float(rne_word2(v, sh, two, half_m1, mask));
 }
 
 // acc = RNE_format(rto(acc + s)) for a whole-format accumulator: the
@@ -487,7 +487,9 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
             const TileInfo ti = src.get(tile);
             const int nchunks = (ti.Kp / 16 + ti.chunk16 - 1) / ti.chunk16;
             const int ro = ti.ro;
-            const uint32_t sh = ro > 0 ? 1u << (32 - ro) : 0u;
+            const uint32_t sh = ro > 0 ? 1u << (31 - ro) : 0u;   // rne_word2 constants
+            uint32_t two;
+            asm volatile("mov.u32 %0, 2;" : "=r"(two));
             const uint32_t half_m1 = ro > 0 ? (1u << (ro - 1)) - 1u : 0u;
             const uint32_t mask = ro > 0 ? ~((1u << ro) - 1u) : ~0u;
             float acc[EPI_COLS];
@@ -497,7 +499,7 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                 if constexpr (ACCK == 0) {
 #pragma unroll
                     for (int i = 0; i < 16; ++i)
-                        acc[off + i] = fold(acc[off + i], __uint_as_float(r[i]), ro, sh, half_m1, mask);
+                        acc[off + i] = fold(acc[off + i], __uint_as_float(r[i]), ro, sh, two, half_m1, mask);
                 } else {
 #pragma unroll
                     for (int i = 0; i < 16; ++i)

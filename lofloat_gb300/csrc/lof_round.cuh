@@ -103,6 +103,15 @@ __device__ __forceinline__ uint32_t rto_word(float rd, float ru) {
 __device__ __forceinline__ uint32_t rne_word(uint32_t v, uint32_t sh, uint32_t half_m1, uint32_t mask) {
     return (v + (__umulhi(v, sh) & 1u) + half_m1) & mask;
 }
+// The same with bit ro of v taken by two multiplies, leaving the logic pipe
+// two operations: v * 2^(31 - ro) has it at bit 31 and the multiply-high by
+// two moves it to bit 0. `two` must be opaque to the compiler (a register the
+// caller fills from an asm), which would otherwise turn the multiply-high
+// into a shift on the logic pipe.
+__device__ __forceinline__ uint32_t rne_word2(uint32_t v, uint32_t sh2, uint32_t two, uint32_t half_m1,
+                                              uint32_t mask) {
+    return (v + __umulhi(v * sh2, two) + half_m1) & mask;
+}
 
 __device__ __forceinline__ double usamp_of(uint64_t r) {
     return (double)(r >> 11) * 0x1.0p-53;
