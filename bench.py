@@ -56,7 +56,8 @@ def parse():
     ap.add_argument("--no-secondary", action="store_true", help="headline workload only")
     ap.add_argument("--only", default=None,
                     choices=["mx", "round_rne", "round_sr", "gemm_plain", "gemm_tc", "conv_plain",
-                             "conv_tc", "pwl", "encode", "decode"],
+                             "conv_tc", "pwl", "encode", "decode", "encode_fp6", "decode_fp6",
+                             "grouped_round"],
                     help="run one workload's kernel warmup+steps times and exit (for ncu captures)")
     ap.add_argument("--size", default="full", choices=["full", "small"],
                     help="with --only: full-size workload or a small case (GEMM 1024^3)")
@@ -427,14 +428,10 @@ def linear_fwd_bwd(torch, lg, dev):
                                              "note": "dY rounded to E5M2 by SR-A: ~2^-3 noise"}}
 
 
-def grouped_workloads(torch, lg, dev):
-    """Config-5 workloads. Part 1: 512 FP32 tensors, n ~ 2^U(10,24), values
-    N(0,1)*2^U(-10,10), each with its own format (exp 2-8, mant 1-10, bias
-    2^(e-1)-1, saturating or not) and mode (RNE/RTZ/RTO/SR-A), seed 5: one
-    grouped launch replayed from a CUDA graph. Part 2: 64 emulated GEMMs,
-    M,N,K in {256..4096 step 256}, MX-E4M3 operands, accumulator bits 7-12,
-    one grouped tensor-core launch with the autotuned schedule, from a graph."""
-    out = {}
+def grouped_round_case(torch, lg, dev):
+    """Config-5 part 1: 512 FP32 tensors, each with its own format and mode
+    (seed 5). Returns the grouped launch and the two generators, which part 2
+    continues."""
     rng = np.random.default_rng(5)
     g = torch.Generator(device=dev).manual_seed(5)
     ins, outs, fmts, modes, lens, seeds = [], [], [], [], [], []
@@ -448,7 +445,18 @@ def grouped_workloads(torch, lg, dev):
         modes.append(int(rng.choice([0, 1, 12, 3])))
         lens.append(8 if modes[-1] == 3 else 0)
         seeds.append(int(rng.integers(0, 2**62)))
-    gr = lg.GroupedRound(ins, outs, fmts, modes, stoch_lens=lens, seeds=seeds)
+    return lg.GroupedRound(ins, outs, fmts, modes, stoch_lens=lens, seeds=seeds), rng, g
+
+
+def grouped_workloads(torch, lg, dev):
+    """Config-5 workloads. Part 1: 512 FP32 tensors, n ~ 2^U(10,24), values
+    N(0,1)*2^U(-10,10), each with its own format (exp 2-8, mant 1-10, bias
+    2^(e-1)-1, saturating or not) and mode (RNE/RTZ/RTO/SR-A), seed 5: one
+    grouped launch replayed from a CUDA graph. Part 2: 64 emulated GEMMs,
+    M,N,K in {256..4096 step 256}, MX-E4M3 operands, accumulator bits 7-12,
+    one grouped tensor-core launch with the autotuned schedule, from a graph."""
+    out = {}
+    gr, rng, g = grouped_round_case(torch, lg, dev)
     gr.capture()
     for _ in range(3):
         gr.replay()
@@ -462,7 +470,7 @@ def grouped_workloads(torch, lg, dev):
     ms = s.elapsed_time(e) / 10
     out["grouped_round_512_GBs"] = round(gr.bytes / ms / 1e6, 1)
     out["grouped_round_512_elements"] = int(gr.bytes // 8)
-    del ins, outs, gr
+    del gr
     torch.cuda.empty_cache()
     e4m3 = fmt_desc(lg, 8, 3, 7)
     e8 = lg.create_e8m0_params()
@@ -693,15 +701,20 @@ def run_only(args):
         ys = torch.empty_like(xs)
         fn = lambda: lg.pwl_silu(xs, lut, 8.0, out=ys)  # noqa: E731
         work, unit = (1 << 26) * 8, "GB/s"
-    elif args.only in ("encode", "decode"):
+    elif args.only in ("encode", "decode", "encode_fp6", "decode_fp6"):
         n = 1 << 26
         x = (torch.randn(n, device=dev) * torch.exp2(torch.randint(-20, 21, (n,), device=dev).float()))
-        fmt = lg.create_p3109_params(8, 4)
+        bits = 6 if args.only.endswith("fp6") else 8
+        fmt = lg.create_p3109_params(bits, 3 if bits == 6 else 4)
         packed = lg.lof_encode(x, fmt)
         y = torch.empty_like(x)
-        fn = (lambda: lg.lof_encode(x, fmt, out=packed)) if args.only == "encode" else \
+        fn = (lambda: lg.lof_encode(x, fmt, out=packed)) if args.only.startswith("encode") else \
             (lambda: lg.lof_decode(packed, n, fmt, out=y))  # noqa: E731
-        work, unit = n * 5, "GB/s"
+        work, unit = n * (4 + bits / 8), "GB/s"
+    elif args.only == "grouped_round":
+        gr = grouped_round_case(torch, lg, dev)[0]
+        fn = gr
+        work, unit = gr.bytes, "GB/s"
     else:
         n = GEMM_N if args.size == "full" else 1024
         g = torch.Generator().manual_seed(3)
