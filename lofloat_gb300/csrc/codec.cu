@@ -457,6 +457,141 @@ decode_direct_kernel(const uint8_t* __restrict__ src, float4* __restrict__ dst, 
     }
 }
 
+// ---- chunk kernels for the other widths ------------------------------------
+// G = lcm(N, 32) / N consecutive codes fill exactly W = lcm(N, 32) / 32 words
+// and hold whole groups (a group is lcm(N, 8 or 16) bits, which divides
+// lcm(N, 32)), so a thread encodes G values (G / 4 float4 loads) into W
+// words and decodes them back without staging: slots in stream order hold
+// the chunk's elements in order (forward) or reversed within each group.
+// The last chunk (fewer than G values left) is done by one thread, with
+// codes of +0.0 as padding and only the bytes below the packed size written.
+template <int N>
+struct ChunkGeo {
+    static constexpr int L = N / cgcd(N, 32) * 32;  // lcm(N, 32)
+    static constexpr int G = L / N;
+    static constexpr int W = L / 32;
+    static constexpr int V = G / 4;
+};
+
+template <int N, bool REV, int MODE, int FAST>
+__device__ __forceinline__ void encode_chunk(const float (&x)[ChunkGeo<N>::G], uint32_t (&out)[ChunkGeo<N>::W],
+                                             const CodecArg& a, uint64_t e0) {
+    constexpr int G = ChunkGeo<N>::G;
+    uint32_t c[G];
+    if constexpr (FAST != 0) {
+        bool sp = false;
+#pragma unroll
+        for (int i = 0; i < G; ++i) sp |= (__float_as_uint(x[i]) & 0x7FFFFFFFu) >= 0x7F800000u;
+        if (__any_sync(__activemask(), sp)) {
+#pragma unroll
+            for (int i = 0; i < G; ++i) c[i] = codec_encode_fast<true>(x[i], a);
+        } else {
+#pragma unroll
+            for (int i = 0; i < G; ++i) c[i] = codec_encode_fast<false>(x[i], a);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < G; i += 4) {
+            uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
+            if (mode_is_stochastic(MODE >= 0 ? MODE : a.mode)) rng_elem4(a.seed, a.offset + e0 + i, a.rng_lg, r);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) c[i + q] = codec_encode<MODE>(x[i + q], a, r[q]);
+        }
+    }
+    uint64_t acc = 0;
+    int fill = 0, widx = 0;
+#pragma unroll
+    for (int sl = 0; sl < G; ++sl) {
+        acc |= (uint64_t)(c[slot_element<N, REV>(sl)] & ((1u << N) - 1u)) << fill;
+        fill += N;
+        if (fill >= 32) {
+            out[widx++] = (uint32_t)acc;
+            acc >>= 32;
+            fill -= 32;
+        }
+    }
+}
+
+template <int N, bool REV, int MODE, int FAST>
+__global__ void __launch_bounds__(256)
+encode_chunk_kernel(const float4* __restrict__ src, uint32_t* __restrict__ dst, int64_t count,
+                    int64_t out_bytes, CodecArg a) {
+    using Geo = ChunkGeo<N>;
+    const int64_t nch = count / Geo::G;
+    for (int64_t ch = (int64_t)blockIdx.x * 256 + threadIdx.x; ch < nch; ch += (int64_t)gridDim.x * 256) {
+        float x[Geo::G];
+#pragma unroll
+        for (int j = 0; j < Geo::V; ++j) {
+            const float4 f = __ldcs(src + ch * Geo::V + j);
+            x[4 * j] = f.x; x[4 * j + 1] = f.y; x[4 * j + 2] = f.z; x[4 * j + 3] = f.w;
+        }
+        uint32_t out[Geo::W];
+        encode_chunk<N, REV, MODE, FAST>(x, out, a, (uint64_t)ch * Geo::G);
+#pragma unroll
+        for (int w = 0; w < Geo::W; ++w) __stcs(dst + ch * Geo::W + w, out[w]);
+    }
+    if (count % Geo::G != 0 && blockIdx.x == 0 && threadIdx.x == 0) {
+        const float* s = reinterpret_cast<const float*>(src);
+        float x[Geo::G];
+#pragma unroll
+        for (int i = 0; i < Geo::G; ++i) x[i] = nch * Geo::G + i < count ? s[nch * Geo::G + i] : 0.0f;
+        uint32_t out[Geo::W];
+        encode_chunk<N, REV, MODE, FAST>(x, out, a, (uint64_t)nch * Geo::G);
+        uint8_t* d8 = reinterpret_cast<uint8_t*>(dst);
+        const int64_t b0 = nch * Geo::W * 4;
+        for (int q = 0; q < Geo::W * 4 && b0 + q < out_bytes; ++q) d8[b0 + q] = (uint8_t)(out[q >> 2] >> (8 * (q & 3)));
+    }
+}
+
+template <int N, bool REV, bool FAST>
+__device__ __forceinline__ void decode_chunk(const uint32_t (&in)[ChunkGeo<N>::W], float (&y)[ChunkGeo<N>::G],
+                                             const CodecArg& a) {
+    constexpr int G = ChunkGeo<N>::G;
+    uint64_t buf = 0;
+    int avail = 0, widx = 0;
+#pragma unroll
+    for (int sl = 0; sl < G; ++sl) {
+        if (avail < N) {
+            buf |= (uint64_t)in[widx++] << avail;
+            avail += 32;
+        }
+        const uint32_t code = (uint32_t)buf & ((1u << N) - 1u);
+        buf >>= N;
+        avail -= N;
+        y[slot_element<N, REV>(sl)] = FAST ? codec_decode_fast(code, a) : codec_decode(code, a);
+    }
+}
+
+template <int N, bool REV, bool FAST>
+__global__ void __launch_bounds__(256)
+decode_chunk_kernel(const uint32_t* __restrict__ src, float4* __restrict__ dst, int64_t count,
+                    int64_t in_bytes, CodecArg a) {
+    using Geo = ChunkGeo<N>;
+    const int64_t nch = count / Geo::G;
+    for (int64_t ch = (int64_t)blockIdx.x * 256 + threadIdx.x; ch < nch; ch += (int64_t)gridDim.x * 256) {
+        uint32_t in[Geo::W];
+#pragma unroll
+        for (int w = 0; w < Geo::W; ++w) in[w] = __ldcs(src + ch * Geo::W + w);
+        float y[Geo::G];
+        decode_chunk<N, REV, FAST>(in, y, a);
+#pragma unroll
+        for (int j = 0; j < Geo::V; ++j)
+            __stcs(dst + ch * Geo::V + j, make_float4(y[4 * j], y[4 * j + 1], y[4 * j + 2], y[4 * j + 3]));
+    }
+    if (count % Geo::G != 0 && blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint8_t* s8 = reinterpret_cast<const uint8_t*>(src);
+        const int64_t b0 = nch * Geo::W * 4;
+        uint32_t in[Geo::W];
+#pragma unroll
+        for (int w = 0; w < Geo::W; ++w) in[w] = 0;
+        for (int q = 0; q < Geo::W * 4 && b0 + q < in_bytes; ++q) in[q >> 2] |= (uint32_t)s8[b0 + q] << (8 * (q & 3));
+        float y[Geo::G];
+        decode_chunk<N, REV, FAST>(in, y, a);
+        float* d = reinterpret_cast<float*>(dst);
+        for (int i = 0; nch * Geo::G + i < count; ++i) d[nch * Geo::G + i] = y[i];
+    }
+}
+
 template <int N, bool REV, bool FAST>
 __global__ void __launch_bounds__(CT)
 decode_kernel(const uint32_t* __restrict__ src, float* __restrict__ dst, int64_t count,
@@ -621,6 +756,13 @@ int grid_direct(int64_t count) {
     return (int)(need < 1 ? 1 : (need < maxg ? need : maxg));
 }
 
+// grid of the chunk kernels: one chunk of g values per thread per step
+int grid_chunk(int64_t count, int g) {
+    const int64_t need = (count / g + 255) / 256;
+    const int64_t maxg = (int64_t)sm_count() * 8;
+    return (int)(need < 1 ? 1 : (need < maxg ? need : maxg));
+}
+
 template <int N>
 int launch_encode_n(const float* src, uint8_t* dst, int64_t count, int reverse, const CodecArg& a,
                     cudaStream_t st) {
@@ -639,6 +781,17 @@ int launch_encode_n(const float* src, uint8_t* dst, int64_t count, int reverse, 
             }
 #undef LOFGB_ENCD
             return check_launch("encode_direct_kernel");
+        }
+    } else {
+        // the float-grid RNE encode (the common case); other modes stay staged
+        if (a.enc_fast == 1 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+            const float4* s4 = reinterpret_cast<const float4*>(src);
+            uint32_t* d32 = reinterpret_cast<uint32_t*>(dst);
+            const int gc = grid_chunk(count, ChunkGeo<N>::G);
+#define LOFGB_ENCC(R) encode_chunk_kernel<N, R, LOFGB_RNE, 1><<<gc, 256, 0, st>>>(s4, d32, count, ob, a)
+            if (reverse) LOFGB_ENCC(true); else LOFGB_ENCC(false);
+#undef LOFGB_ENCC
+            return check_launch("encode_chunk_kernel");
         }
     }
     uint32_t* d = reinterpret_cast<uint32_t*>(dst);
@@ -671,6 +824,17 @@ int launch_decode_n(const uint8_t* src, float* dst, int64_t count, int reverse, 
             }
 #undef LOFGB_DECD
             return check_launch("decode_direct_kernel");
+        }
+    } else {
+        // direct-bits decode (formats FP32 holds exactly); others stay staged
+        if (a.dec_fast && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+            float4* d4 = reinterpret_cast<float4*>(dst);
+            const uint32_t* s32 = reinterpret_cast<const uint32_t*>(src);
+            const int gc = grid_chunk(count, ChunkGeo<N>::G);
+#define LOFGB_DECC(R) decode_chunk_kernel<N, R, true><<<gc, 256, 0, st>>>(s32, d4, count, ib, a)
+            if (reverse) LOFGB_DECC(true); else LOFGB_DECC(false);
+#undef LOFGB_DECC
+            return check_launch("decode_chunk_kernel");
         }
     }
     const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
