@@ -21,6 +21,7 @@ namespace lofgb {
 namespace {
 
 constexpr int GT = 256;
+constexpr int GRING = 3;  // cp.async stages per thread (GRING - 1 vectors prefetched)
 
 template <int MODE>
 __device__ __forceinline__ uint32_t elem(uint32_t w, const GroupedTask& t, uint64_t idx) {
@@ -31,7 +32,7 @@ __device__ __forceinline__ uint32_t elem(uint32_t w, const GroupedTask& t, uint6
 }
 
 template <int MODE, int UNI>
-__device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
+__device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1, uint4 (*ring)[GT]) {
     const bool aligned =
         ((reinterpret_cast<uintptr_t>(t.in) | reinterpret_cast<uintptr_t>(t.out)) & 15) == 0 &&
         (e0 & 3) == 0;
@@ -39,10 +40,25 @@ __device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
         const int64_t v0 = e0 >> 2, v1 = e1 >> 2;  // full float4s
         const uint4* vin = reinterpret_cast<const uint4*>(t.in);
         uint4* vout = reinterpret_cast<uint4*>(t.out);
-        for (int64_t v = v0 + threadIdx.x; v < v1; v += GT) {
-            const uint4 a = __ldcs(vin + v);
+        // per-thread cp.async ring: the loads of the next RING - 1 vectors are
+        // in flight (in shared memory, not registers) while one is rounded
+        auto vec = [&](int k) { return v0 + threadIdx.x + (int64_t)k * GT; };
+#pragma unroll
+        for (int k = 0; k < GRING - 1; ++k) {
+            if (vec(k) < v1) cp_async16(&ring[k][threadIdx.x], vin + vec(k));
+            cp_async_commit();
+        }
+        int stage = 0;
+        for (int k = 0; vec(k) < v1; ++k) {
+            const int64_t v = vec(k);
+            const int64_t vp = vec(k + GRING - 1);
+            if (vp < v1) cp_async16(&ring[stage == 0 ? GRING - 1 : stage - 1][threadIdx.x], vin + vp);
+            cp_async_commit();
+            cp_async_wait<GRING - 1>();
+            const uint4 cur = ring[stage][threadIdx.x];
+            stage = stage == GRING - 1 ? 0 : stage + 1;
             const uint64_t i = (uint64_t)v * 4;
-            uint32_t w[4] = {a.x, a.y, a.z, a.w};
+            uint32_t w[4] = {cur.x, cur.y, cur.z, cur.w};
             uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
             const int mode = MODE >= 0 ? MODE : t.plan.mode;
             if (mode_is_stochastic(mode)) rng_elem4(t.seed, t.offset + i, t.plan.rng_lg, r);
@@ -60,6 +76,7 @@ __device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
             }
             __stcs(vout + v, make_uint4(w[0], w[1], w[2], w[3]));
         }
+        cp_async_wait<0>();
         for (int64_t i = (v1 << 2) + threadIdx.x; i < e1; i += GT) {
             const uint32_t w = reinterpret_cast<const uint32_t*>(t.in)[i];
             reinterpret_cast<uint32_t*>(t.out)[i] = elem<MODE>(w, t, (uint64_t)i);
@@ -75,6 +92,7 @@ __device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1) {
 __global__ void __launch_bounds__(GT)
 grouped_round_kernel(const GroupedTask* __restrict__ tasks, int ntasks, int64_t num_items) {
     __shared__ GroupedTask st;
+    __shared__ uint4 ring[GRING][GT];
     for (int64_t item = blockIdx.x; item < num_items; item += gridDim.x) {
         if (threadIdx.x == 0) {
             int lo = 0, hi = ntasks - 1;  // last task with item_begin <= item
@@ -93,21 +111,21 @@ grouped_round_kernel(const GroupedTask* __restrict__ tasks, int ntasks, int64_t 
         // uni is 1 only for RNE and 2 only for RTZ / RAFZ / RU / RD; sr_uni only for SR-A
         switch (t.plan.mode) {
         case LOFGB_RNE:
-            if (t.plan.uni) run_item<LOFGB_RNE, 1>(t, e0, e1);
-            else run_item<LOFGB_RNE, 0>(t, e0, e1);
+            if (t.plan.uni) run_item<LOFGB_RNE, 1>(t, e0, e1, ring);
+            else run_item<LOFGB_RNE, 0>(t, e0, e1, ring);
             break;
         case LOFGB_RTZ:
-            if (t.plan.uni) run_item<LOFGB_RTZ, 2>(t, e0, e1);
-            else run_item<LOFGB_RTZ, 0>(t, e0, e1);
+            if (t.plan.uni) run_item<LOFGB_RTZ, 2>(t, e0, e1, ring);
+            else run_item<LOFGB_RTZ, 0>(t, e0, e1, ring);
             break;
-        case LOFGB_RTO: run_item<LOFGB_RTO, 0>(t, e0, e1); break;
+        case LOFGB_RTO: run_item<LOFGB_RTO, 0>(t, e0, e1, ring); break;
         case LOFGB_SR_A:
-            if (t.plan.sr_uni) run_item<LOFGB_SR_A, 3>(t, e0, e1);
-            else run_item<LOFGB_SR_A, 0>(t, e0, e1);
+            if (t.plan.sr_uni) run_item<LOFGB_SR_A, 3>(t, e0, e1, ring);
+            else run_item<LOFGB_SR_A, 0>(t, e0, e1, ring);
             break;
         default:
-            if (t.plan.uni) run_item<-1, 2>(t, e0, e1);
-            else run_item<-1, 0>(t, e0, e1);
+            if (t.plan.uni) run_item<-1, 2>(t, e0, e1, ring);
+            else run_item<-1, 0>(t, e0, e1, ring);
             break;
         }
     }

@@ -82,6 +82,21 @@ __device__ __forceinline__ void rng_elem4(uint64_t seed, uint64_t g, int lg, uin
     }
 }
 
+// ---- per-thread cp.async staging (16-byte copies global -> shared) --------
+// Each thread copies into and later reads its own shared-memory slots, so a
+// wait_group is all the ordering it needs (no block barrier).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                     (uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // ---- round-to-odd word and RNE to m mantissa bits (the GEMM leaf) ----------
 // The round-to-odd result of one FP32 operation from its two directed
 // roundings rd (toward -inf) and ru (toward +inf). The reference form
@@ -107,7 +122,7 @@ __device__ __forceinline__ uint32_t rne_word(uint32_t v, uint32_t sh, uint32_t h
 // two operations: v * 2^(31 - ro) has it at bit 31 and the multiply-high by
 // two moves it to bit 0. `two` must be opaque to the compiler (a register the
 // caller fills from an asm), which would otherwise turn the multiply-high
-// into a shift on the logic pipe.
+// into a shift on the logic pipe; the same holds for sh2.
 __device__ __forceinline__ uint32_t rne_word2(uint32_t v, uint32_t sh2, uint32_t two, uint32_t half_m1,
                                               uint32_t mask) {
     return (v + __umulhi(v * sh2, two) + half_m1) & mask;

@@ -26,17 +26,6 @@ namespace {
 constexpr int MT = 256;
 constexpr int RING = 3;  // cp.async stages per thread (RING - 1 runs prefetched)
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                     (uint32_t)__cvta_generic_to_shared(smem)),
-                 "l"(gmem)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
 constexpr uint64_t SCALE_SALT = 0x5CA1E5CA1E5CA1E5ull;
 
 template <bool ALIGNED>

@@ -21,17 +21,6 @@ constexpr int RT = 256;  // threads per CTA
 constexpr int RU = 4;    // 16-byte vectors per thread per iteration
 constexpr int RING = 3;  // cp.async stages per thread (RING - 1 iterations prefetched)
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
-                     (uint32_t)__cvta_generic_to_shared(smem)),
-                 "l"(gmem)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
 
 struct ScaleArg {
     float f;      // f32 scale, or the f16 scale widened to float
