@@ -122,7 +122,7 @@ __device__ __forceinline__ uint32_t rne_word(uint32_t v, uint32_t sh, uint32_t h
 // two operations: v * 2^(31 - ro) has it at bit 31 and the multiply-high by
 // two moves it to bit 0. `two` must be opaque to the compiler (a register the
 // caller fills from an asm), which would otherwise turn the multiply-high
-// into a shift on the logic pipe; the same holds for sh2.
+// into a shift on the logic pipe.
 __device__ __forceinline__ uint32_t rne_word2(uint32_t v, uint32_t sh2, uint32_t two, uint32_t half_m1,
                                               uint32_t mask) {
     return (v + __umulhi(v * sh2, two) + half_m1) & mask;
