@@ -240,6 +240,7 @@ template <int N, bool REV, int MODE, int FAST>
 __global__ void __launch_bounds__(CT)
 encode_kernel(const float* __restrict__ src, uint32_t* __restrict__ dst, int64_t count,
               int64_t out_bytes, CodecArg a) {
+    pdl_wait();
     __shared__ float sx[CT / 32][TILE + 32];
     __shared__ uint32_t sw[CT / 32][32 * (N + 1)];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -375,6 +376,7 @@ template <int N, bool REV, int MODE, int FAST>
 __global__ void __launch_bounds__(256)
 encode_direct_kernel(const float4* __restrict__ src, uint8_t* __restrict__ dst, int64_t count,
                      int64_t out_bytes, CodecArg a) {
+    pdl_wait();
     using T = typename Chunk<N>::T;
     constexpr int U = 2;  // float4 loads in flight per thread
     const int64_t nvec = count >> 2;
@@ -414,6 +416,7 @@ template <int N, bool REV, bool FAST>
 __global__ void __launch_bounds__(256)
 decode_direct_kernel(const uint8_t* __restrict__ src, float4* __restrict__ dst, int64_t count,
                      int64_t in_bytes, CodecArg a) {
+    pdl_wait();
     using T = typename Chunk<N>::T;
     constexpr int U = 1;  // code loads in flight per thread (four measured no faster)
     const int64_t nvec = count >> 2;
@@ -516,6 +519,7 @@ template <int N, bool REV, int MODE, int FAST>
 __global__ void __launch_bounds__(256)
 encode_chunk_kernel(const float4* __restrict__ src, uint32_t* __restrict__ dst, int64_t count,
                     int64_t out_bytes, CodecArg a) {
+    pdl_wait();
     using Geo = ChunkGeo<N>;
     const int64_t nch = count / Geo::G;
     for (int64_t ch = (int64_t)blockIdx.x * 256 + threadIdx.x; ch < nch; ch += (int64_t)gridDim.x * 256) {
@@ -566,6 +570,7 @@ template <int N, bool REV, bool FAST>
 __global__ void __launch_bounds__(256)
 decode_chunk_kernel(const uint32_t* __restrict__ src, float4* __restrict__ dst, int64_t count,
                     int64_t in_bytes, CodecArg a) {
+    pdl_wait();
     using Geo = ChunkGeo<N>;
     const int64_t nch = count / Geo::G;
     for (int64_t ch = (int64_t)blockIdx.x * 256 + threadIdx.x; ch < nch; ch += (int64_t)gridDim.x * 256) {
@@ -596,6 +601,7 @@ template <int N, bool REV, bool FAST>
 __global__ void __launch_bounds__(CT)
 decode_kernel(const uint32_t* __restrict__ src, float* __restrict__ dst, int64_t count,
               int64_t in_bytes, CodecArg a) {
+    pdl_wait();
     __shared__ float sx[CT / 32][TILE + 32];
     __shared__ uint32_t sw[CT / 32][32 * (N + 1)];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -773,7 +779,7 @@ int launch_encode_n(const float* src, uint8_t* dst, int64_t count, int reverse, 
             (reinterpret_cast<uintptr_t>(dst) & (N / 2 - 1)) == 0) {
             const float4* s4 = reinterpret_cast<const float4*>(src);
             const int gd = grid_direct(count);
-#define LOFGB_ENCD(R, M, F) encode_direct_kernel<N, R, M, F><<<gd, 256, 0, st>>>(s4, dst, count, ob, a)
+#define LOFGB_ENCD(R, M, F) launch_pdl(encode_direct_kernel<N, R, M, F>, gd, 256, 0, st, s4, dst, count, ob, a)
             if (a.enc_fast == 1) {
                 if (reverse) LOFGB_ENCD(true, LOFGB_RNE, 1); else LOFGB_ENCD(false, LOFGB_RNE, 1);
             } else {
@@ -788,14 +794,14 @@ int launch_encode_n(const float* src, uint8_t* dst, int64_t count, int reverse, 
             const float4* s4 = reinterpret_cast<const float4*>(src);
             uint32_t* d32 = reinterpret_cast<uint32_t*>(dst);
             const int gc = grid_chunk(count, ChunkGeo<N>::G);
-#define LOFGB_ENCC(R) encode_chunk_kernel<N, R, LOFGB_RNE, 1><<<gc, 256, 0, st>>>(s4, d32, count, ob, a)
+#define LOFGB_ENCC(R) launch_pdl(encode_chunk_kernel<N, R, LOFGB_RNE, 1>, gc, 256, 0, st, s4, d32, count, ob, a)
             if (reverse) LOFGB_ENCC(true); else LOFGB_ENCC(false);
 #undef LOFGB_ENCC
             return check_launch("encode_chunk_kernel");
         }
     }
     uint32_t* d = reinterpret_cast<uint32_t*>(dst);
-#define LOFGB_ENC(R, M, F) encode_kernel<N, R, M, F><<<grid, CT, 0, st>>>(src, d, count, ob, a)
+#define LOFGB_ENC(R, M, F) launch_pdl(encode_kernel<N, R, M, F>, grid, CT, 0, st, src, d, count, ob, a)
 #define LOFGB_ENC_R(M, F) do { if (reverse) LOFGB_ENC(true, M, F); else LOFGB_ENC(false, M, F); } while (0)
     // the float-grid path for RNE (the codec's common mode); every other
     // mode and format through the general restatement
@@ -816,7 +822,7 @@ int launch_decode_n(const uint8_t* src, float* dst, int64_t count, int reverse, 
             (reinterpret_cast<uintptr_t>(src) & (N / 2 - 1)) == 0) {
             float4* d4 = reinterpret_cast<float4*>(dst);
             const int gd = grid_direct(count);
-#define LOFGB_DECD(R, F) decode_direct_kernel<N, R, F><<<gd, 256, 0, st>>>(src, d4, count, ib, a)
+#define LOFGB_DECD(R, F) launch_pdl(decode_direct_kernel<N, R, F>, gd, 256, 0, st, src, d4, count, ib, a)
             if (a.dec_fast) {
                 if (reverse) LOFGB_DECD(true, true); else LOFGB_DECD(false, true);
             } else {
@@ -831,7 +837,7 @@ int launch_decode_n(const uint8_t* src, float* dst, int64_t count, int reverse, 
             float4* d4 = reinterpret_cast<float4*>(dst);
             const uint32_t* s32 = reinterpret_cast<const uint32_t*>(src);
             const int gc = grid_chunk(count, ChunkGeo<N>::G);
-#define LOFGB_DECC(R) decode_chunk_kernel<N, R, true><<<gc, 256, 0, st>>>(s32, d4, count, ib, a)
+#define LOFGB_DECC(R) launch_pdl(decode_chunk_kernel<N, R, true>, gc, 256, 0, st, s32, d4, count, ib, a)
             if (reverse) LOFGB_DECC(true); else LOFGB_DECC(false);
 #undef LOFGB_DECC
             return check_launch("decode_chunk_kernel");
@@ -839,11 +845,11 @@ int launch_decode_n(const uint8_t* src, float* dst, int64_t count, int reverse, 
     }
     const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
     if (a.dec_fast) {
-        if (reverse) decode_kernel<N, true, true><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
-        else decode_kernel<N, false, true><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
+        if (reverse) launch_pdl(decode_kernel<N, true, true>, grid, CT, 0, st, s, dst, count, ib, a);
+        else launch_pdl(decode_kernel<N, false, true>, grid, CT, 0, st, s, dst, count, ib, a);
     } else {
-        if (reverse) decode_kernel<N, true, false><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
-        else decode_kernel<N, false, false><<<grid, CT, 0, st>>>(s, dst, count, ib, a);
+        if (reverse) launch_pdl(decode_kernel<N, true, false>, grid, CT, 0, st, s, dst, count, ib, a);
+        else launch_pdl(decode_kernel<N, false, false>, grid, CT, 0, st, s, dst, count, ib, a);
     }
     return check_launch("decode_kernel");
 }

@@ -1,7 +1,10 @@
 // lofgb_internal.h — types shared by the host launchers and the kernels of
 // liblofgb.so. Not part of the public C ABI (include/lofgb.h).
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
+#include <utility>
 
 #include "../../include/lofgb.h"
 
@@ -143,6 +146,43 @@ int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float*
 size_t gemm_tc_workspace(int M, int N, int K, int batch);
 
 }  // namespace lofgb
+
+namespace lofgb {
+
+// Programmatic dependent launch for the streaming kernels: the launch may
+// begin while the previous kernel in the stream is still running (its CTAs
+// then wait at griddepcontrol.wait, before touching memory, until that kernel
+// has completed and its writes are visible), which hides the gap between
+// back-to-back launches. Kernels launched this way call pdl_wait() before
+// their first global memory access; without the attribute it is a no-op.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t st, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+}  // namespace lofgb
+
+#ifdef __CUDACC__
+namespace lofgb {
+// Wait for the preceding kernel (programmatic dependent launch), then let
+// the next one begin its launch.
+__device__ __forceinline__ void pdl_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+}  // namespace lofgb
+#endif
 
 namespace lofgb {
 

@@ -197,6 +197,7 @@ template <int BS, int EMODE, int SMODE, bool ALIGNED, int UNI = 0>
 __global__ void __launch_bounds__(MT, UNI != 0 ? 5 : 1)
 mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, float inv_pmn,
           uint64_t seed, uint64_t offset) {
+    pdl_wait();
     using G = MxGeo<BS>;
     constexpr int U = G::U, VPT = G::VPT, L = G::L, SLOT = G::SLOT;
     const int lane = threadIdx.x & 31;
@@ -288,15 +289,15 @@ int launch_bs(const float* in, float* out, int64_t n, const RoundPlan& pe, const
     const int grid = (int)(g < 1 ? 1 : (g < maxg ? g : maxg));
     const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
     if (!aligned)
-        mx_kernel<BS, -1, -1, false><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<BS, -1, -1, false>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE && pe.uni == 1)
-        mx_kernel<BS, LOFGB_RNE, LOFGB_RNE, true, 1><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<BS, LOFGB_RNE, LOFGB_RNE, true, 1>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE)
-        mx_kernel<BS, LOFGB_RNE, LOFGB_RNE, true><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<BS, LOFGB_RNE, LOFGB_RNE, true>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (ps.mode == LOFGB_RNE)
-        mx_kernel<BS, -1, LOFGB_RNE, true><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<BS, -1, LOFGB_RNE, true>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else
-        mx_kernel<BS, -1, -1, true><<<grid, MT, 0, st>>>(in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<BS, -1, -1, true>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     return check_launch("mx_kernel");
 }
 

@@ -55,6 +55,7 @@ template <typename T>
 __global__ void __launch_bounds__(PT)
 pwl_silu_kernel(const T* __restrict__ in, T* __restrict__ out, int64_t n,
                 const float* __restrict__ lut, int nseg, float R, float inv_step, int vec) {
+    pdl_wait();
     constexpr int EPV = 16 / sizeof(T);
     const int64_t stride = (int64_t)gridDim.x * PT;
     int64_t done = 0;
@@ -97,8 +98,8 @@ int launch_pwl(const T* in, T* out, int64_t n, const float* lut, int nseg, float
     const int64_t maxg = (int64_t)sm_count() * (2048 / PT);
     if (g < 1) g = 1;
     if (g > maxg) g = maxg;
-    pwl_silu_kernel<T><<<(int)g, PT, 0, static_cast<cudaStream_t>(stream)>>>(in, out, n, lut, nseg, R,
-                                                                             inv_step, vec);
+    launch_pdl(pwl_silu_kernel<T>, (int)g, PT, 0, static_cast<cudaStream_t>(stream), in, out, n, lut,
+               nseg, R, inv_step, vec);
     return check_launch("pwl_silu_kernel");
 }
 

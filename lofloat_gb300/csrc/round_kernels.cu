@@ -61,6 +61,7 @@ template <int MODE, int W, bool FMT, bool SCALED, int UNI = 0>
 __global__ void __launch_bounds__(RT)
 round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
                  RoundPlan p, ScaleArg s, uint64_t seed, uint64_t offset) {
+    pdl_wait();
     using U = typename Src<W>::U;
     constexpr int EPV = 128 / W;  // elements per 16-byte vector
     const int64_t nvec = n / EPV;
@@ -191,6 +192,7 @@ template <int W, bool FMT>
 __global__ void __launch_bounds__(RT)
 round_scalar_kernel(const void* in, void* out, int64_t n, RoundPlan p,
                     ScaleArg s, uint64_t seed, uint64_t offset) {
+    pdl_wait();
     for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < n; i += (int64_t)gridDim.x * RT) {
         if constexpr (W == 32) {
             const uint32_t w = static_cast<const uint32_t*>(in)[i];
@@ -214,7 +216,7 @@ int launch_w(const void* in, void* out, int64_t n, const RoundPlan& p, const Sca
     if (!aligned) {
         int64_t g = (n + RT - 1) / RT;
         const int grid = (int)(g < maxg ? g : maxg);
-        round_scalar_kernel<W, FMT><<<grid, RT, 0, st>>>(in, out, n, p, s, seed, offset);
+        launch_pdl(round_scalar_kernel<W, FMT>, grid, RT, 0, st, in, out, n, p, s, seed, offset);
         return check_launch("round_scalar_kernel");
     }
     constexpr int EPV = 128 / W;
@@ -225,8 +227,8 @@ int launch_w(const void* in, void* out, int64_t n, const RoundPlan& p, const Sca
     auto vi = static_cast<const uint4*>(in);
     auto vo = static_cast<uint4*>(out);
 #define LOFGB_RVU(M, UNI)                                                                    \
-    (s.apply ? round_vec_kernel<M, W, FMT, true, UNI><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset) \
-             : round_vec_kernel<M, W, FMT, false, UNI><<<grid, RT, 0, st>>>(vi, vo, n, p, s, seed, offset))
+    (s.apply ? launch_pdl(round_vec_kernel<M, W, FMT, true, UNI>, grid, RT, 0, st, vi, vo, n, p, s, seed, offset) \
+             : launch_pdl(round_vec_kernel<M, W, FMT, false, UNI>, grid, RT, 0, st, vi, vo, n, p, s, seed, offset))
 #define LOFGB_RV(M) LOFGB_RVU(M, 0)
     if constexpr (W == 32 && FMT) {
         // whole-range float rounding: RNE (uni 1) or the directed modes (uni 2)
