@@ -245,6 +245,13 @@ def time_events(torch, fn, reps, stream):
     return [s.elapsed_time(e) for s, e in zip(starts, ends)]
 
 
+def time_batched(torch, fn, stream, per_batch=10, batches=5):
+    """Median per-launch time (ms) of `per_batch` back-to-back calls between
+    two events, over `batches` batches (no event between two launches)."""
+    return statistics.median(m / per_batch for m in
+                             time_events(torch, lambda: [fn() for _ in range(per_batch)], batches, stream))
+
+
 def secondary(torch, lg, dev, peaks):
     """Plain rounding (config-1 workload) and the 4096^3 emulated GEMMs."""
     out = {}
@@ -355,7 +362,7 @@ def conv_workloads(torch, lg, dev, peaks):
     fn = lambda: lg.pwl_silu(xs, lut, 8.0, out=ys)  # noqa: E731
     for _ in range(3):
         fn()
-    ms = statistics.median(time_events(torch, fn, 20, stream))
+    ms = time_batched(torch, fn, stream)
     gbs = (1 << 26) * 8 / (ms * 1e-3) / 1e9
     out["pwl_silu_2^26_GBs"] = round(gbs, 1)
     out["pwl_silu_2^26_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)
@@ -383,7 +390,7 @@ def codec_workloads(torch, lg, dev, peaks):
         for fn, tag in ((enc, "encode"), (dec, "decode")):
             for _ in range(3):
                 fn()
-            ms = statistics.median(time_events(torch, fn, 10, stream))
+            ms = time_batched(torch, fn, stream)
             gbs = n * (4 + bits / 8) / (ms * 1e-3) / 1e9
             out[f"codec_{tag}_{name}_2^26_GBs"] = round(gbs, 1)
             out[f"codec_{tag}_{name}_2^26_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)
