@@ -454,6 +454,18 @@ __device__ __forceinline__ uint32_t vr_uni_f32(uint32_t x, const RoundPlan& p) {
     return (x & 0x7FFFFFFFu) > 0x7F800000u ? 0x7FC00000u : res;
 }
 
+// vr_uni_f32<RNE, 1> for a saturating format, whose overflow returns the
+// input word: a NaN input rounds to a NaN word, above every overflow
+// threshold, and so comes back as the input NaN rather than the canonical
+// quiet NaN. Only for callers whose next operation on the result turns any
+// NaN into the same canonical NaN (MX multiplies it by the block scale).
+__device__ __forceinline__ uint32_t vr_uni_sat_rne_f32(uint32_t x, const RoundPlan& p) {
+    const uint32_t cb = min(max(x & 0x7F800000u, p.uni_lo), p.uni_hi) + p.uni_d;
+    const float c = __uint_as_float(cb);
+    const uint32_t r = __float_as_uint(__fsub_rn(__fadd_rn(fabsf(__uint_as_float(x)), c), c));
+    return r >= (uint32_t)p.ovf_thr ? x : (r | (x & 0x80000000u));
+}
+
 // virtual_round(x, params, {SR-A, len}) of an f32 word by float arithmetic
 // (RoundPlan::sr_uni); r holds the element's random bits in its low len bits.
 // The noise R' * spacing * 2^-len is built exactly as F - E with

@@ -98,7 +98,12 @@ __device__ __forceinline__ float4 quant4(float4 x, const BlockScale& b, const Ro
         for (int i = 0; i < 4; ++i) q[i] = b.pow2 ? __fmul_rn(q[i], b.inv) : __fdiv_rn(q[i], b.scale);
     }
     uint32_t w[4];
-    if constexpr (UNI != 0) {
+    if constexpr (UNI == 4) {
+        // saturating element format: a NaN q comes back as itself and the
+        // rescale below turns it into the canonical NaN, as for qNaN
+#pragma unroll
+        for (int i = 0; i < 4; ++i) w[i] = vr_uni_sat_rne_f32(__float_as_uint(q[i]), pe);
+    } else if constexpr (UNI != 0) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) w[i] = vr_uni_f32<EMODE, UNI>(__float_as_uint(q[i]), pe);
     } else {
@@ -290,6 +295,8 @@ int launch_bs(const float* in, float* out, int64_t n, const RoundPlan& pe, const
     const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
     if (!aligned)
         launch_pdl(mx_kernel<BS, -1, -1, false>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
+    else if (BS == 32 && pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE && pe.uni == 1 && pe.saturating)
+        launch_pdl(mx_kernel<32, LOFGB_RNE, LOFGB_RNE, true, 4>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE && pe.uni == 1)
         launch_pdl(mx_kernel<BS, LOFGB_RNE, LOFGB_RNE, true, 1>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE)
