@@ -378,27 +378,33 @@ encode_direct_kernel(const float4* __restrict__ src, uint8_t* __restrict__ dst, 
                      int64_t out_bytes, CodecArg a) {
     pdl_wait();
     using T = typename Chunk<N>::T;
-    constexpr int U = 2;  // float4 loads in flight per thread
+    constexpr int RING = 4;  // per-thread cp.async stages (RING - 1 vectors in flight)
+    __shared__ float4 ring[RING][256];
     const int64_t nvec = count >> 2;
     const int64_t stride = (int64_t)gridDim.x * 256;
     T* out = reinterpret_cast<T*>(dst);
-    for (int64_t v0 = (int64_t)blockIdx.x * 256 + threadIdx.x; v0 < nvec; v0 += U * stride) {
-        float4 f[U];
+    const int64_t v0 = (int64_t)blockIdx.x * 256 + threadIdx.x;
 #pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (v0 + u * stride < nvec) f[u] = __ldcs(src + v0 + u * stride);
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int64_t v = v0 + u * stride;
-            if (v >= nvec) break;
-            const float x[4] = {f[u].x, f[u].y, f[u].z, f[u].w};
-            uint32_t c[4];
-            encode4<N, MODE, FAST>(x, c, a, (uint64_t)v * 4);
-            const uint64_t w = pack4<N, REV>(c);
-            if constexpr (N == 16) __stcs(out + v, make_uint2((uint32_t)w, (uint32_t)(w >> 32)));
-            else out[v] = (T)w;
-        }
+    for (int k = 0; k < RING - 1; ++k) {
+        if (v0 + k * stride < nvec) cp_async16(&ring[k][threadIdx.x], src + v0 + k * stride);
+        cp_async_commit();
     }
+    int stage = 0;
+    for (int64_t v = v0; v < nvec; v += stride) {
+        const int64_t vp = v + (RING - 1) * stride;
+        if (vp < nvec) cp_async16(&ring[stage == 0 ? RING - 1 : stage - 1][threadIdx.x], src + vp);
+        cp_async_commit();
+        cp_async_wait<RING - 1>();
+        const float4 f = ring[stage][threadIdx.x];
+        stage = stage == RING - 1 ? 0 : stage + 1;
+        const float x[4] = {f.x, f.y, f.z, f.w};
+        uint32_t c[4];
+        encode4<N, MODE, FAST>(x, c, a, (uint64_t)v * 4);
+        const uint64_t w = pack4<N, REV>(c);
+        if constexpr (N == 16) __stcs(out + v, make_uint2((uint32_t)w, (uint32_t)(w >> 32)));
+        else out[v] = (T)w;
+    }
+    cp_async_wait<0>();
     if ((count & 3) && blockIdx.x == 0 && threadIdx.x == 0) {
         const float* s = reinterpret_cast<const float*>(src);
         float x[4];
