@@ -24,7 +24,7 @@ from .formats import (create_e8m0_params, create_half_params, create_p3109_param
                       create_single_params, make_format)
 from .layers import (LinearConfig, LoF_Conv2d, LoF_Linear, LoF_MultiHeadAttention, LoF_Quantize,
                      LoFLinearFunction, PWLSiLU, STEMXRound, STERound, _fwht, _lof_gemm_2d,
-                     _lof_linear, lof_linear)
+                     _lof_linear, _quantize, exp_mant_quantize, lof_linear, mantissa_quantize)
 from ._custom_ops import get_format, register_format
 from .grouped import GroupedRound
 from .norms import FISRBatchNorm, L1BatchNorm, LinfBatchNorm, PWLBatchNorm
@@ -36,6 +36,7 @@ __all__ = [
     "set_seed", "get_rng_state", "set_rng_state", "create_p3109_params", "create_e8m0_params",
     "create_half_params", "create_single_params", "make_format", "STERound", "STEMXRound",
     "LoF_Quantize", "LoF_Linear", "LoFLinearFunction", "LinearConfig", "lof_linear",
+    "mantissa_quantize", "exp_mant_quantize",
     "register_format", "get_format", "GroupedRound", "GroupedGemm", "lof_conv2d", "conv2d",
     "conv2d_alpha", "pwl_silu", "LoF_Conv2d", "PWLSiLU", "LoF_MultiHeadAttention",
     "SaturationMode", "codec_format", "packed_size", "lof_encode", "lof_decode",

@@ -83,6 +83,32 @@ class LoF_Quantize(nn.Module):
         return STERound.apply(x, self.params, self.rounding_mode)
 
 
+def _quantize(self, tensor, params):
+    """STE rounding of `tensor` to `params` under the owner's rounding_mode
+    (LoFloat/layers.py:106-109); None leaves the tensor as is."""
+    if params is None:
+        return tensor
+    return STERound.apply(tensor, params, self.rounding_mode)
+
+
+def mantissa_quantize(tensor, mantissa_bits):
+    """STE rounding to a signed, saturating P3109 format with 8 exponent bits
+    and `mantissa_bits` stored mantissa bits (LoFloat/layers.py:111-114)."""
+    if mantissa_bits is None:
+        return tensor
+    return STERound.apply(tensor, create_p3109_params(8 + mantissa_bits + 1, mantissa_bits + 1, True, True))
+
+
+def exp_mant_quantize(tensor, exp_bits, mantissa_bits):
+    """STE rounding to a signed, saturating P3109 format with `exp_bits`
+    exponent and `mantissa_bits` stored mantissa bits
+    (LoFloat/layers.py:116-119)."""
+    if exp_bits is None or mantissa_bits is None:
+        return tensor
+    return STERound.apply(tensor, create_p3109_params(exp_bits + mantissa_bits + 1, mantissa_bits + 1,
+                                                      True, True))
+
+
 def _lof_gemm_2d(A, B, accum_mant_bits, gemm_round_mode, stochastic_rounding_bits, scale_a=1.0,
                  scale_b=1.0, variant="plain", chunk=32):
     """(..., M, K) x (..., K, N) -> (..., M, N) (LoFloat/layers.py:121-150), with
