@@ -193,7 +193,7 @@ int make_round_plan(RoundPlan* p, const lofgb_format* f, int src_bits, int mode,
         p->grid_c > 0.0f) {
         p->sr_uni = 1;
         p->sr_mask = len >= 32 ? 0xFFFFFFFFu : ((1u << len) - 1u);
-        p->sr_shift = (uint32_t)len << 23;
+        p->sr_shift = (uint32_t)(p->d - len) << 23;
     }
     return LOFGB_OK;
 }

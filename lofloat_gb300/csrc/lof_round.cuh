@@ -469,23 +469,25 @@ __device__ __forceinline__ uint32_t vr_uni_sat_rne_f32(uint32_t x, const RoundPl
 // virtual_round(x, params, {SR-A, len}) of an f32 word by float arithmetic
 // (RoundPlan::sr_uni); r holds the element's random bits in its low len bits.
 // The noise R' * spacing * 2^-len is built exactly as F - E with
-// E = 2^(e_C - len) (e_C the exponent of C) and F = E with R' in its low
+// E = 2^(e_C - len) (e_C the exponent of C; E's word is the clamped exponent
+// field plus sr_shift = (d - len) << 23) and F = E with R' in its low
 // mantissa bits (R' < 2^len, len <= d <= 23, so F = E + R' * ulp(E)). The
 // truncation of y to the target's spacing at y is y's word with the d low bits
 // cleared where y is at or above the target's smallest normal (every such y
 // then has spacing 2^(e_y - m), or overflows), and fadd_rz(y, Csub) - Csub with
 // Csub = 2^(to_min + d) (ulp = tiny) below it.
+// SAT: a saturating format, whose overflow returns the input word.
+template <bool SAT = false>
 __device__ __forceinline__ uint32_t vr_uni_sra_f32(uint32_t x, const RoundPlan& p, uint32_t r) {
     const uint32_t mag = x & 0x7FFFFFFFu;
-    const uint32_t cbx = min(max(x & 0x7F800000u, p.uni_lo), p.uni_hi) + p.uni_d;
-    const uint32_t eb = cbx - p.sr_shift;
+    const uint32_t eb = min(max(x & 0x7F800000u, p.uni_lo), p.uni_hi) + p.sr_shift;
     const float noise = __fsub_rn(__uint_as_float((r & p.sr_mask) | eb), __uint_as_float(eb));
     const float y = __fadd_rz(__uint_as_float(mag), noise);
     const uint32_t yb = __float_as_uint(y);
     const uint32_t vs = __float_as_uint(__fsub_rn(__fadd_rz(y, p.grid_c), p.grid_c));
     const uint32_t v = yb >= (uint32_t)p.norm_thr ? (yb & (uint32_t)p.keep_mask) : vs;
     uint32_t res = v | (x & 0x80000000u);
-    res = v >= (uint32_t)p.ovf_thr ? ((x & p.sat_and) | p.sat_or) : res;
+    res = v >= (uint32_t)p.ovf_thr ? (SAT ? x : ((x & p.sat_and) | p.sat_or)) : res;
     res = mag < (uint32_t)p.tiny_thr ? (x & 0x80000000u) : res;
     return mag > 0x7F800000u ? 0x7FC00000u : res;
 }

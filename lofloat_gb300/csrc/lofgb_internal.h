@@ -70,7 +70,7 @@ struct RoundPlan {
     // conditions hold, the float grid constant grid_c exists, and
     // len <= min(d, 24) with tiny * 2^-len a normal float.
     int32_t sr_uni;
-    uint32_t sr_mask, sr_shift;      // R' mask; len << 23
+    uint32_t sr_mask, sr_shift;      // R' mask; (d - len) << 23
     // Random words: element g of a stream reads lane g mod 2^rng_lg (from the
     // low end) of the SplitMix64 output number g >> rng_lg; lanes are
     // 64 >> rng_lg bits wide, the narrowest of 8/16/32/64 that holds every

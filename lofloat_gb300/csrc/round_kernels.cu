@@ -72,15 +72,15 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
     auto round_vec = [&](const uint4& vv, int64_t vi, bool full) -> uint4 {
         const uint64_t e0 = offset + (uint64_t)vi * EPV;
         uint4 o;
-        if constexpr (W == 32 && FMT && UNI == 3) {
-            // SR-A by float arithmetic (RoundPlan::sr_uni)
+        if constexpr (W == 32 && FMT && (UNI == 3 || UNI == 5)) {
+            // SR-A by float arithmetic (RoundPlan::sr_uni); UNI 5: saturating format
             uint32_t w[4] = {vv.x, vv.y, vv.z, vv.w};
             uint64_t r[4];
             rng_elem4(seed, e0, p.rng_lg, r);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
-                w[q] = vr_uni_sra_f32(w[q], p, r[q]);
+                w[q] = vr_uni_sra_f32<UNI == 5>(w[q], p, r[q]);
             }
             o = make_uint4(w[0], w[1], w[2], w[3]);
         } else if constexpr (W == 32 && FMT && UNI != 0) {
@@ -242,7 +242,8 @@ int launch_w(const void* in, void* out, int64_t n, const RoundPlan& p, const Sca
             return check_launch("round_vec_kernel");
         }
         if (p.sr_uni) {
-            LOFGB_RVU(LOFGB_SR_A, 3);
+            if (p.saturating) LOFGB_RVU(LOFGB_SR_A, 5);
+            else LOFGB_RVU(LOFGB_SR_A, 3);
             return check_launch("round_vec_kernel");
         }
     }
