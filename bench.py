@@ -460,7 +460,7 @@ def grouped_round_case(torch, lg, dev):
         modes.append(int(rng.choice([0, 1, 12, 3])))
         lens.append(8 if modes[-1] == 3 else 0)
         seeds.append(int(rng.integers(0, 2**62)))
-    return lg.GroupedRound(ins, outs, fmts, modes, stoch_lens=lens, seeds=seeds), rng, g
+    return lg.GroupedRound(ins, outs, fmts, modes, stoch_lens=lens, seeds=seeds, item="auto"), rng, g
 
 
 def grouped_workloads(torch, lg, dev):
@@ -485,6 +485,8 @@ def grouped_workloads(torch, lg, dev):
     ms = s.elapsed_time(e) / 10
     out["grouped_round_512_GBs"] = round(gr.bytes / ms / 1e6, 1)
     out["grouped_round_512_elements"] = int(gr.bytes // 8)
+    out["grouped_round_512_item"] = gr.item
+    out["grouped_round_512_tuning_ms"] = {str(k): v for k, v in gr.tuning_ms.items()}
     del gr
     torch.cuda.empty_cache()
     e4m3 = fmt_desc(lg, 8, 3, 7)

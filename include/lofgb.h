@@ -310,6 +310,12 @@ size_t lofgb_round_grouped_table_size(int ntasks);
 /* Returns LOFGB_OK and stores the number of work items in *num_items. */
 int lofgb_round_grouped_prepare(const lofgb_round_task* tasks, int ntasks, void* table,
                                 size_t table_bytes, int64_t* num_items);
+/* The same with work items of `item_elems` elements (a power of two in
+ * [2^10, 2^24]; the entry above uses 2^16). Smaller items balance uneven task
+ * sizes better, larger ones cost fewer task look-ups; GroupedRound's
+ * item="auto" picks one by timing. */
+int lofgb_round_grouped_prepare_items(const lofgb_round_task* tasks, int ntasks, void* table,
+                                      size_t table_bytes, int64_t item_elems, int64_t* num_items);
 int lofgb_round_grouped_f32(const void* device_table, int ntasks, int64_t num_items,
                             void* stream);
 

@@ -88,6 +88,8 @@ SIGNATURES = [
     ("lofgb_round_grouped_table_size", _sz, [_i32]),
     ("lofgb_round_grouped_prepare", _i32, [C.POINTER(LofgbRoundTask), _i32, _vp, _sz,
                                            C.POINTER(C.c_int64)]),
+    ("lofgb_round_grouped_prepare_items", _i32, [C.POINTER(LofgbRoundTask), _i32, _vp, _sz, _i64,
+                                                 C.POINTER(C.c_int64)]),
     ("lofgb_round_grouped_f32", _i32, [_vp, _i32, _i64, _vp]),
     ("lofgb_conv2d_out_size", _i32, [C.POINTER(LofgbConv2dShape), C.POINTER(C.c_int32),
                                      C.POINTER(C.c_int32)]),

@@ -44,6 +44,11 @@ def signature(shapes) -> str:
     return json.dumps(b)
 
 
+def round_signature(sizes_modes) -> str:
+    """Signature of a grouped rounding problem: sorted (size bucket, mode)."""
+    return "round:" + json.dumps(sorted((_bucket(n), int(m)) for n, m in sizes_modes))
+
+
 def _load_cache() -> dict:
     try:
         with open(CACHE_PATH) as fh:

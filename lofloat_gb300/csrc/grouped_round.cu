@@ -1,7 +1,8 @@
 // grouped_round.cu — one persistent launch that rounds many FP32 tensors, each
 // with its own format, mode, scale and RNG stream.
 //
-// The host splits every tensor into work items of GROUPED_ITEM elements and
+// The host splits every tensor into work items of 2^item_shift elements (2^16
+// unless the caller picks another size) and
 // writes one GroupedTask row per tensor (with the prefix sum of item counts)
 // into a table the caller uploads once. CTAs walk the item space with a
 // grid-stride loop; each item finds its task by binary search over the
@@ -106,8 +107,8 @@ grouped_round_kernel(const GroupedTask* __restrict__ tasks, int ntasks, int64_t 
         __syncthreads();
         const GroupedTask t = st;
         __syncthreads();
-        const int64_t e0 = (item - t.item_begin) * GROUPED_ITEM;
-        const int64_t e1 = min(e0 + GROUPED_ITEM, t.n);
+        const int64_t e0 = (item - t.item_begin) << t.item_shift;
+        const int64_t e1 = min(e0 + ((int64_t)1 << t.item_shift), t.n);
         // uni is 1 only for RNE and 2 only for RTZ / RAFZ / RU / RD; sr_uni only for SR-A
         switch (t.plan.mode) {
         case LOFGB_RNE:
@@ -154,6 +155,17 @@ size_t lofgb_round_grouped_table_size(int ntasks) {
 
 int lofgb_round_grouped_prepare(const lofgb_round_task* tasks, int ntasks, void* table,
                                 size_t table_bytes, int64_t* num_items) {
+    return lofgb_round_grouped_prepare_items(tasks, ntasks, table, table_bytes,
+                                             (int64_t)1 << GROUPED_ITEM_SHIFT, num_items);
+}
+
+int lofgb_round_grouped_prepare_items(const lofgb_round_task* tasks, int ntasks, void* table,
+                                      size_t table_bytes, int64_t item_elems, int64_t* num_items) {
+    int shift = 0;
+    while (shift < 31 && ((int64_t)1 << shift) < item_elems) ++shift;
+    if (item_elems < 1024 || item_elems > (1 << 24) || ((int64_t)1 << shift) != item_elems)
+        return set_error(LOFGB_ERR_SIZE, "item size %lld: a power of two in [2^10, 2^24]",
+                         (long long)item_elems);
     if (ntasks < 0) return set_error(LOFGB_ERR_SIZE, "negative task count");
     if (ntasks > 0 && (!tasks || !table || !num_items))
         return set_error(LOFGB_ERR_NULL, "NULL tasks, table or num_items");
@@ -187,10 +199,11 @@ int lofgb_round_grouped_prepare(const lofgb_round_task* tasks, int ntasks, void*
         g.item_begin = items;
         g.scale = t.scale;
         g.apply_scale = t.scale != 1.0f;
+        g.item_shift = shift;
         g.seed = t.seed;
         g.offset = t.offset;
         rows[i] = g;
-        items += (t.n + GROUPED_ITEM - 1) / GROUPED_ITEM;
+        items += (t.n + ((int64_t)1 << shift) - 1) >> shift;
     }
     if (num_items) *num_items = items;
     return LOFGB_OK;

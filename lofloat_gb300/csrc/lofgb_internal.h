@@ -195,9 +195,10 @@ struct GroupedTask {
     RoundPlan plan;
     float scale;
     int32_t apply_scale;
+    int32_t item_shift;  // work items of 2^item_shift elements
     uint64_t seed, offset;
 };
-constexpr int64_t GROUPED_ITEM = 1 << 16;  // elements per work item
+constexpr int GROUPED_ITEM_SHIFT = 16;  // default work item: 2^16 elements
 
 int launch_round_grouped(const void* table, int ntasks, int64_t num_items, void* stream);
 

@@ -19,12 +19,20 @@ import torch
 
 from . import _native
 from ._native import LofgbRoundTask, check
+from .autotune import _load_cache, _store_cache, round_signature
 from .binding import FloatFormatDescriptor, _stream
 
 
+ITEM_CANDIDATES = (1 << 14, 1 << 15, 1 << 16, 1 << 17)
+
+
 class GroupedRound:
+    """`item`: elements per work item, a power of two in [2^10, 2^24], or
+    "auto" to time ITEM_CANDIDATES on these tensors and keep the fastest
+    (cached per problem signature, like GroupedGemm's schedule)."""
+
     def __init__(self, ins, outs, formats, modes, stoch_lens=None, scales=None, seeds=None,
-                 offsets=None):
+                 offsets=None, item=1 << 16, tune_reps: int = 3):
         n = len(ins)
         if not (len(outs) == len(formats) == len(modes) == n):
             raise ValueError("ins, outs, formats and modes must have the same length")
@@ -52,17 +60,48 @@ class GroupedRound:
                                       f.c_format, int(modes[i]), int(stoch_lens[i]),
                                       float(scales[i]), 0, int(seeds[i]) & ((1 << 64) - 1),
                                       int(offsets[i]))
+        self._tasks = tasks
+        self.ntasks = n
+        self.bytes = sum(8 * x.numel() for x in ins)
+        self.graph = None
+        self.tuning_ms = {}
+        if item == "auto":
+            sig = round_signature([(int(x.numel()), int(m)) for x, m in zip(ins, modes)])
+            cached = _load_cache().get(sig)
+            if cached and cached.get("item") in ITEM_CANDIDATES:
+                item = int(cached["item"])
+            else:
+                for cand in ITEM_CANDIDATES:
+                    self._prepare(cand)
+                    self.tuning_ms[cand] = self._time(tune_reps)
+                item = min(self.tuning_ms, key=self.tuning_ms.get)
+                _store_cache(sig, {"item": item, "ms": self.tuning_ms})
+        self._prepare(int(item))
+
+    def _prepare(self, item: int) -> None:
         L = _native.lib()
+        n = self.ntasks
         nbytes = int(L.lofgb_round_grouped_table_size(n))
         host = np.zeros(max(nbytes, 1), np.uint8)
         items = C.c_int64(0)
-        check(L.lofgb_round_grouped_prepare(tasks, n, host.ctypes.data_as(C.c_void_p), nbytes,
-                                            C.byref(items)), "grouped_round_prepare")
-        self.ntasks = n
+        check(L.lofgb_round_grouped_prepare_items(self._tasks, n, host.ctypes.data_as(C.c_void_p),
+                                                  nbytes, int(item), C.byref(items)),
+              "grouped_round_prepare")
+        self.item = int(item)
         self.num_items = int(items.value)
-        self.table = torch.from_numpy(host).to(dev)  # caching allocator: 512-byte aligned
-        self.bytes = sum(8 * x.numel() for x in ins)
+        self.table = torch.from_numpy(host).to(self.device)  # caching allocator: 512-byte aligned
         self.graph = None
+
+    def _time(self, reps: int) -> float:
+        self()
+        torch.cuda.synchronize(self.device)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(reps):
+            self()
+        e.record()
+        torch.cuda.synchronize(self.device)
+        return s.elapsed_time(e) / reps
 
     def __call__(self):
         with torch.cuda.device(self.device):

@@ -207,6 +207,12 @@ def test_grouped_prepare_host_only():
     assert L.lofgb_round_grouped_prepare(bad, 1, buf, nbytes, C.byref(items)) == -3
     assert "task 0" in L.lofgb_last_error_detail().decode()
     assert L.lofgb_round_grouped_f32(None, 0, 0, None) == 0
+    # work items of a chosen power-of-two size
+    for item, want in ((1 << 14, 5 + 1), (1 << 17, 1 + 1), (1 << 10, 69 + 1)):
+        assert L.lofgb_round_grouped_prepare_items(tasks, 3, buf, nbytes, item, C.byref(items)) == 0
+        assert items.value == want
+    for item in (3000, 512, 1 << 25):
+        assert L.lofgb_round_grouped_prepare_items(tasks, 3, buf, nbytes, item, C.byref(items)) != 0
 
 
 def test_grouped_gemm_validation_host_only():

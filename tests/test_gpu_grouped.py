@@ -70,3 +70,24 @@ def test_grouped_single_task_equals_virtual_round():
     lg.GroupedRound([x], [y], [f], [3], stoch_lens=[8], seeds=[5])()
     ref = lg.virtual_round(x, f, round_mode=3, stoch_len=8, seed=5, offset=0)
     assert torch.equal(y, ref)
+
+
+@pytest.mark.parametrize("item", [1 << 10, 1 << 14, 1 << 17, "auto"])
+def test_grouped_item_sizes(item, tmp_path, monkeypatch):
+    """Any work-item size (and the timed choice) gives the oracle's bits."""
+    monkeypatch.setattr(lg.autotune, "CACHE_PATH", str(tmp_path / "tune.json"))
+    xs, fmts, modes, lens, seeds = _random_tasks(48, 3)
+    ins = [torch.from_numpy(x).cuda() for x in xs]
+    outs = [torch.empty_like(t) for t in ins]
+    g = lg.GroupedRound(ins, outs, fmts, modes, stoch_lens=lens, seeds=seeds, item=item)
+    if item == "auto":
+        assert g.item in lg.grouped.ITEM_CANDIDATES and len(g.tuning_ms) == 4
+        again = lg.GroupedRound(ins, outs, fmts, modes, stoch_lens=lens, seeds=seeds, item="auto")
+        assert again.item == g.item and again.tuning_ms == {}   # from the cache
+    for o in outs:
+        o.zero_()
+    g()
+    torch.cuda.synchronize()
+    for i, x in enumerate(xs):
+        want = O.round(x, ofmt(fmts[i]), modes[i], lens[i], seed=seeds[i], offset=0)
+        assert same_bits(outs[i].cpu().numpy(), want), i
