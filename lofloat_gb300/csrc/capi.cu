@@ -187,6 +187,8 @@ int make_round_plan(RoundPlan* p, const lofgb_format* f, int src_bits, int mode,
         p->uni_d = (uint32_t)p->d << 23;
     }
     if (uni_ok && p->grid != 0) p->uni = p->grid;
+    // round-to-odd on the same grid (vr_uni_rto_f32): needs the subnormal grid constant
+    if (uni_ok && mode == LOFGB_RTO && p->grid_c > 0.0f) p->uni = 6;
     // tiny * 2^-len normal: (to_min - m) - len >= -126
     p->sr_uni = 0;
     if (uni_ok && mode == LOFGB_SR_A && len <= p->d && len <= 23 && gexp - len >= -126 &&

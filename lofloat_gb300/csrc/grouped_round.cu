@@ -69,6 +69,9 @@ __device__ void run_item(const GroupedTask& t, int64_t e0, int64_t e1, uint4 (*r
             if constexpr (UNI == 3) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) w[q] = vr_uni_sra_f32(w[q], t.plan, r[q]);
+            } else if constexpr (UNI == 6) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) w[q] = vr_uni_rto_f32(w[q], t.plan);
             } else if constexpr (UNI != 0) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) w[q] = vr_uni_f32<MODE, UNI>(w[q], t.plan);
@@ -109,7 +112,8 @@ grouped_round_kernel(const GroupedTask* __restrict__ tasks, int ntasks, int64_t 
         __syncthreads();
         const int64_t e0 = (item - t.item_begin) << t.item_shift;
         const int64_t e1 = min(e0 + ((int64_t)1 << t.item_shift), t.n);
-        // uni is 1 only for RNE and 2 only for RTZ / RAFZ / RU / RD; sr_uni only for SR-A
+        // uni is 1 only for RNE, 2 only for RTZ / RAFZ / RU / RD, 6 only for
+        // round-to-odd; sr_uni only for SR-A
         switch (t.plan.mode) {
         case LOFGB_RNE:
             if (t.plan.uni) run_item<LOFGB_RNE, 1>(t, e0, e1, ring);
@@ -119,7 +123,10 @@ grouped_round_kernel(const GroupedTask* __restrict__ tasks, int ntasks, int64_t 
             if (t.plan.uni) run_item<LOFGB_RTZ, 2>(t, e0, e1, ring);
             else run_item<LOFGB_RTZ, 0>(t, e0, e1, ring);
             break;
-        case LOFGB_RTO: run_item<LOFGB_RTO, 0>(t, e0, e1, ring); break;
+        case LOFGB_RTO:
+            if (t.plan.uni == 6) run_item<LOFGB_RTO, 6>(t, e0, e1, ring);
+            else run_item<LOFGB_RTO, 0>(t, e0, e1, ring);
+            break;
         case LOFGB_SR_A:
             if (t.plan.sr_uni) run_item<LOFGB_SR_A, 3>(t, e0, e1, ring);
             else run_item<LOFGB_SR_A, 0>(t, e0, e1, ring);

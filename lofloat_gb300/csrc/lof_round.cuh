@@ -454,6 +454,30 @@ __device__ __forceinline__ uint32_t vr_uni_f32(uint32_t x, const RoundPlan& p) {
     return (x & 0x7FFFFFFFu) > 0x7F800000u ? 0x7FC00000u : res;
 }
 
+// virtual_round(x, params, {RoundToOdd}) of an f32 word on the float grid
+// (RoundPlan::uni == 6): t = fadd_rz(|x|, C) - C truncates |x| onto the
+// target's grid; the reference's RoundToOdd ORs the target's last place into
+// the truncated word when any dropped bit was set (src/lo_float.h:1203-1229).
+// At or above the target's smallest normal that place is FP32 bit d of t; below
+// it the grid is the multiples of tiny and t + Csub (Csub = 2^23 tiny, exact)
+// holds t / tiny in its low bits, so the OR happens there and Csub comes off
+// again exactly. The tiny branch (|x| < tiny gives tiny when |x| > 0) is the
+// same formula with t = 0.
+__device__ __forceinline__ uint32_t vr_uni_rto_f32(uint32_t x, const RoundPlan& p) {
+    const uint32_t mag = x & 0x7FFFFFFFu;
+    const uint32_t cb = min(max(x & 0x7F800000u, p.uni_lo), p.uni_hi) + p.uni_d;
+    const float c = __uint_as_float(cb);
+    const float a = __uint_as_float(mag);
+    const float t = __fsub_rn(__fadd_rz(a, c), c);
+    const uint32_t inexact = t != a ? 1u : 0u;
+    const uint32_t vs = __float_as_uint(
+        __fsub_rn(__uint_as_float(__float_as_uint(__fadd_rn(t, p.grid_c)) | inexact), p.grid_c));
+    const uint32_t v = mag >= (uint32_t)p.norm_thr ? (__float_as_uint(t) | (inexact << p.d)) : vs;
+    uint32_t res = v | (x & 0x80000000u);
+    res = v >= (uint32_t)p.ovf_thr ? ((x & p.sat_and) | p.sat_or) : res;
+    return mag > 0x7F800000u ? 0x7FC00000u : res;
+}
+
 // vr_uni_f32<RNE, 1> for a saturating format, whose overflow returns the
 // input word: a NaN input rounds to a NaN word, above every overflow
 // threshold, and so comes back as the input NaN rather than the canonical

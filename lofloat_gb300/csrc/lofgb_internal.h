@@ -56,6 +56,7 @@ struct RoundPlan {
     // target-subnormal branch) and hi + d <= 254 with hi the FP32 exponent
     // field just above the target's largest finite value (every |x| at or
     // above 2^hi then still rounds to an overflow).
+    // uni == 6: round-to-odd on the same grid (vr_uni_rto_f32).
     int32_t uni;
     uint32_t uni_lo, uni_hi, uni_d;  // FP32 exponent fields, shifted to bit 23
     uint32_t sat_and, sat_or;        // overflow result: (x & sat_and) | sat_or

@@ -83,6 +83,14 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
                 w[q] = vr_uni_sra_f32<UNI == 5>(w[q], p, r[q]);
             }
             o = make_uint4(w[0], w[1], w[2], w[3]);
+        } else if constexpr (W == 32 && FMT && UNI == 6) {
+            uint32_t w[4] = {vv.x, vv.y, vv.z, vv.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (SCALED) w[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(w[q])));
+                w[q] = vr_uni_rto_f32(w[q], p);
+            }
+            o = make_uint4(w[0], w[1], w[2], w[3]);
         } else if constexpr (W == 32 && FMT && UNI != 0) {
             uint32_t w[4] = {vv.x, vv.y, vv.z, vv.w};
 #pragma unroll
@@ -239,6 +247,10 @@ int launch_w(const void* in, void* out, int64_t n, const RoundPlan& p, const Sca
         if (p.uni == 2) {
             if (p.mode == LOFGB_RTZ) LOFGB_RVU(LOFGB_RTZ, 2);
             else LOFGB_RVU(-1, 2);
+            return check_launch("round_vec_kernel");
+        }
+        if (p.uni == 6) {
+            LOFGB_RVU(LOFGB_RTO, 6);
             return check_launch("round_vec_kernel");
         }
         if (p.sr_uni) {
