@@ -4,7 +4,13 @@
 // run one thread per group, stage the group in a 64-float local array and
 // set or read the code bits one at a time through byte read-modify-writes.
 //
-// Here a warp owns a tile of 1024 consecutive values (32 per lane). A tile is
+// Fast paths (RNE encode on the float grid, direct-bits decode, 16-byte
+// aligned float buffers): a thread converts G = lcm(n, 32) / n consecutive
+// values to lcm(n, 32) / 32 whole words and back, with no staging (n = 4, 8,
+// 16: one float4 per thread; the direct encode streams its inputs through a
+// per-thread cp.async ring). Everything else takes the staged kernels below.
+//
+// Staged kernels: a warp owns a tile of 1024 consecutive values (32 per lane). A tile is
 // always a whole number of groups (32 n bits hold 4 gcd(n, 8) or 2 gcd(n, 16)
 // groups), so every lane packs its 32 codes into exactly n 32-bit words on its
 // own, with no cross-lane bit exchange. FP32 values and packed words move

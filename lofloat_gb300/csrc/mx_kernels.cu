@@ -15,6 +15,10 @@
 // When the scale is a power of two in [2^-126, 2^127] the quotient is taken
 // as x * (1/scale), which is bit-identical to the IEEE division (both are one
 // rounding of the same exact value); other scales use __fdiv_rn.
+// Inputs stream through a per-thread cp.async ring; scales are rounded once
+// per (slot, block) pair and shuffled back; RNE elements round on the float
+// grid (a saturating element format with block 32 folds the NaN case into the
+// overflow select). Launched with programmatic dependent launch.
 #include <cuda_runtime.h>
 
 #include "lof_round.cuh"

@@ -5,9 +5,13 @@
 // (src/Lof_kernel.cu:37-60): those launch one element per thread with scalar
 // loads and, for the format overload, round in place on a clone of the input.
 // Here each thread moves 16-byte vectors (4 f32, 2 f64 or 8 f16 values), RU of
-// them in flight per iteration, over a grid-stride loop sized to the SM count;
-// the output is written out of place (in == out also works). HBM-bound:
-// 2 * sizeof(T) algorithmic bytes per element.
+// them per iteration, over a grid-stride loop sized to the SM count; the next
+// iterations' vectors stream into a per-thread cp.async ring in shared memory
+// while the current one is rounded. f32 sources in RNE, the directed modes,
+// round-to-odd and SR-A round on the float grid (lof_round.cuh vr_uni_*); the
+// other modes and sources take the integer rounding core. Launched with
+// programmatic dependent launch. The output is written out of place (in ==
+// out also works). HBM-bound: 2 * sizeof(T) algorithmic bytes per element.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
