@@ -218,3 +218,31 @@ def test_errors_raise():
         lg.virtual_round(torch.ones(4, device="cuda"), bad)
     with pytest.raises(RuntimeError):
         lg.virtual_round(torch.ones(4, device="cuda"), desc, round_mode=99)
+
+
+def _grid_neighbourhood(desc):
+    """Every finite value of a small format, its FP32 neighbours and the
+    midpoints between consecutive values, both signs, plus values below the
+    smallest subnormal and above the largest finite value."""
+    f = ofmt(desc)
+    probe = np.arange(1 << 20, dtype=np.uint32).astype(np.float32) * np.float32(2.0 ** -12)
+    vals = np.unique(O.round(np.concatenate([probe, probe * 2.0 ** -20, probe * 2.0 ** 12]), f, 0))
+    vals = vals[np.isfinite(vals)]
+    mids = (vals[:-1].astype(np.float64) + vals[1:]) / 2
+    around = np.concatenate([vals, mids.astype(np.float32), np.nextafter(vals, np.float32(np.inf)),
+                             np.nextafter(vals, np.float32(-np.inf)),
+                             np.float32([1e-45, 1e-40, 1e-30, 3e38, np.inf, np.nan])])
+    return np.concatenate([around, -around]).astype(np.float32)
+
+
+@pytest.mark.parametrize("fmt", [(8, 3, 7, True, True), (8, 2, 15, False, True), (4, 1, 1, True, True),
+                                 (6, 3, 1, True, True), (16, 10, 15, False, True)])
+@pytest.mark.parametrize("mode", [1, 2, 5, 6, 12])
+def test_float_grid_modes_at_grid_points(fmt, mode):
+    """The float-grid paths (directed modes, round-to-odd) at and next to
+    every grid point, at the subnormal edge and past the overflow edge."""
+    desc = _desc(fmt)
+    x = _grid_neighbourhood(desc)
+    got = from_gpu(lg.virtual_round(to_gpu(x), desc, round_mode=mode))
+    want = O.round(x, ofmt(desc), mode, 0)
+    assert same_bits(got, want), mismatch_report(x, got, want)
