@@ -53,6 +53,7 @@ struct CodecArg {
     uint32_t code_off;        // normal code = (bits >> (23 - m)) - code_off
     float sub_c;              // 2^23 * tiny: subnormal code = bits(v + sub_c) - bits(sub_c)
     uint32_t max_finite, ovf_code, inf_code, neg_zero_code, neg_code, sign_mask;
+    uint32_t neg_keep, neg_or, neg_zero;  // a negative finite code: code ? (code & keep) | or : zero
     // Fast decode: every finite value is a normal FP32 number or an exact
     // FP32 subnormal, so the bits are built directly.
     int dec_fast;
@@ -180,9 +181,15 @@ __device__ __forceinline__ uint32_t codec_encode_fast(float from, const CodecArg
     uint32_t code = vb >= a.min_norm_bits ? (vb >> (23 - a.m)) - a.code_off
                                           : __float_as_uint(__fadd_rn(v, a.sub_c)) - __float_as_uint(a.sub_c);
     code = min(code, a.ovf_code);
-    if (SPECIAL) code = mb == 0x7F800000u ? a.inf_code : code;
+    if (!SPECIAL) {
+        // finite input: the sign rules of both signednesses in one form
+        // (signed: -0 -> neg_zero_code, else code | sign; unsigned: neg_code)
+        const uint32_t ns = code == 0u ? a.neg_zero : ((code & a.neg_keep) | a.neg_or);
+        return neg ? ns : code;
+    }
+    code = mb == 0x7F800000u ? a.inf_code : code;
     code = (neg && a.is_signed) ? (code == 0u ? a.neg_zero_code : (code | a.sign_mask)) : code;
-    if (SPECIAL) code = mb > 0x7F800000u ? a.qnan : code;
+    code = mb > 0x7F800000u ? a.qnan : code;
     return (neg && !a.is_signed) ? a.neg_code : code;
 }
 
@@ -732,6 +739,9 @@ int make_codec_arg(CodecArg* a, const lofgb_codec_format* f, int mode, int sat, 
         else if (a->nan_kind == LOFGB_NAN_IEEE) sign_only_nan = false;  // magnitude 0
     }
     a->neg_zero_code = sign_only_nan ? 0u : a->sign_mask;
+    a->neg_keep = a->is_signed ? 0xFFFFFFFFu : 0u;
+    a->neg_or = a->is_signed ? a->sign_mask : a->neg_code;
+    a->neg_zero = a->is_signed ? a->neg_zero_code : a->neg_code;
     const bool narrower = to_max < 128 || (to_max == 128 && m + 1 < 24);
     const int d = 23 - m;
     const int hi = to_max + 1 + 127;
