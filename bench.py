@@ -142,6 +142,22 @@ def dist_setup(args):
     return world, rank, local
 
 
+def max_over_ranks(dist, seconds, device):
+    """Every rank's timings replaced by the slowest rank's, element by element
+    (one all-reduce of a float64 vector on `device`: the rank's GPU under
+    NCCL, the CPU under gloo)."""
+    import torch
+    t = torch.tensor(list(seconds), device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def whole_job_gbs(world, steps, step_bytes, seconds):
+    """Whole-job throughput of `world` replicas that each processed `steps`
+    steps of `step_bytes` algorithmic bytes in `seconds` (the max over ranks)."""
+    return world * steps * step_bytes / seconds / 1e9
+
+
 def config2_input(torch, dev):
     g = torch.Generator().manual_seed(2)
     x = torch.randn(MX_ROWS * MX_COLS, generator=g, dtype=torch.float32)
@@ -635,16 +651,14 @@ def run_ours(args, world, rank, local):
     clk = clocks.stop()
 
     if dist:
-        t = torch.tensor([elapsed, e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed, e2e_s = float(t[0]), float(t[1])
+        elapsed, e2e_s = max_over_ranks(dist, [elapsed, e2e_s], dev)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
 
     step_bytes = len(efs) * MX_BYTES
-    value = world * args.steps * step_bytes / elapsed / 1e9
+    value = whole_job_gbs(world, args.steps, step_bytes, elapsed)
     achieved = MX_BYTES / per_launch / 1e9
     traffic = profile_traffic("mx_kernel_8192x8192.md")
     line = {
@@ -660,7 +674,7 @@ def run_ours(args, world, rank, local):
                      "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
                      "traffic": traffic, "peak_source": f"{peak_src} hbm_gbs",
                      "kernel": "mx_kernel<32,RNE,RNE>", "algorithmic_bytes_per_launch": MX_BYTES},
-        "e2e": {"value": round(world * e2e_steps * step_bytes / e2e_s / 1e9, 2), "unit": "GB/s",
+        "e2e": {"value": round(whole_job_gbs(world, e2e_steps, step_bytes, e2e_s), 2), "unit": "GB/s",
                 "h2d_bytes_per_step": MX_ROWS * MX_COLS * 4,
                 "d2h_bytes_per_step": len(efs) * MX_ROWS * MX_COLS * 4,
                 "api": "lofloat_gb300.virtual_mx_round (C ABI lofgb_mx_round_f32)"},
