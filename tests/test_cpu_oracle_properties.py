@@ -1,0 +1,167 @@
+"""Properties of the oracle, as the reference's own test programs check them.
+
+The golden vectors pin the oracle to the compiled reference on fixed cases;
+these tests check the properties that the reference's tests assert on random
+and constructed inputs, with expectations built independently here from the
+bit pattern (truncate, step one grid point):
+
+* `test/test_virtual_round.cu:178-227`: directed modes are one-sided and
+  within one grid step; nearest modes are within half a step
+  (inputs u·2^[-20,20] as `rnd32_wide`, `:93-98`; mantissa widths 7/10/15,
+  `:687-689`);
+* `:233-307`: exact ties go to even (RNE), to odd (RNO), away from zero (RTA);
+* `:312-360`: stochastic modes with len 8 give RD or RU;
+* `test/test_prob_round.cpp`: P(up) within 0.02 of its expectation;
+* `test/test_virtual_mx_round_cuda.cu:155-172`: an all-zero block gives 0,
+  not NaN; `:94`: lengths with a trailing partial block;
+* `test/test_mx_round_py.py:33-38`: exactly representable blocks come back
+  unchanged.
+"""
+import numpy as np
+import pytest
+
+O = pytest.importorskip("oracle.oracle")
+
+RNE, RTZ, RAFZ, SRA, RNO, RD, RU, RTA, SRB, SRC, TSR, PROB, RTO, RTTZ, SRD = range(15)
+
+
+def wide_inputs(n, seed):
+    """u·2^e with u uniform in [1, 2) (random sign) and e in [-20, 20]."""
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(1.0, 2.0, n) * rng.choice([-1.0, 1.0], n)
+    return (u * np.exp2(rng.integers(-20, 21, n))).astype(np.float32)
+
+
+def neighbours(x, mbits):
+    """(toward-zero, away-from-zero) grid neighbours at `mbits` fraction bits,
+    as f32, and whether x is already on the grid."""
+    b = x.view(np.uint32)
+    sign = b & np.uint32(0x80000000)
+    mag = b & np.uint32(0x7FFFFFFF)
+    step = np.uint32(1 << (23 - mbits))
+    tz = mag & ~np.uint32(step - 1)
+    exact = tz == mag
+    az = np.where(exact, tz, tz + step)
+    return (tz | sign).view(np.float32), (az | sign).view(np.float32), exact
+
+
+def kept_lsb(y, mbits):
+    return (y.view(np.uint32) >> np.uint32(23 - mbits)) & np.uint32(1)
+
+
+@pytest.mark.parametrize("mbits", [7, 10, 15])
+def test_directed_and_nearest_bounds(mbits):
+    x = wide_inputs(1 << 16, 100 + mbits)
+    tz, az, exact = neighbours(x, mbits)
+    neg = x < 0
+    rd = np.where(neg, az, tz)
+    ru = np.where(neg, tz, az)
+    eq = lambda a, b: np.array_equal(a.view(np.uint32), b.view(np.uint32))  # noqa: E731
+    assert eq(O.round_mantissa(x, mbits, RTZ), tz)
+    assert eq(O.round_mantissa(x, mbits, RAFZ), az)
+    assert eq(O.round_mantissa(x, mbits, RD), rd)
+    assert eq(O.round_mantissa(x, mbits, RU), ru)
+    # round to odd: exact stays, otherwise the neighbour with the odd last bit
+    rto = np.where(exact, x, np.where(kept_lsb(tz, mbits) == 1, tz, az))
+    assert eq(O.round_mantissa(x, mbits, RTO), rto)
+    # nearest modes: within half a step, and the nearer neighbour off ties
+    x64 = x.astype(np.float64)
+    dz, da = np.abs(x64 - tz), np.abs(az.astype(np.float64) - x64)
+    half = (az.astype(np.float64) - tz.astype(np.float64)) / 2
+    for mode in (RNE, RNO, RTA, RTTZ):
+        y = O.round_mantissa(x, mbits, mode)
+        assert np.all(np.abs(y.astype(np.float64) - x64) <= np.abs(half) + 0.0)
+        off_tie = dz != da
+        nearer = np.where(dz < da, tz, az)
+        assert eq(y[off_tie], nearer[off_tie]), mode
+
+
+@pytest.mark.parametrize("mbits", [7, 10, 15])
+def test_exact_ties(mbits):
+    rng = np.random.default_rng(7 + mbits)
+    n = 4096
+    exp = rng.integers(100, 160, n).astype(np.uint32)
+    frac = rng.integers(0, 1 << mbits, n).astype(np.uint32)
+    drop = 23 - mbits
+    # kept bits, then exactly half a step below them: a tie
+    bits = (exp << np.uint32(23)) | (frac << np.uint32(drop)) | np.uint32(1 << (drop - 1))
+    bits |= rng.choice(np.array([0, 0x80000000], np.uint32), n)
+    x = bits.view(np.float32)
+    tz, az, _ = neighbours(x, mbits)
+    eq = lambda a, b: np.array_equal(a.view(np.uint32), b.view(np.uint32))  # noqa: E731
+    even = np.where(kept_lsb(tz, mbits) == 0, tz, az)
+    odd = np.where(kept_lsb(tz, mbits) == 1, tz, az)
+    assert eq(O.round_mantissa(x, mbits, RNE), even)
+    assert eq(O.round_mantissa(x, mbits, RNO), odd)
+    assert eq(O.round_mantissa(x, mbits, RTA), az)
+    assert eq(O.round_mantissa(x, mbits, RTTZ), tz)
+
+
+@pytest.mark.parametrize("mode", [SRA, SRB, SRC, SRD, TSR, PROB])
+def test_stochastic_gives_a_neighbour(mode):
+    mbits = 10
+    x = wide_inputs(1 << 15, 31)
+    tz, az, exact = neighbours(x, mbits)
+    y = O.round_mantissa(x, mbits, mode, stoch_len=8, seed=5)
+    yb, tb, ab = (v.view(np.uint32) for v in (y, tz, az))
+    inexact = ~exact
+    assert np.all((yb[inexact] == tb[inexact]) | (yb[inexact] == ab[inexact]))
+    if mode in (SRA, SRB, TSR, PROB):
+        assert np.array_equal(yb[exact], x.view(np.uint32)[exact])
+
+
+@pytest.mark.parametrize("mode", [SRA, TSR])
+def test_probability_of_rounding_up(mode):
+    # 1.0 plus five 10-bit steps plus a tail of 80/256 of a step (13 dropped bits)
+    mbits, n = 10, 200_000
+    b = np.uint32(0x3F800000 + 5 * (1 << 13) + (80 << 5))
+    x = np.full(n, b, np.uint32).view(np.float32)
+    tz, az, _ = neighbours(x, mbits)
+    y = O.round_mantissa(x, mbits, mode, stoch_len=8, seed=123)
+    up = np.mean(y.view(np.uint32) == az.view(np.uint32))
+    assert np.all((y == tz) | (y == az))
+    assert abs(up - 80 / 256) < 0.02
+
+
+E4M3 = (8, 3, 7)
+E8M0 = dict(saturating=False, signed=False)
+
+
+def test_mx_all_zero_block_is_zero():
+    x = np.zeros(96, np.float32)
+    x[32:64] = np.linspace(-3, 3, 32, dtype=np.float32)
+    y = O.mx_round(x, 32, O.fmt(*E4M3), O.fmt(8, 0, 127, **E8M0))
+    assert not np.any(np.isnan(y))
+    assert np.all(y[:32].view(np.uint32) == 0) and np.all(y[64:].view(np.uint32) == 0)
+
+
+@pytest.mark.parametrize("block", [8, 16, 32, 64, 128, 256])
+def test_mx_trailing_partial_block_equals_zero_padding(block):
+    ef, sf = O.fmt(*E4M3), O.fmt(8, 0, 127, **E8M0)
+    rng = np.random.default_rng(block)
+    for n in (block, 3 * block, 3 * block + 1, 1000, 4096, 5003):
+        x = rng.standard_normal(n).astype(np.float32)
+        pad = -(-n // block) * block
+        xp = np.zeros(pad, np.float32)
+        xp[:n] = x
+        y = O.mx_round(x, block, ef, sf)
+        yp = O.mx_round(xp, block, ef, sf)
+        assert np.array_equal(y.view(np.uint32), yp[:n].view(np.uint32)), n
+
+
+def test_mx_representable_blocks_round_trip():
+    # E4M3 (8,3,7) grid values, each block holding the format's largest value
+    # 1.875·2^8 scaled by a power of two, so that the E8M0 scale is exact
+    ef, sf = O.fmt(*E4M3), O.fmt(8, 0, 127, **E8M0)
+    rng = np.random.default_rng(3)
+    nblk, block = 64, 32
+    m = rng.integers(0, 8, (nblk, block))
+    e = rng.integers(-6, 9, (nblk, block))
+    m[e == 8] = np.minimum(m[e == 8], 7)
+    v = (1 + m / 8.0) * np.exp2(e) * rng.choice([-1.0, 1.0], (nblk, block))
+    v[:, 0] = 1.875 * 256.0
+    k = rng.integers(-20, 21, (nblk, 1))
+    x = (v * np.exp2(k)).astype(np.float32).reshape(-1)
+    for mode in (RNE, RTZ, RD, RU):
+        y = O.mx_round(x, block, ef, sf, mode=mode)
+        assert np.array_equal(y.view(np.uint32), x.view(np.uint32)), mode
