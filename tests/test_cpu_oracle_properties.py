@@ -15,7 +15,10 @@ bit pattern (truncate, step one grid point):
 * `test/test_virtual_mx_round_cuda.cu:155-172`: an all-zero block gives 0,
   not NaN; `:94`: lengths with a trailing partial block;
 * `test/test_mx_round_py.py:33-38`: exactly representable blocks come back
-  unchanged.
+  unchanged;
+* `test/test_virtual_mx_round.cpp` (P3109 <l,p> sweep, l = 2..8): the block
+  scale is the nearer E8M0 power of two of amax/pmn, and every element over
+  that scale is the element format's rounding of x/scale.
 """
 import numpy as np
 import pytest
@@ -165,3 +168,44 @@ def test_mx_representable_blocks_round_trip():
     for mode in (RNE, RTZ, RD, RU):
         y = O.mx_round(x, block, ef, sf, mode=mode)
         assert np.array_equal(y.view(np.uint32), x.view(np.uint32)), mode
+
+
+def _nearer_pow2(q):
+    """The nearer of the two powers of two around q > 0 (None on an exact tie)."""
+    lo = np.float32(2.0) ** np.floor(np.log2(np.float64(q)))
+    lo = np.float32(lo)
+    if q == lo:
+        return lo
+    hi = np.float32(lo * 2)
+    if q - lo == hi - q:
+        return None
+    return lo if q - lo < hi - q else hi
+
+
+@pytest.mark.parametrize("l", range(2, 9))
+def test_mx_p3109_sweep_scale_and_elements(l):
+    """test/test_virtual_mx_round.cpp's P3109 <l,p> sweep (l = 2..8,
+    p = 1..l-1): the block scale is the nearer E8M0 power of two of
+    amax·(1/pmn), and each element, divided by that scale, is the element
+    format's own rounding of x/scale."""
+    sf = O.fmt(8, 0, 127, **E8M0)
+    rng = np.random.default_rng(40 + l)
+    nblk, block = 16, 32
+    x = (rng.standard_normal((nblk, block))
+         * np.exp2(rng.integers(-8, 9, (nblk, 1)))).astype(np.float32)
+    for p in range(1, l):
+        bias = 1 << (l - p - 1)
+        ef = O.fmt(l, p - 1, bias)
+        me = (1 << (l - (p - 1) - 1)) - 1 - bias
+        pmn = np.float32(np.ldexp(1.0, me) * (2.0 - np.ldexp(1.0, -(p - 1))))
+        inv = np.float32(1.0) / pmn
+        for mode in (RNE, RTZ, RD, RU, RAFZ):
+            y = O.mx_round(x.reshape(-1), block, ef, sf, mode=mode).reshape(nblk, block)
+            for b in range(nblk):
+                amax = np.float32(np.max(np.abs(x[b])))
+                s = _nearer_pow2(np.float32(amax * inv))
+                if s is None:
+                    continue
+                z = O.round((x[b] / s).astype(np.float32), ef, mode)
+                got = (y[b] / s).astype(np.float32)
+                assert np.array_equal(got.view(np.uint32), z.view(np.uint32)), (l, p, mode, b)
