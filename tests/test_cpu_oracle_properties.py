@@ -18,7 +18,10 @@ bit pattern (truncate, step one grid point):
   unchanged;
 * `test/test_virtual_mx_round.cpp` (P3109 <l,p> sweep, l = 2..8): the block
   scale is the nearer E8M0 power of two of amax/pmn, and every element over
-  that scale is the element format's rounding of x/scale.
+  that scale is the element format's rounding of x/scale;
+* `test/test_blis_lof_accum.cpp:126-235`: the emulated GEMM within
+  γ_K·|A||B| of the FP64 product, measurably less accurate than FP32, and
+  exact where every partial sum is representable.
 """
 import numpy as np
 import pytest
@@ -209,3 +212,31 @@ def test_mx_p3109_sweep_scale_and_elements(l):
                 z = O.round((x[b] / s).astype(np.float32), ef, mode)
                 got = (y[b] / s).astype(np.float32)
                 assert np.array_equal(got.view(np.uint32), z.view(np.uint32)), (l, p, mode, b)
+
+
+def test_gemm_accumulation_bound_grid_and_exact_case():
+    """test/test_blis_lof_accum.cpp on the emulated GEMM: error within
+    γ_K·|A||B| of the FP64 product with a 10-bit accumulator (part 1); the
+    low-precision accumulator is engaged, far less accurate than FP32 and
+    every output on its grid (part 2); products whose partial sums are all
+    representable give the exact result (part 3)."""
+    rng = np.random.default_rng(13)
+    M, N, K, mbits = 32, 32, 64, 10
+    A = (rng.random((M, K)) - 0.5).astype(np.float32)
+    B = (rng.random((K, N)) - 0.5).astype(np.float32)
+    exact = A.astype(np.float64) @ B.astype(np.float64)
+    absab = np.abs(A.astype(np.float64)) @ np.abs(B.astype(np.float64))
+    keps = K * 2.0 ** -mbits
+    gamma = keps / (1 - keps)
+    D = O.gemm(A, B, mbits)
+    err = np.abs(D.astype(np.float64) - exact)
+    assert np.all(err <= gamma * absab)
+    err32 = np.abs((A @ B).astype(np.float64) - exact).max()
+    assert err.max() > 50 * err32 and err.max() > 1e-4
+    low = D.view(np.uint32) & np.uint32((1 << (23 - mbits)) - 1)
+    assert np.all(low == 0)
+    # small integers: every partial sum is an integer below 2^11, exact at 10 bits
+    Ai = rng.integers(-3, 4, (M, K)).astype(np.float32)
+    Bi = rng.integers(-3, 4, (K, N)).astype(np.float32)
+    Di = O.gemm(Ai, Bi, mbits)
+    assert np.array_equal(Di, (Ai.astype(np.float64) @ Bi.astype(np.float64)).astype(np.float32))
