@@ -21,7 +21,11 @@ bit pattern (truncate, step one grid point):
   that scale is the element format's rounding of x/scale;
 * `test/test_blis_lof_accum.cpp:126-235`: the emulated GEMM within
   γ_K·|A||B| of the FP64 product, measurably less accurate than FP32, and
-  exact where every partial sum is representable.
+  exact where every partial sum is representable;
+* `test/test_pack.cpp`: packed byte counts from an lcm formula, every code of
+  the small P3109 formats round-tripping through the packed form in both
+  byte orders with a partial group, and float round trips equal to the
+  format's rounding.
 """
 import numpy as np
 import pytest
@@ -240,3 +244,63 @@ def test_gemm_accumulation_bound_grid_and_exact_case():
     Bi = rng.integers(-3, 4, (K, N)).astype(np.float32)
     Di = O.gemm(Ai, Bi, mbits)
     assert np.array_equal(Di, (Ai.astype(np.float64) @ Bi.astype(np.float64)).astype(np.float32))
+
+
+def _group(n):
+    """Codes per group and bytes per group: lcm(n, 8) bits up to 8-bit codes,
+    lcm(n, 16) above, computed here independently of the codec."""
+    from math import lcm
+    bits = lcm(n, 8 if n <= 8 else 16)
+    return bits // n, bits // 8
+
+
+def test_codec_packed_sizes():
+    """test/test_pack.cpp:31-38: byte counts against an lcm formula."""
+    for n in range(1, 17):
+        gc, gb = _group(n)
+        for count in list(range(0, 70)) + [1000, 4097]:
+            assert O.packed_size(n, count) == -(-count // gc) * gb, (n, count)
+
+
+P3109_SMALL = [(k, p, sat) for k in range(3, 9) for p in range(1, k) for sat in (True, False)]
+
+
+@pytest.mark.parametrize("k,p,sat", P3109_SMALL)
+def test_codec_every_rep_round_trips(k, p, sat):
+    """test/test_pack.cpp:7-12: decode then encode gives back every non-NaN
+    code, through the packed form in both byte orders and with a partial
+    group at the end."""
+    f = O.codec_p3109(k, p, saturating=sat)
+    reps = np.arange(1 << k)
+    vals = np.array([O.decode_rep(int(r), f) for r in reps], np.float32)
+    finite = ~np.isnan(vals)
+    back = np.array([O.encode_rep(float(v), f) for v in vals[finite]])
+    assert np.array_equal(back, reps[finite])
+    assert np.isnan(O.decode_rep(O.encode_rep(float("nan"), f), f))
+    gc, _ = _group(k)
+    x = vals[finite]
+    x = np.concatenate([x, x[: gc + 1]]) if gc > 1 else x
+    for rev in (0, 1):
+        packed = O.encode(x, f, reverse=rev)
+        assert np.array_equal(O.decode(packed, x.size, f, reverse=rev).view(np.uint32),
+                              x.view(np.uint32))
+    if gc > 1:
+        assert not np.array_equal(O.encode(x, f, reverse=0), O.encode(x, f, reverse=1))
+
+
+@pytest.mark.parametrize("k,p", [(8, 4), (8, 3), (6, 3), (4, 2)])
+def test_codec_float_round_trip_is_the_format_rounding(k, p):
+    """test/test_pack.cpp:141-170: floats from -8 to 8 in steps of 1/8 (and
+    ±0) encode and decode to the format's own rounding of them, within its
+    finite range."""
+    f = O.codec_p3109(k, p)
+    ef = O.fmt(k, p - 1, 1 << (k - p - 1))
+    x = np.concatenate([np.arange(-64, 65) / 8.0, [0.0, -0.0]]).astype(np.float32)
+    top = max(O.decode_rep(r, f) for r in range(1 << (k - 1)) if not np.isnan(O.decode_rep(r, f)))
+    x = x[np.abs(x) <= top]
+    dec = O.decode(O.encode(x, f), x.size, f)
+    want = O.round(x, ef, RNE)
+    # P3109 has a single zero: -0 encodes to the zero code
+    want[want == 0] = 0.0
+    dec[dec == 0] = 0.0
+    assert np.array_equal(dec.view(np.uint32), want.view(np.uint32))
