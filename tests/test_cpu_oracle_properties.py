@@ -25,7 +25,9 @@ bit pattern (truncate, step one grid point):
 * `test/test_pack.cpp`: packed byte counts from an lcm formula, every code of
   the small P3109 formats round-tripping through the packed form in both
   byte orders with a partial group, and float round trips equal to the
-  format's rounding.
+  format's rounding;
+* `test/test_sat_mode.cpp:70-140`: the codec's three saturation modes on
+  over-range and infinite inputs.
 """
 import numpy as np
 import pytest
@@ -304,3 +306,34 @@ def test_codec_float_round_trip_is_the_format_rounding(k, p):
     want[want == 0] = 0.0
     dec[dec == 0] = 0.0
     assert np.array_equal(dec.view(np.uint32), want.view(np.uint32))
+
+
+OVF_INF, SAT_FINITE, SAT_PROPAGATE = 0, 1, 2
+
+
+@pytest.mark.parametrize("k,p,sat", P3109_SMALL)
+def test_codec_saturation_modes(k, p, sat):
+    """test/test_sat_mode.cpp:70-140 on the codec: finite over-range inputs
+    clamp to ±max-finite under SatFinite and SatPropagate and become ±inf
+    under OvfInf where the format has an infinity; infinite inputs clamp under
+    SatFinite and stay infinite under OvfInf and SatPropagate; 1.0 is the
+    same under all three."""
+    f = O.codec_p3109(k, p, saturating=sat)
+    vals = np.array([O.decode_rep(r, f) for r in range(1 << k)])
+    maxf = vals[np.isfinite(vals)].max()
+    if not maxf > 0:
+        pytest.skip("no finite nonzero value in this format")
+    has_inf = bool(np.isinf(vals).any())
+    rt = lambda x, s: O.decode_rep(O.encode_rep(x, f, RNE, s), f)  # noqa: E731
+    for sign in (1.0, -1.0):
+        for m in (2.0, 8.0, 137.0, 1e6):
+            x = float(np.float32(sign * maxf * m))
+            assert rt(x, SAT_FINITE) == sign * maxf
+            assert rt(x, SAT_PROPAGATE) == sign * maxf
+            assert rt(x, OVF_INF) == (sign * np.inf if has_inf else sign * maxf)
+        xi = sign * np.inf
+        assert rt(xi, SAT_FINITE) == sign * maxf
+        for s in (OVF_INF, SAT_PROPAGATE):
+            assert rt(xi, s) == (xi if has_inf else sign * maxf)
+    if 1.0 <= maxf:
+        assert rt(1.0, OVF_INF) == rt(1.0, SAT_FINITE) == rt(1.0, SAT_PROPAGATE) == 1.0
