@@ -45,6 +45,10 @@ MX_BYTES = MX_ROWS * MX_COLS * 8  # per format: 4 B read + 4 B write per element
 ELEM_FORMATS = {"e2m1": (4, 1, 1), "e4m3": (8, 3, 7), "e5m2": (8, 2, 15)}
 C1_N = 1 << 24
 GEMM_N = 4096
+# the headline line's metric and workload, the same in both arms
+METRIC = "MX block rounding throughput (8 B/elem); secondary: emulated-accum GEMM TFLOP/s"
+WORKLOAD = ("MX round 8192x8192 f32, block 32 along rows, E8M0 scale, "
+            "E2M1/E4M3/E5M2 in turn, RNE")
 
 
 def parse():
@@ -200,11 +204,11 @@ def run_reference(args, world, rank):
         step()
     dt = time.perf_counter() - t0
     gbs = args.steps * len(efs) * sample.size * 8 / dt / 1e9
-    line = {"impl": "reference", "metric": "MX block rounding throughput (8 B/elem)", "value": gbs,
+    line = {"impl": "reference", "metric": METRIC, "value": gbs,
             "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "MX round 8192x8192 f32, block 32, E2M1/E4M3/E5M2 + E8M0, RNE",
+            "config": {"workload": WORKLOAD,
                        "sample": "first 2^24 elements per format per step"},
             "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
                              "sample": "MX rounding of 2^24 of the 2^26 config elements, 3 formats"},
@@ -662,13 +666,12 @@ def run_ours(args, world, rank, local):
     achieved = MX_BYTES / per_launch / 1e9
     traffic = profile_traffic("mx_kernel_8192x8192.md")
     line = {
-        "metric": "MX block rounding throughput (8 B/elem); secondary: emulated-accum GEMM TFLOP/s",
+        "metric": METRIC,
         "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": round(elapsed / args.steps * 1e3, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded N(0,1), 1% outliers x2^12)",
-        "config": {"workload": "MX round 8192x8192 f32, block 32 along rows, E8M0 scale, "
-                               "E2M1/E4M3/E5M2 in turn, RNE",
+        "config": {"workload": WORKLOAD,
                    "l2": "input 256 MiB > 129 MB L2; no flush", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
