@@ -27,7 +27,10 @@ bit pattern (truncate, step one grid point):
   byte orders with a partial group, and float round trips equal to the
   format's rounding;
 * `test/test_sat_mode.cpp:70-140`: the codec's three saturation modes on
-  over-range and infinite inputs.
+  over-range and infinite inputs;
+* `test/test_rounding_modes.cpp` (P3109 formats, down into the subnormals):
+  format rounding lands on the codec's decoded grid, RD/RU bracket x with
+  no grid value between them, and tiny values round away to denorm_min.
 """
 import numpy as np
 import pytest
@@ -337,3 +340,44 @@ def test_codec_saturation_modes(k, p, sat):
             assert rt(xi, s) == (xi if has_inf else sign * maxf)
     if 1.0 <= maxf:
         assert rt(1.0, OVF_INF) == rt(1.0, SAT_FINITE) == rt(1.0, SAT_PROPAGATE) == 1.0
+
+
+@pytest.mark.parametrize("k,p,sat", [(k, p, s) for k in range(4, 9) for p in range(2, k)
+                                     for s in (True, False)])
+def test_format_rounding_brackets_on_the_decoded_grid(k, p, sat):
+    """test/test_rounding_modes.cpp's bounds on the format overload, with the
+    grid taken from the codec's decoded values of the same format: every
+    result lies on that grid; RD and RU bracket x with no grid value between
+    them; RTZ/RAFZ are the neighbours toward/away from zero; nearest modes
+    return the nearer neighbour off ties; a tiny nonzero value rounds away
+    from zero to ±denorm_min, never to 0."""
+    f = O.codec_p3109(k, p, saturating=sat)
+    ef = O.fmt(k, p - 1, 1 << (k - p - 1), saturating=sat)
+    vals = np.array([O.decode_rep(r, f) for r in range(1 << k)], np.float64)
+    grid = np.unique(np.concatenate([vals[np.isfinite(vals)], [0.0]]))
+    maxf, dmin = grid.max(), grid[grid > 0].min()
+    rng = np.random.default_rng(k * 100 + p)
+    mag = np.exp2(rng.uniform(np.log2(dmin) - 2, np.log2(maxf), 4096))
+    x = (mag * rng.choice([-1.0, 1.0], mag.size)).astype(np.float32)
+    x = x[np.abs(x) <= maxf]
+    x64 = x.astype(np.float64)
+    idx = np.searchsorted(grid, x64, side="right") - 1
+    on = grid[idx] == x64
+    lo = grid[idx]
+    hi = np.where(on, lo, grid[np.minimum(idx + 1, grid.size - 1)])
+    res = {m: O.round(x, ef, m).astype(np.float64) for m in (RNE, RTZ, RAFZ, RD, RU, RNO, RTA)}
+    for m, y in res.items():
+        assert np.all(np.isin(np.abs(y), grid)), m
+        assert np.all(y[on] == x64[on]), m
+    assert np.all(res[RD] == lo) and np.all(res[RU] == hi)
+    toward = np.where(x64 < 0, hi, lo)
+    away = np.where(x64 < 0, lo, hi)
+    assert np.all(res[RTZ] == toward) and np.all(res[RAFZ] == away)
+    dl, dh = x64 - lo, hi - x64
+    off_tie = dl != dh
+    nearer = np.where(dl < dh, lo, hi)
+    for m in (RNE, RNO, RTA):
+        assert np.all(res[m][off_tie] == nearer[off_tie]), m
+    tiny = np.array([dmin / 3, -dmin / 3], np.float32)
+    assert np.array_equal(O.round(tiny, ef, RAFZ).astype(np.float64), [dmin, -dmin])
+    assert np.all(O.round(tiny, ef, RTZ) == 0)
