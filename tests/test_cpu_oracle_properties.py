@@ -30,7 +30,8 @@ bit pattern (truncate, step one grid point):
   over-range and infinite inputs;
 * `test/test_rounding_modes.cpp` (P3109 formats, down into the subnormals):
   format rounding lands on the codec's decoded grid, RD/RU bracket x with
-  no grid value between them, and tiny values round away to denorm_min.
+  no grid value between them, and tiny values round away to denorm_min;
+* `test/stoch_expect_test.cpp`: stochastic rounding unbiased in the mean.
 """
 import numpy as np
 import pytest
@@ -381,3 +382,20 @@ def test_format_rounding_brackets_on_the_decoded_grid(k, p, sat):
     tiny = np.array([dmin / 3, -dmin / 3], np.float32)
     assert np.array_equal(O.round(tiny, ef, RAFZ).astype(np.float64), [dmin, -dmin])
     assert np.all(O.round(tiny, ef, RTZ) == 0)
+
+
+@pytest.mark.parametrize("mode,ln", [(TSR, 0), (SRA, 13), (SRB, 13)])
+def test_stochastic_rounding_is_unbiased(mode, ln):
+    """test/stoch_expect_test.cpp's concern: stochastic rounding is unbiased.
+    With as many random bits as dropped bits (13 at 10 mantissa bits; True-SR
+    draws a double), the mean over many independent draws of each value is
+    the value itself, within six standard errors."""
+    mbits, reps = 10, 20000
+    x = wide_inputs(64, 77)
+    xs = np.repeat(x, reps)
+    y = O.round_mantissa(xs, mbits, mode, stoch_len=ln, seed=9).astype(np.float64)
+    tz, az, _ = neighbours(x, mbits)
+    step = np.abs(az.astype(np.float64) - tz.astype(np.float64))
+    mean = y.reshape(64, reps).mean(axis=1)
+    tol = 6 * 0.5 * step / np.sqrt(reps) + 1e-30
+    assert np.all(np.abs(mean - x.astype(np.float64)) <= tol)
