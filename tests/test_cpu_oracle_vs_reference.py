@@ -1,0 +1,96 @@
+"""The oracle against the compiled reference, live, on fresh random inputs.
+
+The committed golden vectors pin the oracle on fixed cases everywhere. Where
+the reference sources are present, `oracle/build_oracle.py` also compiles the
+reference's own scalar code into `oracle/_ref/libref_shim.so`; these tests
+feed it and the oracle new seeded inputs (random bit patterns, so NaNs,
+infinities, subnormals and overflow included) and require the same bits, for
+every deterministic mode, on formats beyond the golden set (every P3109
+<k,p> with k = 3..8, both overflow behaviours, signed and unsigned).
+They skip where the shim is not built (no reference checkout).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+O = pytest.importorskip("oracle.oracle")
+
+DETERMINISTIC = (0, 1, 2, 4, 5, 6, 7, 12, 13)
+
+
+@pytest.fixture(scope="module")
+def R():
+    r = O.ref()
+    if r is None:
+        pytest.skip("reference shim not built (no reference checkout)")
+    return r
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _bits_f32(n, seed):
+    rng = np.random.default_rng(seed)
+    b = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    x = b.view(np.float32).copy()
+    # half of them in a range where most formats round rather than overflow
+    k = n // 2
+    x[:k] = (rng.standard_normal(k) * np.exp2(rng.integers(-30, 30, k))).astype(np.float32)
+    return x
+
+
+FORMATS = [(k, p - 1, 1 << (k - p - 1), sat, signed)
+           for k in range(3, 9) for p in range(1, k) for sat in (True, False)
+           for signed in (True, False) if not (signed and k - (p - 1) - 1 < 1)]
+
+
+@pytest.mark.parametrize("f", FORMATS, ids=lambda f: "k%d_m%d_b%d_%s_%s" % (
+    f[0], f[1], f[2], "sat" if f[3] else "ext", "s" if f[4] else "u"))
+def test_format_rounding_matches_reference(R, f):
+    x = _bits_f32(4096, hash(f) & 0xFFFF)
+    of = O.fmt(f[0], f[1], f[2], saturating=f[3], signed=f[4])
+    for mode in DETERMINISTIC:
+        y = np.empty_like(x)
+        R.ref_round_f32(_p(x), _p(y), x.size, f[0], f[1], f[2], int(f[3]), 0,
+                        0 if f[4] else 1, mode, 0, None, None, None)
+        got = O.round(x, of, mode)
+        same = (got.view(np.uint32) == y.view(np.uint32)) | (np.isnan(got) & np.isnan(y))
+        assert np.all(same), (f, mode, x[~same][:4], got[~same][:4], y[~same][:4])
+
+
+@pytest.mark.parametrize("mbits", [0, 1, 3, 7, 10, 15, 22])
+def test_mantissa_rounding_matches_reference(R, mbits):
+    x = _bits_f32(1 << 14, 1000 + mbits)
+    for mode in DETERMINISTIC:
+        y = np.empty_like(x)
+        R.ref_round_mantissa_f32(_p(x), _p(y), x.size, mbits, mode, 0, None, None, None)
+        got = O.round_mantissa(x, mbits, mode)
+        assert np.array_equal(got.view(np.uint32), y.view(np.uint32)), (mbits, mode)
+
+
+@pytest.mark.parametrize("block", [8, 32, 128])
+def test_mx_matches_reference(R, block):
+    rng = np.random.default_rng(block)
+    n = 5003
+    x = (rng.standard_normal(n) * np.exp2(rng.integers(-12, 12, n))).astype(np.float32)
+    for ef in ((8, 3, 7), (8, 2, 15), (4, 1, 1), (6, 2, 3)):
+        for mode in (0, 1, 5, 6):
+            y = np.empty_like(x)
+            R.ref_mx_round_f32(_p(x), _p(y), n, block, ef[0], ef[1], ef[2], 1, 0,
+                               8, 0, 127, 0, 1, mode, 0, 0)
+            got = O.mx_round(x, block, O.fmt(*ef), O.fmt(8, 0, 127, saturating=False,
+                                                          signed=False), mode=mode)
+            assert np.array_equal(got.view(np.uint32), y.view(np.uint32)), (ef, mode)
+
+
+@pytest.mark.parametrize("mbits", [3, 7, 10, 15])
+def test_gemm_matches_reference(R, mbits):
+    rng = np.random.default_rng(mbits)
+    M, N, K = 24, 20, 70
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((K, N)).astype(np.float32)
+    D = np.empty((M, N), np.float32)
+    R.ref_gemm_f32(_p(A), _p(B), _p(D), M, N, K, mbits, C.c_float(0.5))
+    assert np.array_equal(O.gemm(A, B, mbits, alpha=0.5).view(np.uint32), D.view(np.uint32))
