@@ -6,7 +6,9 @@ reference's own scalar code into `oracle/_ref/libref_shim.so`; these tests
 feed it and the oracle new seeded inputs (random bit patterns, so NaNs,
 infinities, subnormals and overflow included) and require the same bits, for
 every deterministic mode, on formats beyond the golden set (every P3109
-<k,p> with k = 3..8, both overflow behaviours, signed and unsigned).
+<k,p> with k = 3..8, both overflow behaviours, signed and unsigned), for
+f64 sources and every f16 bit pattern, and for the codec's bytes (modes,
+saturation modes, both byte orders) and decoded values.
 They skip where the shim is not built (no reference checkout).
 """
 import ctypes as C
@@ -94,3 +96,67 @@ def test_gemm_matches_reference(R, mbits):
     D = np.empty((M, N), np.float32)
     R.ref_gemm_f32(_p(A), _p(B), _p(D), M, N, K, mbits, C.c_float(0.5))
     assert np.array_equal(O.gemm(A, B, mbits, alpha=0.5).view(np.uint32), D.view(np.uint32))
+
+
+F64_FORMATS = [(8, 3, 7, True, True), (16, 10, 15, False, True), (16, 7, 127, True, True),
+               (32, 23, 127, False, True), (40, 30, 255, True, True), (8, 2, 16, False, False)]
+
+
+@pytest.mark.parametrize("f", F64_FORMATS, ids=str)
+def test_f64_format_rounding_matches_reference(R, f):
+    rng = np.random.default_rng(f[0] * 100 + f[1])
+    n = 4096
+    x = rng.integers(0, 1 << 64, n, dtype=np.uint64).view(np.float64).copy()
+    x[: n // 2] = rng.standard_normal(n // 2) * np.exp2(rng.integers(-300, 300, n // 2))
+    of = O.fmt(f[0], f[1], f[2], saturating=f[3], signed=f[4])
+    for mode in DETERMINISTIC:
+        y = np.empty_like(x)
+        R.ref_round_f64(_p(x), _p(y), n, f[0], f[1], f[2], int(f[3]), 0, 0 if f[4] else 1,
+                        mode, 0, None, None, None)
+        got = O.round(x, of, mode)
+        same = (got.view(np.uint64) == y.view(np.uint64)) | (np.isnan(got) & np.isnan(y))
+        assert np.all(same), (f, mode)
+
+
+@pytest.mark.parametrize("t,mbits", [("f64", m) for m in (0, 10, 30, 51)] +
+                         [("f16", m) for m in (0, 2, 5, 9)])
+def test_f64_f16_mantissa_rounding_matches_reference(R, t, mbits):
+    rng = np.random.default_rng(mbits)
+    if t == "f64":
+        x = rng.integers(0, 1 << 64, 1 << 13, dtype=np.uint64).view(np.float64).copy()
+        view = np.uint64
+    else:
+        x = np.arange(1 << 16, dtype=np.uint16)  # every f16 bit pattern
+        view = np.uint16
+    for mode in DETERMINISTIC:
+        y = np.empty_like(x)
+        getattr(R, f"ref_round_mantissa_{t}")(_p(x), _p(y), x.size, mbits, mode, 0,
+                                              None, None, None)
+        got = O.round_mantissa(x, mbits, mode)
+        assert np.array_equal(got.view(view), y.view(view)), (t, mbits, mode)
+
+
+@pytest.mark.parametrize("k,p,sat", [(k, p, s) for k in range(3, 9) for p in range(1, k)
+                                     for s in (True, False)])
+def test_codec_matches_reference(R, k, p, sat):
+    f = O.codec_p3109(k, p, saturating=sat)
+    cf = O.codec_fields(f)
+    rng = np.random.default_rng(k * 10 + p)
+    x = _bits_f32(1001, k * 10 + p)
+    x[:500] = (rng.standard_normal(500) * np.exp2(rng.integers(-12, 12, 500))).astype(np.float32)
+    size = int(R.ref_packed_size(k, x.size))
+    assert size == O.packed_size(k, x.size)
+    for mode in (0, 1, 5, 6, 12):
+        for s in (0, 1, 2):
+            for rev in (0, 1):
+                buf = np.zeros(size, np.uint8)
+                R.ref_encode_f32(_p(buf), _p(x), x.size, _p(cf), mode, s, 0, rev)
+                assert np.array_equal(O.encode(x, f, mode=mode, sat=s, reverse=rev), buf), \
+                    (mode, s, rev)
+    raw = rng.integers(0, 256, size, dtype=np.uint8)
+    for rev in (0, 1):
+        dec = np.empty(x.size, np.float32)
+        R.ref_decode_f32(_p(dec), _p(raw), x.size, _p(cf), rev)
+        got = O.decode(raw, x.size, f, reverse=rev)
+        same = (got.view(np.uint32) == dec.view(np.uint32)) | (np.isnan(got) & np.isnan(dec))
+        assert np.all(same), rev
