@@ -160,3 +160,31 @@ def test_codec_matches_reference(R, k, p, sat):
         got = O.decode(raw, x.size, f, reverse=rev)
         same = (got.view(np.uint32) == dec.view(np.uint32)) | (np.isnan(got) & np.isnan(dec))
         assert np.all(same), rev
+
+
+STOCH = (3, 8, 9, 10, 11, 14)
+LEN_MODES = (3, 8, 9, 14)
+
+
+@pytest.mark.parametrize("f", [(8, 3, 7, True, True), (8, 2, 15, True, True),
+                               (6, 2, 3, False, True), (16, 10, 15, False, True),
+                               (16, 7, 127, False, True)], ids=str)
+def test_stochastic_formulas_match_reference(R, f):
+    """The reference's host stochastic rounding re-seeds its generator per
+    call, so the shim seeds it per element and reports the draw each element
+    consumed; fed those same bits, the oracle must give the same results."""
+    rng = np.random.default_rng(f[0] * 7 + f[1])
+    n = 4096
+    x = (rng.standard_normal(n) * np.exp2(rng.integers(-20, 20, n))).astype(np.float32)
+    of = O.fmt(f[0], f[1], f[2], saturating=f[3], signed=f[4])
+    for mode in STOCH:
+        ln = min(8, 23 - f[1]) if mode in LEN_MODES else 0
+        seeds = rng.integers(1, 2 ** 32 - 1, n, dtype=np.uint32)
+        rb = np.zeros(n, np.uint64)
+        us = np.zeros(n, np.float64)
+        y = np.empty_like(x)
+        R.ref_round_f32(_p(x), _p(y), n, f[0], f[1], f[2], int(f[3]), 0, 0 if f[4] else 1,
+                        mode, ln, _p(seeds), _p(rb), _p(us))
+        assert rb.any() or us.any()  # the draws were recorded
+        got = O.round_bits(x, of, mode, ln, rbits=rb, usamp=us)
+        assert np.array_equal(got.view(np.uint32), y.view(np.uint32)), (f, mode)
