@@ -31,7 +31,10 @@ bit pattern (truncate, step one grid point):
 * `test/test_rounding_modes.cpp` (P3109 formats, down into the subnormals):
   format rounding lands on the codec's decoded grid, RD/RU bracket x with
   no grid value between them, and tiny values round away to denorm_min;
-* `test/stoch_expect_test.cpp`: stochastic rounding unbiased in the mean.
+* `test/stoch_expect_test.cpp`: stochastic rounding unbiased in the mean;
+* the PWL SiLU kernel's definition (`src/Lof_kernel.cu:231-257`; the
+  reference has no test of it): relu outside [-R, R], the table at the knots,
+  linear interpolation between them.
 """
 import numpy as np
 import pytest
@@ -399,3 +402,31 @@ def test_stochastic_rounding_is_unbiased(mode, ln):
     mean = y.reshape(64, reps).mean(axis=1)
     tol = 6 * 0.5 * step / np.sqrt(reps) + 1e-30
     assert np.all(np.abs(mean - x.astype(np.float64)) <= tol)
+
+
+@pytest.mark.parametrize("nseg,R", [(16, 4.0), (64, 8.0), (256, 8.0)])
+def test_pwl_silu_knots_interpolation_and_asymptote(nseg, R):
+    """The PWL SiLU of `src/Lof_kernel.cu:231-257`: outside [-R, R] the relu
+    asymptote exactly; at every knot but the last the table value exactly;
+    between knots the linear interpolation of the two neighbouring knots,
+    within one float32 ulp of it evaluated in FP64 from the kernel's own
+    float32 steps."""
+    knots = np.linspace(-R, R, nseg + 1)
+    lut = (knots / (1 + np.exp(-knots))).astype(np.float32)
+    rng = np.random.default_rng(nseg)
+    out = np.concatenate([rng.uniform(R, 4 * R, 500), -rng.uniform(R, 4 * R, 500)])
+    out = out.astype(np.float32)
+    out = out[np.abs(out) > R]
+    assert np.array_equal(O.pwl_silu(out, lut, R), np.where(out > 0, out, 0).astype(np.float32))
+    kx = knots[:-1].astype(np.float32)
+    assert np.array_equal(O.pwl_silu(kx, lut, R), lut[:-1])
+    x = rng.uniform(-R, R, 20000).astype(np.float32)
+    inv = np.float32(nseg) / np.float32(2 * R)
+    u = ((x + np.float32(R)) * inv).astype(np.float32)
+    i = np.minimum(u.astype(np.int64), nseg - 1)
+    frac = (u - i.astype(np.float32)).astype(np.float32)
+    d = (lut[i + 1] - lut[i]).astype(np.float32)
+    want = frac.astype(np.float64) * d + lut[i]
+    got = O.pwl_silu(x, lut, R).astype(np.float64)
+    ulp = np.spacing(np.abs(want).astype(np.float32)).astype(np.float64)
+    assert np.all(np.abs(got - want) <= ulp)
