@@ -58,3 +58,27 @@ def test_ctypes_structs_match_header_layout(tmp_path):
         assert C.sizeof(cls) == layout[(cname, "sizeof")], cname
         for fname, _ in cls._fields_:
             assert getattr(cls, fname).offset == layout[(cname, fname)], (cname, fname)
+
+
+def test_header_gives_cpp_callers_c_linkage(tmp_path):
+    """A C++ translation unit that includes `lofgb.h` and takes the address of
+    every declared entry point refers to them by their plain C names (the
+    header's extern "C" block), so a C++ binding links against liblofgb."""
+    import re
+    cxx = shutil.which("g++") or shutil.which("c++")
+    nm = shutil.which("nm")
+    if cxx is None or nm is None:
+        pytest.skip("no host C++ compiler or nm")
+    header = open(os.path.join(ROOT, "include", "lofgb.h")).read()
+    names = sorted(set(re.findall(r"^[A-Za-z_][\w\s\*]*?\b(lofgb_\w+)\s*\(", header, re.M)))
+    assert len(names) >= 30
+    body = "\n".join(f"  (void*)&{n}," for n in names)
+    src = tmp_path / "probe.cpp"
+    src.write_text('#include "lofgb.h"\nvoid* table[] = {\n' + body + "\n};\n")
+    obj = tmp_path / "probe.o"
+    subprocess.run([cxx, "-c", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(obj)],
+                   check=True, capture_output=True)
+    undefined = subprocess.run([nm, "-u", str(obj)], check=True, capture_output=True,
+                               text=True).stdout.split()
+    for n in names:
+        assert n in undefined, n
