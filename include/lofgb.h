@@ -219,13 +219,24 @@ int lofgb_gemm_accfmt_f32(const float* A, int64_t lda, int trans_a, const float*
  *   - the split operands need lofgb_gemm_tc_workspace_size(M, N, K) bytes;
  *     above 64 MiB (for example M = N = K = 2048 fits, 4096 does not) the
  *     call returns LOFGB_ERR_WORKSPACE and does nothing;
+ *   - arguments are checked first and give the codes lofgb_gemm_f32 gives;
+ *     only a valid request is compared with the 64 MiB limit;
  *   - the first call on each device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture;
+ *     (cudaGetSymbolAddress) with that device current. With lazy module
+ *     loading (the CUDA default) that lookup can load this library's kernel
+ *     module on the device, which commits the 64 MiB array and the module
+ *     code at that moment. So make the first call on each device at set-up,
+ *     outside any region where allocation is forbidden, and before any
+ *     stream capture; later calls on that device allocate nothing;
  *   - all calls share the one array, which keeps the last call's contents
  *     (every call rewrites the parts it reads, so nothing leaks into the
  *     result); calls that overlap on the GPU (different streams, or
- *     different host threads, without ordering between them) race on it. */
+ *     different host threads, without ordering between them) race on it;
+ *   - device-side timeouts are not reported: the tensor-core kernel bounds
+ *     its waits (about 2 s) and, when one runs out, leaves D incomplete and
+ *     records LOFGB_ERR_TIMEOUT in a status word inside the private array,
+ *     which no entry point reads back. lofgb_gemm_f32 with a caller
+ *     workspace exposes that word (the workspace's first 4 bytes). */
 int lofgb_gemm_tc_noalloc_f32(const float* A, int64_t lda, int trans_a, const float* B,
                               int64_t ldb, int trans_b, float* D, int64_t ldd, int M, int N,
                               int K, int accum_mant_bits, float alpha, int chunk,

@@ -232,6 +232,20 @@ static int check_arrays(const void* in, const void* out, int64_t n, int elem) {
     return LOFGB_OK;
 }
 
+// GEMM argument checks shared by every GEMM entry point (sizes, trans flags,
+// NULL pointers, leading dimensions).
+int check_gemm_args(const void* A, int64_t lda, int ta, const void* B, int64_t ldb, int tb,
+                    const void* D, int64_t ldd, int M, int N, int K) {
+    if (M < 0 || N < 0 || K < 0) return set_error(LOFGB_ERR_SIZE, "negative GEMM dimension");
+    if ((ta != 0 && ta != 1) || (tb != 0 && tb != 1))
+        return set_error(LOFGB_ERR_SIZE, "trans flags must be 0 or 1");
+    if (M && N && !D) return set_error(LOFGB_ERR_NULL, "D is NULL");
+    if (M && N && K && (!A || !B)) return set_error(LOFGB_ERR_NULL, "A or B is NULL");
+    if (lda < (ta ? M : K) || lda < 1 || ldb < (tb ? K : N) || ldb < 1 || ldd < N || ldd < 1)
+        return set_error(LOFGB_ERR_SIZE, "leading dimension too small");
+    return LOFGB_OK;
+}
+
 }  // namespace lofgb
 
 using namespace lofgb;
@@ -315,18 +329,6 @@ int lofgb_mx_round_f32(const float* in, float* out, int64_t n, int block_size,
     volatile float pmn = a * b;
     volatile float inv = 1.0f / pmn;
     return launch_mx(in, out, n, block_size, pe, ps, pmn, inv, seed, offset, stream);
-}
-
-static int check_gemm_args(const void* A, int64_t lda, int ta, const void* B, int64_t ldb,
-                           int tb, const void* D, int64_t ldd, int M, int N, int K) {
-    if (M < 0 || N < 0 || K < 0) return set_error(LOFGB_ERR_SIZE, "negative GEMM dimension");
-    if ((ta != 0 && ta != 1) || (tb != 0 && tb != 1))
-        return set_error(LOFGB_ERR_SIZE, "trans flags must be 0 or 1");
-    if (M && N && !D) return set_error(LOFGB_ERR_NULL, "D is NULL");
-    if (M && N && K && (!A || !B)) return set_error(LOFGB_ERR_NULL, "A or B is NULL");
-    if (lda < (ta ? M : K) || lda < 1 || ldb < (tb ? K : N) || ldb < 1 || ldd < N || ldd < 1)
-        return set_error(LOFGB_ERR_SIZE, "leading dimension too small");
-    return LOFGB_OK;
 }
 
 static int gemm_impl(const float* A, int64_t lda, int64_t sa, int trans_a, const float* B,

@@ -742,13 +742,12 @@ int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float*
                    void* workspace, size_t workspace_bytes, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (K == 0) {
-        // no products: D = alpha * (+0)
-        for (int z = 0; z < batch; ++z)
-            for (int i = 0; i < M; ++i) {
-                cudaError_t e = cudaMemsetAsync(D + (int64_t)z * sd + (int64_t)i * ldd, 0,
-                                                sizeof(float) * N, st);
-                if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
-            }
+        // no products: D = alpha * (+0), one pitched clear per batch entry
+        for (int z = 0; z < batch; ++z) {
+            cudaError_t e = cudaMemset2DAsync(D + (int64_t)z * sd, sizeof(float) * (size_t)ldd, 0,
+                                              sizeof(float) * (size_t)N, (size_t)M, st);
+            if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+        }
         return LOFGB_OK;
     }
     const WsLayout w = ws_layout(M, N, K, batch);
@@ -888,16 +887,24 @@ extern "C" int lofgb_gemm_tc_noalloc_f32(const float* A, int64_t lda, int trans_
                                          int N, int K, int accum_mant_bits, float alpha, int chunk,
                                          void* stream) {
     using namespace lofgb;
-    if (M > 0 && N > 0 && K > 0) {
+    // the arguments first, with the codes lofgb_gemm_f32 returns for them;
+    // only a valid request is measured against the scratch array
+    int st = check_gemm_args(A, lda, trans_a, B, ldb, trans_b, D, ldd, M, N, K);
+    if (st) return st;
+    if (accum_mant_bits < 0 || accum_mant_bits > 23)
+        return set_error(LOFGB_ERR_FORMAT, "accum_mant_bits %d outside [0, 23]", accum_mant_bits);
+    if (chunk <= 0 || chunk % 16 != 0 || chunk > 256)
+        return set_error(LOFGB_ERR_SIZE, "chunk %d must be a multiple of 16 in [16, 256]", chunk);
+    const bool work = M > 0 && N > 0 && K > 0;
+    if (work) {
         const size_t need = gemm_tc_workspace(M, N, K, 1);
         if (need > NOALLOC_SCRATCH_BYTES)
             return set_error(LOFGB_ERR_WORKSPACE,
                              "no-alloc GEMM needs %zu bytes of scratch; the built-in array holds %zu",
                              need, NOALLOC_SCRATCH_BYTES);
     }
-    int st = LOFGB_OK;
     void* scratch = nullptr;
-    if (M > 0 && N > 0 && K > 0) {
+    if (work) {
         scratch = noalloc_scratch(&st);
         if (!scratch) return st;
     }

@@ -102,6 +102,8 @@ int sm_count();
 int set_error(int status, const char* fmt, ...);
 void clear_error();
 int check_launch(const char* what);
+int check_gemm_args(const void* A, int64_t lda, int ta, const void* B, int64_t ldb, int tb,
+                    const void* D, int64_t ldd, int M, int N, int K);
 
 // Tensor-core GEMM workspace (gemm_tc.cu): a status word, then the BF16 hi /
 // lo splits of A (Mp x Kp) and B (Np x Kp), K-major and zero padded

@@ -102,6 +102,29 @@ def test_gemm_validation_codes():
     assert L.lofgb_gemm_tc_workspace_size(0, 4, 4) == 0
 
 
+def test_noalloc_gemm_checks_arguments_before_its_scratch_limit():
+    """The no-allocation GEMM reports bad arguments with lofgb_gemm_f32's codes
+    even when the shape would also exceed its built-in scratch (host checks
+    only: nothing reaches the device)."""
+    L = _native.lib()
+    A, B, D = C.c_void_p(0x1000), C.c_void_p(0x2000), C.c_void_p(0x3000)
+    big = 4096
+
+    def call(A=A, lda=big, ta=0, ldd=big, mbits=10, chunk=32, M=big):
+        return L.lofgb_gemm_tc_noalloc_f32(A, lda, ta, B, big, 0, D, ldd, M, big, big, mbits, 1.0,
+                                           chunk, None)
+    assert call(lda=big - 1) == -2
+    assert call(ldd=1) == -2
+    assert call(ta=3) == -2
+    assert call(M=-1) == -2
+    assert call(A=None) == -1
+    assert call(mbits=24) == -3
+    assert call(chunk=24) == -2
+    assert call() == -9               # valid request beyond the 64 MiB scratch
+    assert "scratch" in L.lofgb_last_error_detail().decode()
+    assert call(M=0) == 0             # empty output: nothing to do
+
+
 def test_batched_gemm_and_conv_validation_codes():
     L = _native.lib()
     A, B, D = C.c_void_p(0x1000), C.c_void_p(0x2000), C.c_void_p(0x3000)
