@@ -16,8 +16,10 @@ rounding of 2^24 FP32 to E4M3 (RNE and SR-A), and the 4096^3 emulated GEMM
 error).
 
 --impl reference times the reference algorithm on the host cores (the C
-oracle, a restatement of the reference's scalar code, with all threads) on a
-bounded sample of the same workload.
+oracle, a restatement of the reference's scalar code, with all threads) on
+the same workload: the whole matrix, three formats, every step. The
+reference's own host code is compiled only where its sources are present
+(x86, for the parity tests), so the timed CPU implementation is the port.
 
 With N > 1 (torchrun) every rank runs an independent replica of the workload
 on its own GPU (weak scaling, no data-path collective); timing is the max
@@ -188,8 +190,8 @@ def run_reference(args, world, rank):
 
     from oracle import oracle as O
     threads = O.max_threads()
-    x = config2_input(torch, None).reshape(-1).numpy()
-    sample = x[: 1 << 24]  # a quarter of the matrix per format per step
+    # the whole 8192 x 8192 matrix per format per step: the same work as our arm
+    sample = config2_input(torch, None).reshape(-1).numpy()
     sf = O.fmt(8, 0, 127, saturating=False, signed=False)
     efs = [O.fmt(*v) for v in ELEM_FORMATS.values()]
 
@@ -208,10 +210,9 @@ def run_reference(args, world, rank):
             "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD,
-                       "sample": "first 2^24 elements per format per step"},
+            "config": {"workload": WORKLOAD},
             "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
-                             "sample": "MX rounding of 2^24 of the 2^26 config elements, 3 formats"},
+                             "sample": "MX rounding of all 2^26 elements, 3 formats, every step"},
             "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -537,6 +538,76 @@ def grouped_workloads(torch, lg, dev):
     return out
 
 
+def bind_gpu_local_numa(local):
+    """Restrict this process to the host CPUs of the GPU's NUMA node (the
+    node sysfs records for the GPU's PCI device), so that pinned host buffers
+    allocated next live next to the GPU. Returns what was done and the CPU
+    set to restore once the buffers exist."""
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(local), "--query-gpu=pci.bus_id",
+                              "--format=csv,noheader"], capture_output=True, text=True,
+                             timeout=30).stdout.strip().lower()
+        # sysfs names the device with a 4-digit domain
+        dom, rest = bus.split(":", 1)
+        path = f"/sys/bus/pci/devices/{int(dom, 16):04x}:{rest}/numa_node"
+        node = int(open(path).read().strip())
+        if node < 0:
+            return {"node": None, "note": "no NUMA node recorded for the GPU"}
+        cpus = set()
+        for part in open(f"/sys/devices/system/node/node{node}/cpulist").read().strip().split(","):
+            a, _, b = part.partition("-")
+            cpus.update(range(int(a), int(b or a) + 1))
+        before = os.sched_getaffinity(0)
+        cpus &= before
+        if not cpus:
+            return {"node": node, "note": "no allowed CPU on the GPU's node"}
+        os.sched_setaffinity(0, cpus)
+        return {"node": node, "cpus": len(cpus), "restore": before}
+    except (OSError, ValueError, subprocess.SubprocessError) as e:
+        return {"node": None, "note": str(e)[:120]}
+
+
+def link_bandwidth(torch, xh, yh, xd, yd, stream, s_out):
+    """Host<->device copy rates of the e2e buffers, measured apart from the
+    e2e loop: one 256 MiB pinned host-to-device copy, one device-to-host copy,
+    and two device-to-host copies in flight on two streams. The e2e step
+    moves 1x in and 3x out, with the input copy overlapping the outputs, so
+    its ceiling is the step's algorithmic bytes over the slower direction."""
+    nbytes = xh.numel() * 4
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / reps
+
+    t_h2d = timed(lambda: xd[0].copy_(xh, non_blocking=True))
+    t_d2h = timed(lambda: yh[0].copy_(yd[0], non_blocking=True))
+
+    def two_d2h():
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        for i, so in enumerate(s_out):
+            so.wait_event(ev)
+            with torch.cuda.stream(so):
+                yh[i].copy_(yd[i], non_blocking=True)
+        for so in s_out:
+            stream.wait_stream(so)
+    t_d2h2 = timed(two_d2h)
+    h2d, d2h, d2h2 = nbytes / t_h2d / 1e9, nbytes / t_d2h / 1e9, 2 * nbytes / t_d2h2 / 1e9
+    # one e2e step: 3 formats x 8 algorithmic B/elem = 6 x nbytes; its copies
+    # take at least the slower of nbytes in and 3 x nbytes out
+    t_copy = max(nbytes / (h2d * 1e9), 3 * nbytes / (max(d2h, d2h2) * 1e9))
+    return {"h2d_gbs": round(h2d, 1), "d2h_gbs": round(d2h, 1), "d2h_two_streams_gbs": round(d2h2, 1),
+            "e2e_ceiling_gbs": round(6 * nbytes / t_copy / 1e9, 1),
+            "note": "ceiling = 3 x 8 B/elem over the slower of 1 x 4 B/elem in and 3 x 4 B/elem out"}
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -594,8 +665,11 @@ def run_ours(args, world, rank, local):
     # result copies alternate over two streams (two copy engines device to
     # host), the roundings stay on the timed stream; events order the reuse
     # of every device buffer.
+    numa = bind_gpu_local_numa(local)
     xh = x_host.pin_memory()
     yh = [torch.empty_like(xh).pin_memory() for _ in efs]
+    if "restore" in numa:  # pages are placed; the CPU baseline later uses every core
+        os.sched_setaffinity(0, numa.pop("restore"))
     s_in = torch.cuda.Stream(dev)
     s_out = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
     xd = [torch.empty(xh.shape, dtype=xh.dtype, device=dev) for _ in range(2)]
@@ -653,6 +727,8 @@ def run_ours(args, world, rank, local):
             raise RuntimeError(f"end-to-end result {i} differs from the device result")
     e2e_s = e0.elapsed_time(e1) / 1e3
     clk = clocks.stop()
+    link = link_bandwidth(torch, xh, yh, xd, yd, stream, s_out)
+    link["numa"] = numa
 
     if dist:
         elapsed, e2e_s = max_over_ranks(dist, [elapsed, e2e_s], dev)
@@ -680,7 +756,8 @@ def run_ours(args, world, rank, local):
         "e2e": {"value": round(whole_job_gbs(world, e2e_steps, step_bytes, e2e_s), 2), "unit": "GB/s",
                 "h2d_bytes_per_step": MX_ROWS * MX_COLS * 4,
                 "d2h_bytes_per_step": len(efs) * MX_ROWS * MX_COLS * 4,
-                "api": "lofloat_gb300.virtual_mx_round (C ABI lofgb_mx_round_f32)"},
+                "api": "lofloat_gb300.virtual_mx_round (C ABI lofgb_mx_round_f32)",
+                "link": link},
         "gpu_launches": args.steps * len(efs),
         "clocks": clk,
     }
