@@ -194,8 +194,9 @@ conv_plain_kernel(ConvGeo g, AccRound r, float alpha) {
 template <int ORDER>
 __global__ void __launch_bounds__(256)
 split_conv_weight_kernel(ConvGeo g, int Mp, int Kp, __nv_bfloat16* __restrict__ hi,
-                         __nv_bfloat16* __restrict__ lo) {
+                         __nv_bfloat16* __restrict__ lo, uint32_t* __restrict__ range) {
     __shared__ float tile[32][65];
+    ExpRange er;
     const int tiles_k = Kp / 64;
     const int64_t items = (int64_t)(Mp / 32) * tiles_k;
     for (int64_t item = blockIdx.x; item < items; item += gridDim.x) {
@@ -212,9 +213,10 @@ split_conv_weight_kernel(ConvGeo g, int Mp, int Kp, __nv_bfloat16* __restrict__ 
             tile[rr][kk] = v;
         }
         __syncthreads();
-        split_store_tile(tile, r0, k0, Mp, Kp, hi, lo);
+        split_store_tile(tile, r0, k0, Mp, Kp, hi, lo, er);
         __syncthreads();
     }
+    range_flush(range, er);
 }
 
 // Implicit im2col: row j (output pixel), column t -> x[img][c][h][w] or 0.
@@ -223,8 +225,9 @@ split_conv_weight_kernel(ConvGeo g, int Mp, int Kp, __nv_bfloat16* __restrict__ 
 template <int ORDER>
 __global__ void __launch_bounds__(256)
 split_im2col_kernel(ConvGeo g, int Np, int Kp, __nv_bfloat16* __restrict__ hi,
-                    __nv_bfloat16* __restrict__ lo) {
+                    __nv_bfloat16* __restrict__ lo, uint32_t* __restrict__ range) {
     __shared__ float tile[32][65];
+    ExpRange er;
     const int tiles_k = Kp / 64;
     const int64_t items = (int64_t)(Np / 32) * tiles_k;
     for (int64_t item = blockIdx.x; item < items; item += gridDim.x) {
@@ -248,9 +251,10 @@ split_im2col_kernel(ConvGeo g, int Np, int Kp, __nv_bfloat16* __restrict__ hi,
             tile[rr][kk] = v;
         }
         __syncthreads();
-        split_store_tile(tile, r0, k0, Np, Kp, hi, lo);
+        split_store_tile(tile, r0, k0, Np, Kp, hi, lo, er);
         __syncthreads();
     }
+    range_flush(range, er);
 }
 
 int conv_geometry(const lofgb_conv2d_shape* s, int* P, int* Q) {
@@ -337,18 +341,21 @@ int launch_conv_tc(const ConvGeo& g, int mbits, float alpha, int chunk, void* wo
     if (!workspace || workspace_bytes < w.total || (reinterpret_cast<uintptr_t>(workspace) & 255))
         return set_error(LOFGB_ERR_WORKSPACE, "need %zu bytes of 256-byte aligned workspace", w.total);
     uint8_t* ws = static_cast<uint8_t*>(workspace);
-    cudaError_t e = cudaMemsetAsync(ws + w.status, 0, sizeof(int), st);
+    cudaError_t e = cudaMemsetAsync(ws + w.status, 0, WS_HEADER_CLEAR, st);
     if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+    auto* range = reinterpret_cast<uint32_t*>(ws + w.range);
     auto* ahi = reinterpret_cast<__nv_bfloat16*>(ws + w.ahi);
     auto* alo = reinterpret_cast<__nv_bfloat16*>(ws + w.alo);
     auto* bhi = reinterpret_cast<__nv_bfloat16*>(ws + w.bhi);
     auto* blo = reinterpret_cast<__nv_bfloat16*>(ws + w.blo);
     const int64_t maxg = (int64_t)sm_count() * 8;
     const int64_t ia = (int64_t)(w.Mp / 32) * (w.Kp / 64), ib = (int64_t)(w.Np / 32) * (w.Kp / 64);
-    split_conv_weight_kernel<ORDER><<<(int)(ia < maxg ? ia : maxg), 256, 0, st>>>(g, w.Mp, w.Kp, ahi, alo);
+    split_conv_weight_kernel<ORDER><<<(int)(ia < maxg ? ia : maxg), 256, 0, st>>>(g, w.Mp, w.Kp, ahi, alo,
+                                                                               range);
     int rc = check_launch("split_conv_weight_kernel");
     if (rc) return rc;
-    split_im2col_kernel<ORDER><<<(int)(ib < maxg ? ib : maxg), 256, 0, st>>>(g, w.Np, w.Kp, bhi, blo);
+    split_im2col_kernel<ORDER><<<(int)(ib < maxg ? ib : maxg), 256, 0, st>>>(g, w.Np, w.Kp, bhi, blo,
+                                                                          range + 2);
     if ((rc = check_launch("split_im2col_kernel"))) return rc;
     return launch_tc_presplit(ws, w, g.y, g.L, 0, g.K, g.ncols, mbits, alpha, chunk, g.L,
                               (int64_t)g.K * g.L, stream);

@@ -25,11 +25,14 @@
 //               tcgen05.mma.cta_group::1.kind::f16, M=128 N=128 K=16,
 //               chunk sums in four 128-column TMEM buffers (all 512
 //               columns), so the MMAs run up to three chunks ahead;
-//   warps 2..9  epilogue (two per TMEM lane quarter): tcgen05.ld the chunk
-//               sum of its lane quarter and one 64-column half, in four
+//   warps 2..17 epilogue (four per TMEM lane quarter): tcgen05.ld the chunk
+//               sum of its lane quarter and one 32-column slice, in two
 //               16-column loads pipelined with the folds (one piece loads
-//               while the previous one is folded), fold it into 64 register
+//               while the previous one is folded), fold it into 32 register
 //               accumulators, release the TMEM buffer; store D at tile end.
+// The fold runs on the FMA pipe in packed pairs (fold2_fast) whenever the
+// operands' exponent ranges, published by the split kernels, rule out
+// subnormal and overflowing partial sums; otherwise with integer rounding.
 // Every wait is bounded (~2 s of %globaltimer): on expiry the CTA records
 // LOFGB_ERR_TIMEOUT in the workspace status word, drains its own in-flight
 // copies and MMAs (again bounded), frees its TMEM and exits.
@@ -38,6 +41,7 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <cmath>
 #include <cstring>
 #include <mutex>
 
@@ -55,10 +59,10 @@ constexpr int SK = 64;            // k per pipeline stage (one 128-byte swizzle 
 constexpr int STAGES = 3;
 constexpr int TILE_BYTES = TBM * SK * 2;       // 16 KiB per operand tile
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;    // A hi, A lo, B hi, B lo
-constexpr int EPI_WARPS = 8;                   // two per TMEM lane quarter
+constexpr int EPI_WARPS = 16;                  // EPI_WARPS / 4 per TMEM lane quarter
 constexpr int EPI_COLS = TBN * 4 / EPI_WARPS;  // accumulator columns per epilogue thread
 constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
-static_assert(EPI_COLS == 64, "the epilogue folds four pipelined 16-column pieces");
+static_assert(EPI_COLS == 64 || EPI_COLS == 32, "the epilogue folds 16-column pieces, 4 or 2 per chunk");
 constexpr int NBUF = 4;                        // TMEM chunk buffers (all 512 columns)
 constexpr int TMEM_COLS = NBUF * TBN;
 static_assert((NBUF & (NBUF - 1)) == 0 && TMEM_COLS <= 512, "TMEM chunk buffers");
@@ -82,6 +86,8 @@ struct TcParams {
     int acc_kind;          // 0: RNE to ro mantissa bits; 2 / 3: the format acc_plan
                            // (whole-range float rounding / integer rounding core)
     RoundPlan acc_plan;
+    uint32_t* range;       // exponent ranges of A and B (workspace words)
+    int fast_lim;          // fast fold iff emax_a + emax_b <= fast_lim (FAST_OFF: never)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -249,6 +255,54 @@ __device__ __forceinline__ float fold_fmt(float acc, float s, const RoundPlan& p
     return __uint_as_float(vr_format<LOFGB_RNE, 32>(v, p, 0ull));
 }
 
+// The fold acc = RNE_m(rto(acc + s)) for two accumulators at a time, with
+// the arithmetic in packed FP32 pairs on the FMA pipe: rto is rto_word's
+// select, and RNE to m = 23 - ro mantissa bits is Veltkamp's split
+// hi = t - (t - v), t = v * (2^ro + 1), which for 1 <= ro <= 22 equals the
+// integer RNE of rne_word2 for every zero or normal v with |v| * (2^ro + 1)
+// finite (checked exhaustively over all FP32 patterns for every ro). The two
+// subtractions are fused multiply-adds by -1 (exact products), which keeps
+// signed zeros. The epilogue takes this fold only when the operands'
+// exponent ranges guarantee those conditions for every partial sum
+// (fast_fold_ok).
+__device__ __forceinline__ void fold2_fast(float& a0, float& a1, float s0, float s1, float sigma) {
+    const float2 a = make_float2(a0, a1), s = make_float2(s0, s1);
+    const float2 rd = __fadd2_rd(a, s), ru = __fadd2_ru(a, s);
+    const float2 v = make_float2(__uint_as_float(rto_word(rd.x, ru.x)),
+                                 __uint_as_float(rto_word(rd.y, ru.y)));
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 t = __fmul2_rn(v, make_float2(sigma, sigma));
+    const float2 h = __ffma2_rn(__ffma2_rn(v, m1, t), m1, t);   // t - (t - v)
+    a0 = h.x;
+    a1 = h.y;
+}
+
+constexpr int FAST_OFF = -100000;
+
+// Largest exponent-field sum (emax_a + emax_b) for which every partial sum v
+// of a K-long product keeps |v| * (2^ro + 1) finite: with |a| < 2^(emax_a -
+// 126) and |b| alike, |v| <= Kp * 2^(ea + eb) * G, G the growth of nchunks
+// roundings by at most (1 + 2^-(m+1)) (1 + 2^-23) each; two more bits of
+// margin cover the tensor cores' chunk sums and the dropped lo * lo term.
+int fast_fold_limit(int Kp, int chunk, int mbits) {
+    const int ro = 23 - mbits;
+    if (ro < 1 || ro > 22) return FAST_OFF;
+    const int nchunks = (Kp + chunk - 1) / chunk;
+    const double g = nchunks * std::log2((1.0 + std::ldexp(1.0, -(mbits + 1))) * (1.0 + 0x1p-23));
+    const int L = (int)std::ceil(std::log2((double)Kp)) + (int)std::ceil(g) + 2;
+    return 378 - ro - L;
+}
+
+// The fast fold is exact for the whole tile iff no partial sum can overflow
+// it (the limit above) and none can be an FP32 subnormal: every operand part
+// is a multiple of 2^(emin - 150), so every partial sum is a multiple of
+// 2^(emin_a + emin_b - 300), which must be at least 2^-126.
+__device__ __forceinline__ bool fast_fold_ok(const uint32_t (&r)[4], int lim) {
+    const int emax = (int)r[0] + (int)r[2];
+    const int emin = (255 - (int)r[1]) + (255 - (int)r[3]);
+    return lim != FAST_OFF && emax <= lim && emin >= 174;
+}
+
 // ---- tile sources ------------------------------------------------------------
 // Everything the three roles need to know about one 128 x 128 output tile.
 struct TileInfo {
@@ -261,6 +315,7 @@ struct TileInfo {
     // conv2d output (img_L > 0): column j = img * img_L + l of row i is
     // stored at D[img * img_stride + i * ldd + l]
     int64_t img_L, img_stride;
+    int fast_lim;               // fast_fold_limit of this GEMM
 };
 
 // One GEMM; its tensor maps are kernel parameters.
@@ -288,6 +343,7 @@ struct SingleSrc {
         ti.alpha = prm.alpha;
         ti.img_L = prm.img_L;
         ti.img_stride = prm.img_stride;
+        ti.fast_lim = prm.fast_lim;
         return ti;
     }
 };
@@ -300,7 +356,8 @@ struct GroupRow {
     int64_t ldd;
     int32_t M, N, Kp, chunk16, ro;
     float alpha;
-    int32_t pad[8];
+    int32_t fast_lim;
+    int32_t pad[7];
 };
 struct TileRef {
     int32_t task, m0, n0, pad;
@@ -311,13 +368,19 @@ struct SplitRow {
     __nv_bfloat16* hi;
     __nv_bfloat16* lo;
     int64_t item_begin;  // first 32 x 64 split item of this operand
-    int32_t kmajor, rows, K, R, Kp, pad;
+    int32_t kmajor, rows, K, R, Kp, operand;  // operand: 0 = A, 1 = B
 };
 struct GroupHeader {   // at the start of the device table; offsets from its base
     int32_t ntasks, ntiles, nsplit, pad;
     int64_t split_items;
     int64_t rows_off, tiles_off, splits_off;
     int* status;
+    // exponent ranges of all A and all B operands (zero in the prepared
+    // table; the split kernel raises them, the GEMM kernel reads them and its
+    // last CTA clears them, and the reader count, for the next launch)
+    uint32_t range[4];
+    uint32_t range_readers;
+    uint32_t pad2[3];
 };
 
 struct GroupedSrc {
@@ -344,6 +407,7 @@ struct GroupedSrc {
         ti.alpha = g->alpha;
         ti.img_L = 0;
         ti.img_stride = 0;
+        ti.fast_lim = g->fast_lim;
         return ti;
     }
 };
@@ -351,8 +415,13 @@ struct GroupedSrc {
 // ---- the persistent tensor-core body (shared by both launches) ---------------
 // ACCK: 0 RNE to ro mantissa bits; 2 / 3 a whole-format accumulator (acc_plan)
 // by the whole-range float rounding / by the integer rounding core.
+// range: the four exponent-range words the split kernels published (A's
+// largest field, 255 - its smallest non-zero field, the same for B);
+// reset_range: the last CTA to read them clears them (and range[4], the
+// reader count) for the next launch of the same device table.
 template <int ACCK, class Src>
 __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* smem_raw,
+                                       uint32_t* range, bool reset_range,
                                        const RoundPlan* acc_plan = nullptr) {
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                ~uintptr_t(1023));
@@ -361,6 +430,7 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
     // bars: full[STAGES], empty[STAGES], tfull[NBUF], tempty[NBUF], drain
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 2 * NBUF + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    uint32_t* range_s = tmem_slot + 2;  // four words
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -382,6 +452,14 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
         mbar_init(bar_drain, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int i = 0; i < 4; ++i)
+            range_s[i] = range ? *reinterpret_cast<volatile uint32_t*>(range + i) : 255u;
+        if (range && reset_range) {
+            __threadfence();
+            if (atomicAdd(range + 4, 1u) == gridDim.x - 1) {
+                for (int i = 0; i < 5; ++i) range[i] = 0;
+            }
+        }
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -424,42 +502,48 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
         }
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
+        // Lean issue loop (one thread): stage, phase, chunk position and
+        // TMEM buffer kept as counters (no divisions), descriptors as a
+        // per-stage base plus constant offsets (the start-address field,
+        // bits 0-13, is the byte address >> 4 and never carries: shared
+        // memory is below 256 KiB).
         if (lane == 0) {
-            uint32_t it = 0;      // stage counter
-            uint32_t cg = 0;      // global chunk counter
+            const uint64_t dbase = smem_desc_sw128(smem_u32(tiles));
+            constexpr uint64_t TSTEP = TILE_BYTES >> 4, SSTEP = STAGE_BYTES >> 4;
+            uint32_t s = 0, sph = 0;         // stage and its phase
+            uint32_t buf = 0, bph = 0;       // TMEM chunk buffer and its phase
             bool ok = true;
             for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
                 const TileInfo ti = src.get(tile);
                 const int ksteps = ti.Kp / SK;
-                const int k16 = ti.Kp / 16;
-                int kk16 = 0;
-                for (int ks = 0; ks < ksteps && ok; ++ks, ++it) {
-                    const uint32_t s = it % STAGES;
-                    if (!mbar_wait(bar_full + 8 * s, (it / STAGES) & 1u, abort_flag, status)) { ok = false; break; }
+                const int chunk16 = ti.chunk16;
+                int pos = 0;                 // k16 step within the chunk
+                for (int ks = 0; ks < ksteps && ok; ++ks) {
+                    if (!mbar_wait(bar_full + 8 * s, sph, abort_flag, status)) { ok = false; break; }
                     tc_fence_after();
-                    const uint32_t base = smem_u32(tiles + s * STAGE_BYTES);
-                    for (int j = 0; j < SK / 16; ++j, ++kk16) {
-                        const int pos = kk16 % ti.chunk16;
-                        const uint32_t buf = cg % NBUF;
+                    const uint64_t sd = dbase + s * SSTEP;
+                    const bool last_stage = ks == ksteps - 1;
+#pragma unroll
+                    for (int j = 0; j < SK / 16; ++j) {
                         if (pos == 0) {
-                            if (!mbar_wait(bar_tempty + 8 * buf, ((cg / NBUF) & 1u) ^ 1u, abort_flag, status)) { ok = false; break; }
+                            if (!mbar_wait(bar_tempty + 8 * buf, bph ^ 1u, abort_flag, status)) { ok = false; break; }
                             tc_fence_after();
                         }
                         const uint32_t d = tmem_base + buf * TBN;
-                        const uint64_t ahi = smem_desc_sw128(base + 0 * TILE_BYTES + j * 32);
-                        const uint64_t alo = smem_desc_sw128(base + 1 * TILE_BYTES + j * 32);
-                        const uint64_t bhi = smem_desc_sw128(base + 2 * TILE_BYTES + j * 32);
-                        const uint64_t blo = smem_desc_sw128(base + 3 * TILE_BYTES + j * 32);
+                        const uint64_t ahi = sd + 2 * j, alo = sd + TSTEP + 2 * j;
+                        const uint64_t bhi = sd + 2 * TSTEP + 2 * j, blo = sd + 3 * TSTEP + 2 * j;
                         umma_f16(d, ahi, bhi, pos > 0 ? 1u : 0u);
                         umma_f16(d, ahi, blo, 1u);
                         umma_f16(d, alo, bhi, 1u);
-                        if (pos == ti.chunk16 - 1 || kk16 == k16 - 1) {
+                        if (++pos == chunk16 || (last_stage && j == SK / 16 - 1)) {
                             umma_commit(bar_tfull + 8 * buf);
-                            ++cg;
+                            pos = 0;
+                            if (++buf == NBUF) { buf = 0; bph ^= 1u; }
                         }
                     }
                     if (!ok) break;
                     umma_commit(bar_empty + 8 * s);  // stage's smem free once its MMAs finish
+                    if (++s == STAGES) { s = 0; sph ^= 1u; }
                 }
             }
             // all issued MMAs complete before the TMEM is released
@@ -474,6 +558,9 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
         const uint32_t lane_base = tmem_base + ((uint32_t)(quarter * 32) << 16) + slice * EPI_COLS;
         uint32_t cg = 0;
         bool ok = true;
+        uint32_t rng[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) rng[i] = range_s[i];
         // every lane waits; the warp goes on only when all lanes saw the phase
         // complete, reconverged for the .sync.aligned TMEM loads
         auto wait_full = [&](uint32_t g) -> bool {
@@ -492,23 +579,33 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
             asm volatile("mov.u32 %0, 2;" : "=r"(two));
             const uint32_t half_m1 = ro > 0 ? (1u << (ro - 1)) - 1u : 0u;
             const uint32_t mask = ro > 0 ? ~((1u << ro) - 1u) : ~0u;
+            const bool fast = ACCK == 0 && fast_fold_ok(rng, ti.fast_lim);
+            const float sigma = (float)((1u << (ro & 31)) + 1u);
             float acc[EPI_COLS];
 #pragma unroll
             for (int i = 0; i < EPI_COLS; ++i) acc[i] = 0.0f;
             auto fold16 = [&](int off, const uint32_t (&r)[16]) {
                 if constexpr (ACCK == 0) {
+                    if (fast) {
 #pragma unroll
-                    for (int i = 0; i < 16; ++i)
-                        acc[off + i] = fold(acc[off + i], __uint_as_float(r[i]), ro, sh, two, half_m1, mask);
+                        for (int i = 0; i < 16; i += 2)
+                            fold2_fast(acc[off + i], acc[off + i + 1], __uint_as_float(r[i]),
+                                       __uint_as_float(r[i + 1]), sigma);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 16; ++i)
+                            acc[off + i] = fold(acc[off + i], __uint_as_float(r[i]), ro, sh, two, half_m1, mask);
+                    }
                 } else {
 #pragma unroll
                     for (int i = 0; i < 16; ++i)
                         acc[off + i] = fold_fmt<ACCK>(acc[off + i], __uint_as_float(r[i]), *acc_plan);
                 }
             };
-            // Four 16-column pieces per chunk, software-pipelined over two
-            // register sets: each piece loads while the previous one is
-            // folded, and piece 0 of chunk c+1 loads during piece 3 of chunk c.
+            // EPI_COLS / 16 pieces of 16 columns per chunk, software-pipelined
+            // over two register sets: each piece loads while the previous one
+            // is folded, and piece 0 of chunk c+1 loads during the last piece
+            // of chunk c.
             uint32_t ra[16], rb[16];
             if (!wait_full(cg)) { ok = false; break; }
             tmem_ld16(lane_base + (cg % NBUF) * TBN, ra);
@@ -520,16 +617,18 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                 fold16(0, ra);
                 pin16<0>(acc);
                 tmem_ld_wait16(rb);
-                tmem_ld16(col + 32, ra);
-                pin16<16>(acc);
-                fold16(16, rb);
-                pin16<16>(acc);
-                tmem_ld_wait16(ra);
-                tmem_ld16(col + 48, rb);
-                pin16<32>(acc);
-                fold16(32, ra);
-                pin16<32>(acc);
-                tmem_ld_wait16(rb);
+                if constexpr (EPI_COLS == 64) {
+                    tmem_ld16(col + 32, ra);
+                    pin16<16>(acc);
+                    fold16(16, rb);
+                    pin16<16>(acc);
+                    tmem_ld_wait16(ra);
+                    tmem_ld16(col + 48, rb);
+                    pin16<32>(acc);
+                    fold16(32, ra);
+                    pin16<32>(acc);
+                    tmem_ld_wait16(rb);
+                }
                 tc_fence_before();
                 mbar_arrive(bar_tempty + 8 * (cg % NBUF));   // all of chunk c is in registers
                 ++cg;
@@ -538,9 +637,9 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                     if (!wait_full(cg)) { ok = false; break; }
                     tmem_ld16(lane_base + (cg % NBUF) * TBN, ra);
                 }
-                pin16<48>(acc);
-                fold16(48, rb);
-                pin16<48>(acc);
+                pin16<EPI_COLS - 16>(acc);
+                fold16(EPI_COLS - 16, rb);
+                pin16<EPI_COLS - 16>(acc);
                 if (more) tmem_ld_wait16(ra);
             }
             if (!ok) break;
@@ -597,14 +696,14 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
     src.m[2] = &tm_bhi;
     src.m[3] = &tm_blo;
     src.prm = prm;
-    tc_body<ACCK>(src, prm.status, smem_raw, &prm.acc_plan);
+    tc_body<ACCK>(src, prm.status, smem_raw, prm.range, false, &prm.acc_plan);
 }
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 gemm_tc_grouped_kernel(const GroupHeader* __restrict__ h) {
     extern __shared__ uint8_t smem_raw[];
     GroupedSrc src{h};
-    tc_body<0>(src, h->status, smem_raw);
+    tc_body<0>(src, h->status, smem_raw, const_cast<uint32_t*>(h->range), true);
 }
 
 // ---- operand split: FP32 -> K-major BF16 hi/lo, zero padded -----------------
@@ -614,7 +713,8 @@ gemm_tc_grouped_kernel(const GroupHeader* __restrict__ h) {
 // lo = RN_bf16(x - hi) (exact difference), lo = 0 for non-finite x.
 __device__ __forceinline__ void split_tile(const float* __restrict__ src, int64_t ld, int kmajor,
                                            int rows, int K, int R, int Kp, __nv_bfloat16* hi,
-                                           __nv_bfloat16* lo, int tr, int tk, float (*tile)[65]) {
+                                           __nv_bfloat16* lo, int tr, int tk, float (*tile)[65],
+                                           ExpRange& er) {
     const int r0 = tr * 32, k0 = tk * 64;
     const int t = threadIdx.x;
     if (kmajor) {
@@ -631,22 +731,24 @@ __device__ __forceinline__ void split_tile(const float* __restrict__ src, int64_
         }
     }
     __syncthreads();
-    split_store_tile(tile, r0, k0, R, Kp, hi, lo);
+    split_store_tile(tile, r0, k0, R, Kp, hi, lo, er);
     __syncthreads();
 }
 
 // blockIdx.z walks a strided batch: operand z at src + z * src_stride, its
-// split at hi / lo + z * R * Kp.
+// split at hi / lo + z * R * Kp. range: the operand's two exponent-range words.
 __global__ void __launch_bounds__(256)
 split_bf16_kernel(const float* __restrict__ src, int64_t ld, int64_t src_stride, int kmajor,
                   int rows, int K, int R, int Kp, int batch, __nv_bfloat16* __restrict__ hi,
-                  __nv_bfloat16* __restrict__ lo) {
+                  __nv_bfloat16* __restrict__ lo, uint32_t* __restrict__ range) {
     __shared__ float tile[32][65];
+    ExpRange er;
     for (int z = blockIdx.z; z < batch; z += gridDim.z) {
         const int64_t off = (int64_t)z * R * Kp;
         split_tile(src + (int64_t)z * src_stride, ld, kmajor, rows, K, R, Kp, hi + off, lo + off,
-                   blockIdx.y, blockIdx.x, tile);
+                   blockIdx.y, blockIdx.x, tile, er);
     }
+    range_flush(range, er);
 }
 
 // All operands of a grouped launch: items are 32 x 64 tiles, walked
@@ -658,6 +760,7 @@ split_grouped_kernel(const GroupHeader* __restrict__ h) {
     const SplitRow* rows = reinterpret_cast<const SplitRow*>(
         reinterpret_cast<const uint8_t*>(h) + h->splits_off);
     const int nrows = h->nsplit;
+    ExpRange era, erb;  // all A operands, all B operands
     // the device status word starts every launch cleared (this kernel runs
     // first on the stream; the GEMM kernel only ever sets it)
     if (blockIdx.x == 0 && threadIdx.x == 0) *h->status = 0;
@@ -676,9 +779,16 @@ split_grouped_kernel(const GroupHeader* __restrict__ h) {
         __syncthreads();
         const int64_t local = item - r.item_begin;
         const int tiles_k = r.Kp / 64;
+        ExpRange cur;
         split_tile(r.src, r.ld, r.kmajor, r.rows, r.K, r.R, r.Kp, r.hi, r.lo,
-                   (int)(local / tiles_k), (int)(local % tiles_k), tile);
+                   (int)(local / tiles_k), (int)(local % tiles_k), tile, cur);
+        ExpRange& dst = r.operand ? erb : era;
+        dst.emax = max(dst.emax, cur.emax);
+        dst.emin_c = max(dst.emin_c, cur.emin_c);
     }
+    uint32_t* range = const_cast<uint32_t*>(h->range);
+    range_flush(range, era);
+    range_flush(range + 2, erb);
 }
 
 // ---- host side ---------------------------------------------------------------
@@ -694,6 +804,7 @@ WsLayout ws_layout(int M, int N, int K, int batch) {
     w.batch = batch;
     const size_t a = (size_t)batch * w.Mp * w.Kp * 2, b = (size_t)batch * w.Np * w.Kp * 2;
     w.status = 0;
+    w.range = 4;
     w.ahi = 1024;
     w.alo = align_up(w.ahi + a, 1024);
     w.bhi = align_up(w.alo + a, 1024);
@@ -759,17 +870,20 @@ int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float*
     auto* bhi = reinterpret_cast<__nv_bfloat16*>(ws + w.bhi);
     auto* blo = reinterpret_cast<__nv_bfloat16*>(ws + w.blo);
     int* status = reinterpret_cast<int*>(ws + w.status);
-    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), st);
+    auto* range = reinterpret_cast<uint32_t*>(ws + w.range);
+    cudaError_t e = cudaMemsetAsync(status, 0, WS_HEADER_CLEAR, st);
     if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
 
     dim3 sb256(256);
     const unsigned gz = batch < 65535 ? batch : 65535;
     split_bf16_kernel<<<dim3(w.Kp / 64, w.Mp / 32, gz), sb256, 0, st>>>(A, lda, sa, ta ? 0 : 1, M, K,
-                                                                        w.Mp, w.Kp, batch, ahi, alo);
+                                                                        w.Mp, w.Kp, batch, ahi, alo,
+                                                                        range);
     int rc = check_launch("split_bf16_kernel(A)");
     if (rc) return rc;
     split_bf16_kernel<<<dim3(w.Kp / 64, w.Np / 32, gz), sb256, 0, st>>>(B, ldb, sb, tb ? 1 : 0, N, K,
-                                                                        w.Np, w.Kp, batch, bhi, blo);
+                                                                        w.Np, w.Kp, batch, bhi, blo,
+                                                                        range + 2);
     if ((rc = check_launch("split_bf16_kernel(B)"))) return rc;
     return launch_tc_presplit(ws, w, D, ldd, sd, M, N, mbits, alpha, chunk, 0, 0, stream, acc_fmt);
 }
@@ -813,6 +927,8 @@ int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, in
         p.acc_kind = acc_fmt->uni == 1 ? 2 : 3;
         p.acc_plan = *acc_fmt;
     }
+    p.range = reinterpret_cast<uint32_t*>(ws + w.range);
+    p.fast_lim = acc_fmt ? FAST_OFF : fast_fold_limit(w.Kp, chunk, mbits);
 
     int dev = 0;
     cudaGetDevice(&dev);
@@ -1042,13 +1158,16 @@ int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* w
         r.chunk16 = t.chunk / 16;
         r.ro = 23 - t.accum_mant_bits;
         r.alpha = t.alpha;
+        r.fast_lim = g.Kp[i] > 0 ? fast_fold_limit(g.Kp[i], t.chunk, t.accum_mant_bits) : FAST_OFF;
         SplitRow& sa = splits[2 * i];
         SplitRow& sbr = splits[2 * i + 1];
         sa.src = t.A; sa.ld = t.lda; sa.kmajor = t.trans_a ? 0 : 1; sa.rows = t.M; sa.K = t.K;
         sa.R = g.Mp[i]; sa.Kp = g.Kp[i]; sa.hi = ahi; sa.lo = alo; sa.item_begin = item;
+        sa.operand = 0;
         item += (int64_t)(g.Mp[i] / 32) * (g.Kp[i] / 64);
         sbr.src = t.B; sbr.ld = t.ldb; sbr.kmajor = t.trans_b ? 1 : 0; sbr.rows = t.N; sbr.K = t.K;
         sbr.R = g.Np[i]; sbr.Kp = g.Kp[i]; sbr.hi = bhi; sbr.lo = blo; sbr.item_begin = item;
+        sbr.operand = 1;
         item += (int64_t)(g.Np[i] / 32) * (g.Kp[i] / 64);
         if (g.Mp[i] == 0 || g.Np[i] == 0 || g.Kp[i] == 0) continue;
         int rc;

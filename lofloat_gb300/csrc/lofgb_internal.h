@@ -110,10 +110,15 @@ int check_gemm_args(const void* A, int64_t lda, int ta, const void* B, int64_t l
 // (Mp, Np multiples of 128, Kp of 64), each 1024-byte aligned.
 // A strided batch of GEMMs stacks `batch` such splits (A rows b*Mp.., B rows
 // b*Np..) in each operand region.
+// Four words after the status word hold the exponent ranges of A and B
+// (tc_split.cuh ExpRange: largest field, 255 - smallest non-zero field),
+// which the split kernels publish and the epilogue reads to pick its fold;
+// the host clears WS_HEADER_CLEAR bytes from the status word before a launch.
 struct WsLayout {
-    size_t status, ahi, alo, bhi, blo, total;
+    size_t status, range, ahi, alo, bhi, blo, total;
     int Mp, Np, Kp, batch;
 };
+constexpr size_t WS_HEADER_CLEAR = 32;
 WsLayout ws_layout(int M, int N, int K, int batch = 1);
 // Runs the chunked tensor-core GEMM on operands already split into `ws`
 // (laid out by ws_layout) whose status word the caller has cleared.

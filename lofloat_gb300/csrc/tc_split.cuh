@@ -9,18 +9,63 @@
 namespace lofgb {
 namespace {
 
+// Exponent range of an operand, for the tensor-core epilogue's choice of
+// fold: every thread keeps the largest FP32 exponent field it has seen (255
+// for inf / NaN) and 255 minus the smallest field of a non-zero value (255
+// for an FP32 subnormal); range_flush publishes them with atomicMax into two
+// words that the host cleared before the split.
+struct ExpRange {
+    uint32_t emax = 0, emin_c = 0;
+    __device__ __forceinline__ void add(float x) {
+        const uint32_t b = __float_as_uint(x) & 0x7FFFFFFFu;
+        const uint32_t f = b >> 23;
+        emax = max(emax, f);
+        if (b) emin_c = max(emin_c, 255u - f);
+    }
+};
+
+// CTA-wide maximum of both words, then one atomicMax per word from thread 0,
+// skipped when the published value is already as large (most CTAs).
+// Called by all threads of the CTA (blockDim.x a multiple of 32, <= 1024);
+// range == nullptr publishes nothing.
+__device__ __forceinline__ void range_flush(uint32_t* range, const ExpRange& er) {
+    __shared__ uint32_t red[2][32];
+    const uint32_t a = __reduce_max_sync(0xFFFFFFFFu, er.emax);
+    const uint32_t b = __reduce_max_sync(0xFFFFFFFFu, er.emin_c);
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        red[0][w] = a;
+        red[1][w] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && range) {
+        uint32_t ma = 0, mb = 0;
+        for (int i = 0; i < nw; ++i) {
+            ma = max(ma, red[0][i]);
+            mb = max(mb, red[1][i]);
+        }
+        if (ma > *reinterpret_cast<volatile uint32_t*>(range)) atomicMax(range, ma);
+        if (mb > *reinterpret_cast<volatile uint32_t*>(range + 1)) atomicMax(range + 1, mb);
+    }
+    __syncthreads();
+}
+
 // Writes a staged 32-row x 64-k FP32 tile (tile[row][k]) to the K-major BF16
 // operands hi / lo (R rows x Kp columns) at rows r0.., columns k0..:
 // hi = RZ_bf16(x), lo = RN_bf16(x - hi) (the difference is exact in FP32),
-// lo = 0 for non-finite x. Called by all 256 threads of the CTA.
+// lo = 0 for non-finite x; er collects the exponent range of the values.
+// Called by all 256 threads of the CTA.
 __device__ __forceinline__ void split_store_tile(const float (*tile)[65], int r0, int k0, int R,
-                                                 int Kp, __nv_bfloat16* hi, __nv_bfloat16* lo) {
+                                                 int Kp, __nv_bfloat16* hi, __nv_bfloat16* lo,
+                                                 ExpRange& er) {
     for (int i = threadIdx.x; i < 32 * 32; i += 256) {
         const int rr = i / 32, kp = (i % 32) * 2;
         const int r = r0 + rr, k = k0 + kp;
         if (r >= R || k >= Kp) continue;
         __nv_bfloat162 h2, l2;
         const float x0 = tile[rr][kp], x1 = tile[rr][kp + 1];
+        er.add(x0);
+        er.add(x1);
         const __nv_bfloat16 h0 = __float2bfloat16_rz(x0), h1 = __float2bfloat16_rz(x1);
         float d0 = x0 - __bfloat162float(h0), d1 = x1 - __bfloat162float(h1);
         if (!isfinite(x0)) d0 = 0.0f;

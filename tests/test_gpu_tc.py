@@ -100,6 +100,28 @@ def test_exact_chunk_sums_bitexact(chunk, mbits):
         np.count_nonzero(got.view(np.uint32) != want.view(np.uint32))
 
 
+@pytest.mark.parametrize("scale_a,scale_b", [(2.0**-70, 2.0**-40), (2.0**55, 2.0**45), (1.0, 1.0)])
+@pytest.mark.parametrize("mbits", [5, 14])
+def test_fold_choice_by_exponent_range(scale_a, scale_b, mbits):
+    """The epilogue folds on the FMA pipe only when the operands' exponent
+    ranges rule out subnormal and overflowing partial sums, and with the
+    integer rounding otherwise. Tiny operands (partial sums down to 2^-110,
+    whose smallest multiple would be subnormal), huge operands (partial sums
+    near 2^125, where the FMA-pipe rounding would overflow) and plain ones:
+    exact chunk sums, so every case must equal the CPU chunked model bit for
+    bit."""
+    rng = np.random.default_rng(mbits + int(np.log2(scale_a)) + 200)
+    M, N, K = 128, 160, 512
+    A = (rng.integers(-600, 601, (M, K)) * scale_a).astype(np.float32)
+    B = (rng.integers(-100, 101, (K, N)) * scale_b).astype(np.float32)
+    got = from_gpu(lg.gemm(to_gpu(A), to_gpu(B), mbits, variant="tc", chunk=64))
+    _status_ok()
+    want = O.gemm_chunked(A, B, mbits, 64)
+    assert np.all(np.isfinite(want))
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
+        np.count_nonzero(got.view(np.uint32) != want.view(np.uint32))
+
+
 def test_exact_inputs_match_plain():
     """Small integers: every partial sum is exact, so all accumulation orders
     agree (the reference's exact-input check, test/test_blis_lof_accum.cpp:200-235)."""
