@@ -19,6 +19,8 @@ import torch.nn as nn
 from . import binding as lof
 from ._custom_ops import register_format
 from .formats import create_e8m0_params, create_p3109_params
+from .pwl import pwl_table
+from .pwl import silu as pwl_silu_fn
 
 
 class STERound(torch.autograd.Function):
@@ -639,9 +641,12 @@ class _PWLSiLUApprox(torch.autograd.Function):
 
 class PWLSiLU(nn.Module):
     """SiLU from a piecewise-linear table of 2^lut_bits uniform segments on
-    [-R, R], relu outside (LoFloat/layers.py:1072-1146). The knot values follow
-    the reference's "uniform" / "midpoint" / "minimax" constructions in the
-    buffer's dtype."""
+    [-R, R], relu outside (LoFloat/layers.py:1072-1146), run by the
+    pwl_silu kernel (one read, one write); backward is the analytic SiLU
+    derivative. The table is built by pwl.pwl_table ('uniform', 'midpoint'
+    or 'minimax'). The kernel holds tables of up to 4096 segments
+    (lut_bits <= 12); `use_ext` is accepted for the reference's signature,
+    and there is no other path."""
 
     def __init__(self, R=8.0, lut_bits=4, lut_method="minimax", use_ext=True):
         super().__init__()
@@ -650,50 +655,18 @@ class PWLSiLU(nn.Module):
         self.lut_size = 1 << lut_bits
         if self.lut_size % 2 != 0:
             raise ValueError("lut_size must be even so x=0 is a knot.")
-        self.use_ext = use_ext and self.lut_size <= 4096
+        if self.lut_size > 4096:
+            raise ValueError(f"lut_bits {lut_bits}: the pwl_silu kernel holds at most 4096 segments")
+        self.use_ext = True
         self.register_buffer("lut", torch.empty(self.lut_size + 1))
         self.init_lut(lut_method)
 
-    @staticmethod
-    def _silu(x):
-        return x * torch.sigmoid(x)
-
     def init_lut(self, method="minimax"):
-        n = self.lut_size
-        knots = torch.linspace(-self.R, self.R, n + 1, dtype=self.lut.dtype)
-        fk = self._silu(knots)
-        if method == "uniform":
-            lut = fk.clone()
-        elif method == "midpoint":
-            mids = 0.5 * (knots[:-1] + knots[1:])
-            lut = fk.clone()
-            lut[1:-1] = self._silu(mids)[:-1]
-        elif method == "minimax":
-            mids = 0.5 * (knots[:-1] + knots[1:])
-            delta = self._silu(mids) - 0.5 * (fk[:-1] + fk[1:])
-            c = torch.empty_like(fk)
-            c[0] = delta[0] / 2
-            c[1:-1] = (delta[:-1] + delta[1:]) / 4
-            c[-1] = delta[-1] / 2
-            lut = fk + c
-        else:
-            raise ValueError(f"Unknown lut_method {method!r}")
-        self.lut.copy_(lut)
+        self.lut.copy_(pwl_table(pwl_silu_fn, -self.R, self.R, self.lut_size, method, self.lut.dtype))
         self.lut_method = method
 
     def forward(self, x):
-        if self.use_ext:
-            return _PWLSiLUApprox.apply(x, self.lut, self.R)
-        return self._forward_ref(x)
-
-    def _forward_ref(self, x):
-        """The torch op chain the kernel replaces (kept for comparison)."""
-        n, r = self.lut_size, self.R
-        u = (x.clamp(-r, r) + r) * (n / (2 * r))
-        idx = u.long().clamp_(max=n - 1)
-        frac = u - idx.to(x.dtype)
-        out = torch.lerp(self.lut[idx], self.lut[idx + 1], frac)
-        return torch.where(x.abs() > r, torch.relu(x), out)
+        return _PWLSiLUApprox.apply(x, self.lut, self.R)
 
 
 # ---- attention -------------------------------------------------------------------

@@ -14,6 +14,8 @@ import math
 import torch
 import torch.nn as nn
 
+from .pwl import inv_sqrt, pwl_table
+
 
 def _scale_buffer(scale, num_features):
     if isinstance(scale, torch.Tensor):
@@ -162,26 +164,7 @@ class PWLBatchNorm(_BatchNormBase):
         self.init_lut(lut_method)
 
     def init_lut(self, method="minimax"):
-        n = self.lut_size
-        knots = torch.linspace(1.0, 2.0, n + 1, dtype=self.lut.dtype)
-        fk = 1.0 / knots.sqrt()
-        if method == "uniform":
-            lut = fk.clone()
-        elif method == "midpoint":
-            mids = 0.5 * (knots[:-1] + knots[1:])
-            lut = fk.clone()
-            lut[1:-1] = (1.0 / mids.sqrt())[:-1]
-        elif method == "minimax":
-            mids = 0.5 * (knots[:-1] + knots[1:])
-            delta = 1.0 / mids.sqrt() - 0.5 * (fk[:-1] + fk[1:])
-            c = torch.empty_like(fk)
-            c[0] = delta[0] / 2
-            c[1:-1] = (delta[:-1] + delta[1:]) / 4
-            c[-1] = delta[-1] / 2
-            lut = fk + c
-        else:
-            raise ValueError(f"Unknown lut_method {method!r}")
-        self.lut.copy_(lut)
+        self.lut.copy_(pwl_table(inv_sqrt, 1.0, 2.0, self.lut_size, method, self.lut.dtype))
         self.lut_method = method
 
     def _rsqrt_pwl(self, v):

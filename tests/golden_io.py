@@ -18,6 +18,12 @@ def verify_sha(name):
         return hashlib.sha256(fh.read()).hexdigest() == manifest()["files"][name]["sha256"]
 
 
+def load(name):
+    """One fixture file, after checking it against its MANIFEST.json sha256."""
+    assert verify_sha(name), f"{name} does not match MANIFEST.json"
+    return np.load(os.path.join(GOLDEN, name))
+
+
 def cases(group):
     """Yield (case_name, dict of arrays) for one fixture group."""
     z = np.load(os.path.join(GOLDEN, f"golden_{group}.npz"))

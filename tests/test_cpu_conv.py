@@ -76,12 +76,19 @@ def test_conv_oracle_column_sample():
     assert not flat_part[:40].any() and not flat_part[60:].any()
 
 
-def test_pwl_oracle_against_torch_chain():
+def test_pwl_oracle_against_interpolation_formula():
+    """The oracle against the table interpolation written out in float64:
+    u = (clamp(x) + R) n / 2R, i = min(floor(u), n - 1),
+    y = T_i + (u - i)(T_(i+1) - T_i), relu outside [-R, R]."""
     import lofloat_gb300 as lg
     m = lg.PWLSiLU(R=8.0, lut_bits=6)
     x = (np.random.default_rng(3).standard_normal(20000) * 5).astype(np.float32)
     got = O.pwl_silu(x, m.lut.numpy(), 8.0)
-    ref = m._forward_ref(torch.from_numpy(x)).numpy()
+    t = m.lut.numpy().astype(np.float64)
+    u = (np.clip(x.astype(np.float64), -8, 8) + 8) * (64 / 16)
+    i = np.minimum(np.floor(u).astype(np.int64), 63)
+    ref = t[i] + (u - i) * (t[i + 1] - t[i])
+    ref = np.where(np.abs(x) > 8, np.maximum(x, 0), ref)
     assert np.allclose(got, ref, atol=2e-6, rtol=1e-6)
     knots = np.linspace(-8.0, 8.0, 65, dtype=np.float32)[:-1]
     assert same_bits(O.pwl_silu(knots, m.lut.numpy(), 8.0), m.lut.numpy()[:-1])
