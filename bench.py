@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--only", default=None,
                     choices=["mx", "round_rne", "round_sr", "gemm_plain", "gemm_tc", "conv_plain",
                              "conv_tc", "pwl", "encode", "decode", "encode_fp6", "decode_fp6",
-                             "grouped_round"],
+                             "grouped_round", "bn_train", "bn_eval"],
                     help="run one workload's kernel warmup+steps times and exit (for ncu captures)")
     ap.add_argument("--size", default="full", choices=["full", "small"],
                     help="with --only: full-size workload or a small case (GEMM 1024^3)")
@@ -389,6 +389,38 @@ def conv_workloads(torch, lg, dev, peaks):
     out["pwl_silu_2^26_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)
     del xs, ys
     out.update(codec_workloads(torch, lg, dev, peaks))
+    out.update(bn_workloads(torch, lg, dev, peaks))
+    return out
+
+
+BN_SHAPE = (32, 256, 56, 56)
+
+
+def bn_workloads(torch, lg, dev, peaks):
+    """BatchNorm approximations on an NCHW 32x256x56x56 FP32 activation
+    (103 MB): training-mode forward (statistics + fused normalise/affine) of
+    each variant, and the eval-mode forward (normalise/affine only). GB/s at
+    8 B per element (one read and one write: the least any implementation
+    moves); the statistics passes read the input again, mostly from L2."""
+    out = {}
+    stream = torch.cuda.current_stream(dev)
+    g = torch.Generator(device=dev).manual_seed(9)
+    x = torch.randn(*BN_SHAPE, device=dev, generator=g) * 2 + 0.5
+    nbytes = x.numel() * 8
+    for name, cls in (("l1", lg.L1BatchNorm), ("linf", lg.LinfBatchNorm), ("fisr", lg.FISRBatchNorm),
+                      ("pwl", lg.PWLBatchNorm)):
+        m = cls(BN_SHAPE[1]).to(dev)
+        for mode in ("train", "eval"):
+            m.train(mode == "train")
+            with torch.no_grad():
+                fn = lambda: m(x)  # noqa: E731
+                for _ in range(3):
+                    fn()
+                ms = time_batched(torch, fn, stream)
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            out[f"bn_{name}_{mode}_GBs"] = round(gbs, 1)
+            out[f"bn_{name}_{mode}_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)
+    out["bn_note"] = "NCHW 32x256x56x56 f32; 8 B/elem; train = statistics + normalise"
     return out
 
 
@@ -817,6 +849,14 @@ def run_only(args):
         fn = (lambda: lg.lof_encode(x, fmt, out=packed)) if args.only.startswith("encode") else \
             (lambda: lg.lof_decode(packed, n, fmt, out=y))  # noqa: E731
         work, unit = n * (4 + bits / 8), "GB/s"
+    elif args.only in ("bn_train", "bn_eval"):
+        x = torch.randn(*BN_SHAPE, device=dev) * 2 + 0.5
+        m = lg.L1BatchNorm(BN_SHAPE[1]).to(dev).train(args.only == "bn_train")
+
+        def fn():
+            with torch.no_grad():
+                return m(x)
+        work, unit = x.numel() * 8, "GB/s"
     elif args.only == "grouped_round":
         gr = grouped_round_case(torch, lg, dev)[0]
         fn = gr

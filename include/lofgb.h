@@ -391,6 +391,42 @@ int lofgb_pwl_silu_f64(const double* in, double* out, int64_t n, const float* lu
 int lofgb_pwl_silu_f16(const uint16_t* in, uint16_t* out, int64_t n, const float* lut,
                        int segments, float R, void* stream);
 
+/* ---- BatchNorm approximations ------------------------------------------------
+ * Replace the torch compositions of L1BatchNorm, LinfBatchNorm, FISRBatchNorm
+ * and PWLBatchNorm (LoFloat/layers.py:805-1047). x is [n, c, inner]
+ * contiguous FP32 (NCHW: inner = H*W; (N, C): inner = 1); channel ch holds the
+ * n rows of inner values at (nn*c + ch)*inner.
+ *
+ * lofgb_bn_stats_f32 computes per channel the FP32 mean and one deviation
+ * statistic:
+ *   LOFGB_BN_MEAN_ABS_DEV  mean |x - mean| (L1BatchNorm's mad),
+ *   LOFGB_BN_MAX_ABS_DEV   max |x - mean| (LinfBatchNorm's maxdev; NaN if any),
+ *   LOFGB_BN_VARIANCE      the biased variance (FISR / PWL),
+ * with the centring x - mean done in FP32 with the FP32 mean, as the
+ * reference does, and the sums in double. running_mean / running_dev (NULL:
+ * skipped) are updated to r (1 - momentum) + momentum s in FP32. Needs
+ * lofgb_bn_workspace_size(n, c, inner) bytes of 16-byte aligned workspace.
+ *
+ * lofgb_bn_apply_f32 writes, per element, in FP32 and the reference's order,
+ *   LOFGB_BN_DIVIDE  y = ((x - mean) / (dev + eps)) * scale   (scale NULL: no multiply)
+ *   LOFGB_BN_FISR    y = (x - mean) * fisr(dev + eps)
+ *   LOFGB_BN_PWL     y = (x - mean) * pwl(dev + eps)
+ * then y = y * weight + bias when weight is not NULL. fisr is the bit-trick
+ * seed 0x5F3759DF - (bits >> 1) with two Newton steps y (1.5 - (v/2) y y);
+ * pwl interpolates `lut` (segments + 1 knots of 1/sqrt over [1, 2]) at the
+ * mantissa m in [1, 2) of v = m 2^e and multiplies by 2^-floor(e/2), and by
+ * 1/sqrt(2) in FP32 for odd e. x == y is allowed. */
+enum lofgb_bn_stat { LOFGB_BN_MEAN_ABS_DEV = 0, LOFGB_BN_MAX_ABS_DEV = 1, LOFGB_BN_VARIANCE = 2 };
+enum lofgb_bn_norm { LOFGB_BN_DIVIDE = 0, LOFGB_BN_FISR = 1, LOFGB_BN_PWL = 2 };
+size_t lofgb_bn_workspace_size(int64_t n, int64_t c, int64_t inner);
+int lofgb_bn_stats_f32(const float* x, int64_t n, int64_t c, int64_t inner, int stat, float* mean,
+                       float* dev, float* running_mean, float* running_dev, float momentum,
+                       void* workspace, size_t workspace_bytes, void* stream);
+int lofgb_bn_apply_f32(const float* x, float* y, int64_t n, int64_t c, int64_t inner,
+                       const float* mean, const float* dev, float eps, int norm, const float* scale,
+                       const float* weight, const float* bias, const float* lut, int segments,
+                       void* stream);
+
 /* ---- low-precision storage codec -------------------------------------------
  * Replaces LoF_encode_cuda / LoF_decode_cuda and their CPU twins
  * (src/lo_pack.hpp:109-532): FP32 values are converted to n-bit codes of a

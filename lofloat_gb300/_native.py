@@ -99,6 +99,11 @@ SIGNATURES = [
     ("lofgb_pwl_silu_f32", _i32, [_vp, _vp, _i64, _vp, _i32, _f32, _vp]),
     ("lofgb_pwl_silu_f64", _i32, [_vp, _vp, _i64, _vp, _i32, _f32, _vp]),
     ("lofgb_pwl_silu_f16", _i32, [_vp, _vp, _i64, _vp, _i32, _f32, _vp]),
+    ("lofgb_bn_workspace_size", _sz, [_i64, _i64, _i64]),
+    ("lofgb_bn_stats_f32", _i32, [_vp, _i64, _i64, _i64, _i32, _vp, _vp, _vp, _vp, _f32, _vp, _sz,
+                                  _vp]),
+    ("lofgb_bn_apply_f32", _i32, [_vp, _vp, _i64, _i64, _i64, _vp, _vp, _f32, _i32, _vp, _vp, _vp,
+                                  _vp, _i32, _vp]),
     ("lofgb_packed_size", _sz, [_i32, _i64]),
     ("lofgb_encode_f32", _i32, [_vp, _vp, _i64, C.POINTER(LofgbCodecFormat), _i32, _i32, _i32, _i32,
                                 _u64, _u64, _vp]),

@@ -484,6 +484,96 @@ def pwl_silu(input: torch.Tensor, lut: torch.Tensor, R: float, *,
     return y
 
 
+# ---- BatchNorm approximations (LoFloat/layers.py:805-1047) ------------------------
+class BnStat(enum.IntEnum):
+    MEAN_ABS_DEV = 0
+    MAX_ABS_DEV = 1
+    VARIANCE = 2
+
+
+class BnNorm(enum.IntEnum):
+    DIVIDE = 0
+    FISR = 1
+    PWL = 2
+
+
+def _bn_view(x: torch.Tensor, what: str) -> tuple[torch.Tensor, int, int, int]:
+    _require_cuda(x, what)
+    if x.dim() < 2:
+        raise RuntimeError(f"{what}: input must be (N, C, *)")
+    if x.dtype != torch.float32:
+        raise RuntimeError(f"{what}: float32 input required (got {x.dtype})")
+    x = x.contiguous()
+    n, c = x.shape[0], x.shape[1]
+    inner = x.numel() // max(1, n * c)
+    return x, n, c, inner
+
+
+def _chan(t, c: int, dev, what: str):
+    if t is None:
+        return None
+    t = t.detach()
+    if t.numel() != c or t.dtype != torch.float32 or t.device != dev:
+        raise RuntimeError(f"{what}: per-channel tensors must be float32 with {c} elements on {dev}")
+    return t.contiguous()
+
+
+def bn_stats(x: torch.Tensor, stat: BnStat, *, running_mean: torch.Tensor | None = None,
+             running_dev: torch.Tensor | None = None, momentum: float = 0.1):
+    """Per-channel FP32 mean and deviation statistic of x (N, C, *) in one or
+    two passes (lofgb_bn_stats_f32). running_mean / running_dev, if given
+    (float32, contiguous, C elements), are updated in place to
+    r (1 - momentum) + momentum s."""
+    x, n, c, inner = _bn_view(x, "bn_stats")
+    L = _native.lib()
+    mean = torch.empty(c, dtype=torch.float32, device=x.device)
+    dev = torch.empty_like(mean)
+    for r in (running_mean, running_dev):
+        if r is not None and (r.numel() != c or r.dtype != torch.float32 or not r.is_contiguous()
+                              or r.device != x.device):
+            raise RuntimeError("bn_stats: running buffers must be contiguous float32 with C elements")
+    with torch.cuda.device(x.device):
+        ws = _workspace(x.device, int(L.lofgb_bn_workspace_size(n, c, inner)))
+        check(L.lofgb_bn_stats_f32(x.data_ptr(), n, c, inner, int(stat), mean.data_ptr(),
+                                   dev.data_ptr(),
+                                   running_mean.data_ptr() if running_mean is not None else None,
+                                   running_dev.data_ptr() if running_dev is not None else None,
+                                   float(momentum), ws.data_ptr(), ws.numel(), _stream(x)),
+              "bn_stats")
+    return mean, dev
+
+
+def bn_apply(x: torch.Tensor, mean: torch.Tensor, dev: torch.Tensor, eps: float, norm: BnNorm, *,
+             scale: torch.Tensor | None = None, weight: torch.Tensor | None = None,
+             bias: torch.Tensor | None = None, lut: torch.Tensor | None = None,
+             out: torch.Tensor | None = None) -> torch.Tensor:
+    """Fused normalise + scale + affine of x (N, C, *) with per-channel
+    statistics (lofgb_bn_apply_f32)."""
+    x, n, c, inner = _bn_view(x, "bn_apply")
+    L = _native.lib()
+    mean, dev = _chan(mean, c, x.device, "bn_apply"), _chan(dev, c, x.device, "bn_apply")
+    scale, weight, bias = (_chan(t, c, x.device, "bn_apply") for t in (scale, weight, bias))
+    if (weight is None) != (bias is None):
+        raise RuntimeError("bn_apply: weight and bias go together")
+    segs = 0
+    if int(norm) == BnNorm.PWL:
+        if lut is None or lut.dim() != 1 or lut.numel() < 2:
+            raise RuntimeError("bn_apply: the PWL normaliser needs a 1-D table")
+        lut = lut.detach().to(device=x.device, dtype=torch.float32).contiguous()
+        segs = lut.numel() - 1
+    y = torch.empty_like(x) if out is None else out
+    if y.shape != x.shape or y.dtype != x.dtype or not y.is_contiguous() or y.device != x.device:
+        raise RuntimeError("bn_apply: out must be a contiguous tensor like input")
+
+    def ptr(t):
+        return t.data_ptr() if t is not None else None
+    with torch.cuda.device(x.device):
+        check(L.lofgb_bn_apply_f32(x.data_ptr(), y.data_ptr(), n, c, inner, mean.data_ptr(),
+                                   dev.data_ptr(), float(eps), int(norm), ptr(scale), ptr(weight),
+                                   ptr(bias), ptr(lut), segs, _stream(x)), "bn_apply")
+    return y
+
+
 # ---- storage codec (src/lo_pack.hpp) ----------------------------------------------
 class SaturationMode(enum.IntEnum):
     """Saturation_Mode (src/fp_tools.hpp:38-41): what an overflow encodes to."""

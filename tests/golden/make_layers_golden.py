@@ -8,8 +8,9 @@ layers never call it, so a stand-in module takes its place (every attribute
 a harmless placeholder). The script records, with torch on the CPU:
   * PWLSiLU tables (R, lut_bits, method) and PWLBatchNorm tables (lut_bits,
     method), as float32;
-  * the four BatchNorm variants on seeded inputs: training-mode outputs and
-    updated running statistics, then eval-mode outputs on a second input.
+  * the four BatchNorm variants on seeded inputs: training-mode outputs, the
+    gradients for a seeded upstream gradient and the updated running
+    statistics, then eval-mode outputs on a second input.
 It writes tests/golden/golden_layers.npz and its entry in MANIFEST.json. The
 tests read only the fixture, never the reference.
 """
@@ -98,10 +99,17 @@ def main():
                     mod.weight.copy_(w)
                     mod.bias.copy_(b)
             mod.train()
-            with torch.no_grad():
-                y = mod(x)
+            xg = x.clone().requires_grad_(True)
+            y = mod(xg)
+            gy = torch.randn(*shape, generator=g)
+            y.backward(gy)
             key = f"bn_{sname}_{vname}"
-            out[key + "_y_train"] = y.numpy()
+            out[key + "_y_train"] = y.detach().numpy()
+            out[key + "_gy"] = gy.numpy()
+            out[key + "_dx"] = xg.grad.numpy()
+            if mod.affine:
+                out[key + "_dw"] = mod.weight.grad.numpy().copy()
+                out[key + "_db"] = mod.bias.grad.numpy().copy()
             for buf in ("running_mean", "running_mad", "running_maxdev", "running_var"):
                 if hasattr(mod, buf):
                     out[key + "_" + buf] = getattr(mod, buf).numpy().copy()

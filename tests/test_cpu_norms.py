@@ -1,54 +1,102 @@
-"""The BatchNorm approximations (LoFloat/layers.py:805-1047) are torch
-compositions in the reference and here; checked on CPU against the formulas
-they implement."""
+"""BatchNorm approximations (LoFloat/layers.py:805-1047), host side.
+
+The modules run on two CUDA kernels (tests/test_gpu_norms.py checks them);
+their backward differentiates the reference's own FP32 formulation, restated
+in lofloat_gb300.norms._chain. Here, on the CPU: that restatement against
+outputs and gradients recorded from the reference's modules
+(tests/golden/golden_layers.npz, tests/golden/make_layers_golden.py), the
+buffers and arguments of the modules, and the CUDA-only forward."""
 import math
 
+import numpy as np
+import pytest
 import torch
 
 import lofloat_gb300 as lg
+from golden_io import load, same_bits
+from lofloat_gb300 import norms
+
+SHAPES = ("nchw", "nc", "ncl")
+VARIANTS = {
+    "l1": ("l1", lambda c: lg.L1BatchNorm(c)),
+    "l1_tensor_scale": ("l1", lambda c: lg.L1BatchNorm(c, scale=torch.linspace(0.5, 1.5, c))),
+    "linf": ("linf", lambda c: lg.LinfBatchNorm(c)),
+    "linf_scale": ("linf", lambda c: lg.LinfBatchNorm(c, scale=0.75, momentum=0.3)),
+    "fisr": ("fisr", lambda c: lg.FISRBatchNorm(c)),
+    "pwl_minimax": ("pwl", lambda c: lg.PWLBatchNorm(c)),
+    "pwl_uniform6": ("pwl", lambda c: lg.PWLBatchNorm(c, lut_bits=6, lut_method="uniform")),
+    "l1_noaffine": ("l1", lambda c: lg.L1BatchNorm(c, affine=False)),
+    "fisr_noaffine_eps": ("fisr", lambda c: lg.FISRBatchNorm(c, affine=False, eps=1e-3)),
+}
 
 
-def _x():
-    g = torch.Generator().manual_seed(0)
-    return torch.randn(16, 6, 5, 5, generator=g) * 3 + 1
+@pytest.fixture(scope="module")
+def golden():
+    return load("golden_layers.npz")
 
 
-def test_l1_and_linf_normalise_by_deviation():
-    x = _x()
-    for cls, stat in ((lg.L1BatchNorm, lambda d: d.abs().mean(dim=(0, 2, 3))),
-                      (lg.LinfBatchNorm, lambda d: d.abs().amax(dim=(0, 2, 3)))):
-        bn = cls(6)
-        y = bn(x)
-        mean = x.mean(dim=(0, 2, 3))
-        d = x - mean.view(1, -1, 1, 1)
-        want = d / (stat(d).view(1, -1, 1, 1) + bn.eps) * bn.scale.view(1, -1, 1, 1)
-        assert torch.allclose(y, want, rtol=1e-6, atol=1e-6)
-        assert torch.allclose(bn.running_mean, 0.1 * mean, rtol=1e-5, atol=1e-6)
-        bn.eval()
-        y2 = bn(x)
-        assert y2.shape == x.shape
-    assert abs(lg.L1BatchNorm(3).scale[0].item() - math.sqrt(2 / math.pi)) < 1e-7
+def _chain_of(mod, kind, x, stats=None, w=None, b=None):
+    return norms._chain(kind, x, w, b, getattr(mod, "scale", None), mod.eps,
+                        getattr(mod, "lut", None), stats)
 
 
-def test_fisr_and_pwl_rsqrt_accuracy():
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("vname", list(VARIANTS))
+def test_restated_chain_matches_reference(golden, shape, vname):
+    """Training outputs and gradients, and eval outputs from the recorded
+    running statistics, bit for bit."""
+    kind, make = VARIANTS[vname]
+    key = f"bn_{shape}_{vname}"
+    x = torch.from_numpy(golden[f"bn_{shape}_x"]).requires_grad_(True)
+    c = x.shape[1]
+    mod = make(c)
+    w = b = None
+    if mod.affine:
+        w = torch.from_numpy(golden[f"bn_{shape}_w"]).requires_grad_(True)
+        b = torch.from_numpy(golden[f"bn_{shape}_b"]).requires_grad_(True)
+    y = _chain_of(mod, kind, x, None, w, b)
+    assert same_bits(y.detach().numpy(), golden[key + "_y_train"])
+    y.backward(torch.from_numpy(golden[key + "_gy"]))
+    assert same_bits(x.grad.numpy(), golden[key + "_dx"])
+    if w is not None:
+        assert same_bits(w.grad.numpy(), golden[key + "_dw"])
+        assert same_bits(b.grad.numpy(), golden[key + "_db"])
+    dev_name = {"l1": "running_mad", "linf": "running_maxdev"}.get(kind, "running_var")
+    stats = (torch.from_numpy(golden[key + "_running_mean"]), torch.from_numpy(golden[key + "_" + dev_name]))
+    x2 = torch.from_numpy(golden[f"bn_{shape}_x2"])
+    y2 = _chain_of(mod, kind, x2, stats, w.detach() if w is not None else None,
+                   b.detach() if b is not None else None)
+    assert same_bits(y2.numpy(), golden[key + "_y_eval"])
+
+
+def test_module_buffers_and_arguments():
+    l1 = lg.L1BatchNorm(3)
+    assert abs(l1.scale[0].item() - math.sqrt(2 / math.pi)) < 1e-7
+    assert [n for n, _ in l1.named_buffers()] == ["running_mean", "running_mad", "num_batches_tracked", "scale"]
+    assert [n for n, _ in lg.LinfBatchNorm(3).named_buffers()] == ["running_mean", "running_maxdev", "scale"]
+    assert [n for n, _ in lg.FISRBatchNorm(3).named_buffers()] == ["running_mean", "running_var",
+                                                                   "num_batches_tracked"]
+    assert [n for n, _ in lg.PWLBatchNorm(3).named_buffers()] == ["running_mean", "running_var",
+                                                                  "num_batches_tracked", "lut"]
+    assert lg.L1BatchNorm(4, affine=False).weight is None
+    assert torch.equal(lg.L1BatchNorm(3, scale=torch.tensor([2.0])).scale, torch.full((3,), 2.0))
+    with pytest.raises(ValueError):
+        lg.L1BatchNorm(3, scale=torch.ones(2))
+
+
+def test_rsqrt_approximations():
     v = torch.logspace(-6, 6, 2001)
-    fisr = lg.FISRBatchNorm._fast_rsqrt(v)
-    assert ((fisr * v.sqrt() - 1).abs().max() < 1e-5)
-    pwl = lg.PWLBatchNorm(4, lut_bits=6)
-    r = pwl._rsqrt_pwl(v)
-    assert ((r * v.sqrt() - 1).abs().max() < 2e-4)
-    # the "midpoint" table shifts interior knots to segment midpoints, a coarser fit
+    assert ((lg.FISRBatchNorm._fast_rsqrt(v) * v.sqrt() - 1).abs().max() < 1e-5)
     for method, tol in (("uniform", 1e-3), ("midpoint", 2e-2), ("minimax", 1e-3)):
         p = lg.PWLBatchNorm(4, lut_bits=4, lut_method=method)
         assert ((p._rsqrt_pwl(v) * v.sqrt() - 1).abs().max() < tol)
 
 
-def test_variance_variants_match_batchnorm():
-    x = _x()
-    ref = torch.nn.BatchNorm2d(6, affine=False)
-    want = ref(x)
-    for cls in (lg.FISRBatchNorm, lg.PWLBatchNorm):
-        bn = cls(6, affine=False)
-        y = bn(x)
-        assert (y - want).abs().max() < 5e-3 * want.abs().max()
-        assert int(bn.num_batches_tracked) == 1
+def test_forward_needs_cuda():
+    with pytest.raises(RuntimeError):
+        lg.L1BatchNorm(3)(torch.zeros(2, 3, 4))
+
+
+def test_golden_fixture_is_consistent(golden):
+    assert golden["bn_nchw_x"].shape == (8, 6, 5, 7)
+    assert np.isfinite(golden["bn_nchw_fisr_y_train"]).all()
