@@ -10,16 +10,17 @@
 // rows of `inner` consecutive values at (nn * c + ch) * inner.
 //
 // Statistics (HBM-bound, 4 B read per element and pass):
-//   stats_partial_kernel   a grid of (row splits) x (channels); every CTA
-//                          reduces its slice of one channel to a pair of
-//                          doubles: sum x, or the shifted sums
-//                          sum (x - K), sum (x - K)^2 (K = the channel's
-//                          first value), or sum |x - mean|, or max |x - mean|
-//                          with the FP32 mean of the previous pass, the
-//                          centring the reference performs in FP32;
-//   stats_finalize_kernel  one warp per channel combines the splits in
-//                          double and writes the FP32 statistic, and the
-//                          running-average update r = r (1 - m) + m s.
+//   stats_pass_kernel      a grid of (row splits) x (channels), sized to one
+//                          co-resident wave; every CTA reduces its slice of
+//                          one channel to a pair of doubles: sum x, or the
+//                          shifted sums sum (x - K), sum (x - K)^2 (K = the
+//                          channel's first value), or sum |x - mean|, or
+//                          max |x - mean| with the FP32 mean of the previous
+//                          pass, the centring the reference performs in FP32;
+//                          the channel's last CTA (a ticket per channel)
+//                          combines the splits in double, writes the FP32
+//                          statistic and the running-average update
+//                          r = r (1 - m) + m s.
 // L1 / L-infinity take two statistics passes (mean, then the deviation
 // about it); the variance variants one.
 //
@@ -47,6 +48,7 @@ namespace {
 constexpr int NT = 256;            // threads per CTA
 constexpr int TARGET_CTAS = 1216;  // statistics grid: about 8 CTAs per SM
 constexpr int MAX_SPLITS = 1024;
+constexpr int UNR = 4;             // 16-byte vectors in flight per thread
 
 enum { P_SUM = 0, P_SHIFTED = 1, P_ABSDEV = 2, P_MAXDEV = 3 };
 
@@ -68,7 +70,9 @@ BnGeo bn_geo(int64_t n, int64_t c, int64_t inner, const void* x) {
     g.inner = inner;
     g.flat = inner < 64;
     g.vec = !g.flat && inner % 4 == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0;
-    int64_t want = cdiv(TARGET_CTAS, c);
+    // as many splits per channel as keep the whole grid one co-resident wave
+    // (no tail of a few CTAs), at least one
+    int64_t want = std::max<int64_t>(1, TARGET_CTAS / std::max<int64_t>(c, 1));
     if (g.flat) {
         const int64_t per_ch = n * inner;
         int64_t s = std::min<int64_t>(want, cdiv(per_ch, 4096));
@@ -119,80 +123,19 @@ struct Acc {
     }
 };
 
+// Combines a channel's split results in double (one warp) and writes the
+// FP32 statistic. P_SUM writes mean; P_SHIFTED mean and the biased variance
+// (to dev); P_ABSDEV / P_MAXDEV dev. running_mean / running_dev (NULL: not
+// updated) take r (1 - m) + m s for what was written.
 template <int P>
-__global__ void __launch_bounds__(NT)
-stats_partial_kernel(const float* __restrict__ x, BnGeo g, const float* __restrict__ center,
-                     double2* __restrict__ part) {
-    pdl_wait();
-    const int s = blockIdx.x;
-    const int64_t ch = blockIdx.y;
-    Acc<P> acc;
-    if constexpr (P == P_SHIFTED) acc.k = x[ch * g.inner];
-    if constexpr (P == P_ABSDEV || P == P_MAXDEV) acc.k = center[ch];
-    if (g.flat) {
-        const int64_t per_ch = g.n * g.inner;
-        const int64_t j0 = (int64_t)s * g.elems_per;
-        const int64_t j1 = min(per_ch, j0 + g.elems_per);
-        for (int64_t j = j0 + threadIdx.x; j < j1; j += NT) {
-            const int64_t nn = j / g.inner, ii = j - nn * g.inner;
-            acc.add(x[(nn * g.c + ch) * g.inner + ii]);
-        }
-    } else {
-        const int64_t r0 = (int64_t)s * g.rows_per;
-        const int64_t r1 = min(g.n, r0 + g.rows_per);
-        for (int64_t nn = r0; nn < r1; ++nn) {
-            const float* row = x + (nn * g.c + ch) * g.inner;
-            if (g.vec) {
-                const float4* v = reinterpret_cast<const float4*>(row);
-                const int64_t nv = g.inner / 4;
-                for (int64_t i = threadIdx.x; i < nv; i += NT) {
-                    const float4 q = __ldg(v + i);
-                    acc.add(q.x);
-                    acc.add(q.y);
-                    acc.add(q.z);
-                    acc.add(q.w);
-                }
-            } else {
-                for (int64_t i = threadIdx.x; i < g.inner; i += NT) acc.add(__ldg(row + i));
-            }
-        }
-    }
-    __shared__ double red[2][NT / 32];
-    double a = acc.a, b = acc.b;
-    a = (P == P_MAXDEV) ? warp_max(a) : warp_sum(a);
-    b = warp_sum(b);
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        red[0][w] = a;
-        red[1][w] = b;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double ta = red[0][0], tb = red[1][0];
-        for (int i = 1; i < NT / 32; ++i) {
-            ta = (P == P_MAXDEV) ? fmax(ta, red[0][i]) : ta + red[0][i];
-            tb += red[1][i];
-        }
-        part[ch * g.splits + s] = make_double2(ta, tb);
-    }
-}
-
-// One warp per channel. P_SUM writes mean; P_SHIFTED writes mean and the
-// biased variance (to dev); P_ABSDEV / P_MAXDEV write dev. running_mean /
-// running_dev (NULL: not updated) take r (1 - m) + m s for what was written.
-template <int P>
-__global__ void __launch_bounds__(NT)
-stats_finalize_kernel(const double2* __restrict__ part, BnGeo g, const float* __restrict__ x,
-                      float* __restrict__ mean, float* __restrict__ dev,
-                      float* __restrict__ running_mean, float* __restrict__ running_dev,
-                      float momentum) {
-    pdl_wait();
-    const int64_t ch = (int64_t)blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
+__device__ __forceinline__ void finalize_channel(const double2* part, const BnGeo& g, int64_t ch,
+                                                 const float* x, float* mean, float* dev,
+                                                 float* running_mean, float* running_dev,
+                                                 float momentum) {
     const int lane = threadIdx.x & 31;
-    if (ch >= g.c) return;
     double a = 0.0, b = 0.0;
     for (int s = lane; s < g.splits; s += 32) {
-        const double2 p = part[ch * g.splits + s];
+        const double2 p = __ldcg(part + ch * g.splits + s);
         a = (P == P_MAXDEV) ? fmax(a, p.x) : a + p.x;
         b += p.y;
     }
@@ -224,6 +167,88 @@ stats_finalize_kernel(const double2* __restrict__ part, BnGeo g, const float* __
     } else {
         dev[ch] = b > 0.0 ? __int_as_float(0x7FC00000) : (float)a;
         track(running_dev, dev[ch]);
+    }
+}
+
+// One statistics pass. Every CTA reduces its slice of one channel to a pair
+// of doubles; the last CTA of the channel to finish (a ticket per channel)
+// combines them (finalize_channel) and resets the ticket for the next pass.
+template <int P>
+__global__ void __launch_bounds__(NT)
+stats_pass_kernel(const float* __restrict__ x, BnGeo g, const float* __restrict__ center,
+                  double2* __restrict__ part, unsigned* __restrict__ tickets, float* mean,
+                  float* dev, float* running_mean, float* running_dev, float momentum) {
+    pdl_wait();
+    const int s = blockIdx.x;
+    const int64_t ch = blockIdx.y;
+    Acc<P> acc;
+    if constexpr (P == P_SHIFTED) acc.k = x[ch * g.inner];
+    if constexpr (P == P_ABSDEV || P == P_MAXDEV) acc.k = center[ch];
+    if (g.flat) {
+        const int64_t per_ch = g.n * g.inner;
+        const int64_t j0 = (int64_t)s * g.elems_per;
+        const int64_t j1 = min(per_ch, j0 + g.elems_per);
+        for (int64_t j = j0 + threadIdx.x; j < j1; j += NT) {
+            const int64_t nn = j / g.inner, ii = j - nn * g.inner;
+            acc.add(x[(nn * g.c + ch) * g.inner + ii]);
+        }
+    } else {
+        const int64_t r0 = (int64_t)s * g.rows_per;
+        const int64_t r1 = min(g.n, r0 + g.rows_per);
+        for (int64_t nn = r0; nn < r1; ++nn) {
+            const float* row = x + (nn * g.c + ch) * g.inner;
+            if (g.vec) {
+                // UNR vectors per thread in flight before they are consumed
+                const float4* v = reinterpret_cast<const float4*>(row);
+                const int64_t nv = g.inner / 4;
+                for (int64_t i0 = threadIdx.x; i0 < nv; i0 += (int64_t)NT * UNR) {
+                    float4 q[UNR];
+#pragma unroll
+                    for (int u = 0; u < UNR; ++u) {
+                        const int64_t i = i0 + (int64_t)u * NT;
+                        q[u] = i < nv ? __ldg(v + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int u = 0; u < UNR; ++u) {
+                        if (i0 + (int64_t)u * NT < nv) {
+                            acc.add(q[u].x);
+                            acc.add(q[u].y);
+                            acc.add(q[u].z);
+                            acc.add(q[u].w);
+                        }
+                    }
+                }
+            } else {
+                for (int64_t i = threadIdx.x; i < g.inner; i += NT) acc.add(__ldg(row + i));
+            }
+        }
+    }
+    __shared__ double red[2][NT / 32];
+    __shared__ int last;
+    double a = acc.a, b = acc.b;
+    a = (P == P_MAXDEV) ? warp_max(a) : warp_sum(a);
+    b = warp_sum(b);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        red[0][w] = a;
+        red[1][w] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ta = red[0][0], tb = red[1][0];
+        for (int i = 1; i < NT / 32; ++i) {
+            ta = (P == P_MAXDEV) ? fmax(ta, red[0][i]) : ta + red[0][i];
+            tb += red[1][i];
+        }
+        part[ch * g.splits + s] = make_double2(ta, tb);
+        __threadfence();
+        last = atomicAdd(tickets + ch, 1u) == (unsigned)g.splits - 1;
+    }
+    __syncthreads();
+    if (last && w == 0) {
+        __threadfence();
+        finalize_channel<P>(part, g, ch, x, mean, dev, running_mean, running_dev, momentum);
+        if (threadIdx.x == 0) tickets[ch] = 0;
     }
 }
 
@@ -314,13 +339,26 @@ bn_apply_rows_kernel(ApplyArgs a) {
         float* yr = a.y + row * a.inner;
         if (a.vec) {
             const int64_t nv = a.inner / 4;
-            for (int64_t i = threadIdx.x; i < nv; i += NT) {
-                float4 q = __ldcs(reinterpret_cast<const float4*>(xr) + i);
-                q.x = normalise(q.x, f, a);
-                q.y = normalise(q.y, f, a);
-                q.z = normalise(q.z, f, a);
-                q.w = normalise(q.w, f, a);
-                __stcs(reinterpret_cast<float4*>(yr) + i, q);
+            const float4* xv = reinterpret_cast<const float4*>(xr);
+            float4* yv = reinterpret_cast<float4*>(yr);
+            for (int64_t i0 = threadIdx.x; i0 < nv; i0 += (int64_t)NT * UNR) {
+                float4 q[UNR];
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    const int64_t i = i0 + (int64_t)u * NT;
+                    if (i < nv) q[u] = __ldcs(xv + i);
+                }
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    const int64_t i = i0 + (int64_t)u * NT;
+                    if (i < nv) {
+                        q[u].x = normalise(q[u].x, f, a);
+                        q[u].y = normalise(q[u].y, f, a);
+                        q[u].z = normalise(q[u].z, f, a);
+                        q[u].w = normalise(q[u].w, f, a);
+                        __stcs(yv + i, q[u]);
+                    }
+                }
             }
         } else {
             for (int64_t i = threadIdx.x; i < a.inner; i += NT) yr[i] = normalise(xr[i], f, a);
@@ -347,17 +385,15 @@ int check_geo(const float* x, int64_t n, int64_t c, int64_t inner) {
 }
 
 template <int P>
-int run_pass(const float* x, const BnGeo& g, const float* center, double2* part, float* mean,
-             float* dev, float* rmean, float* rdev, float momentum, cudaStream_t st) {
-    cudaError_t e = launch_pdl(stats_partial_kernel<P>, dim3(g.splits, (unsigned)g.c), dim3(NT), 0, st,
-                               x, g, center, part);
-    if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "stats_partial_kernel: %s", cudaGetErrorString(e));
-    const unsigned fg = (unsigned)cdiv(g.c, NT / 32);
-    e = launch_pdl(stats_finalize_kernel<P>, dim3(fg), dim3(NT), 0, st, (const double2*)part, g, x,
-                   mean, dev, rmean, rdev, momentum);
-    if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "stats_finalize_kernel: %s", cudaGetErrorString(e));
+int run_pass(const float* x, const BnGeo& g, const float* center, double2* part, unsigned* tickets,
+             float* mean, float* dev, float* rmean, float* rdev, float momentum, cudaStream_t st) {
+    cudaError_t e = launch_pdl(stats_pass_kernel<P>, dim3(g.splits, (unsigned)g.c), dim3(NT), 0, st,
+                               x, g, center, part, tickets, mean, dev, rmean, rdev, momentum);
+    if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "stats_pass_kernel: %s", cudaGetErrorString(e));
     return LOFGB_OK;
 }
+
+size_t part_bytes(const BnGeo& g) { return ((size_t)g.splits * (size_t)g.c * sizeof(double2) + 255) & ~(size_t)255; }
 
 }  // namespace
 
@@ -370,7 +406,7 @@ extern "C" {
 size_t lofgb_bn_workspace_size(int64_t n, int64_t c, int64_t inner) {
     if (n <= 0 || c <= 0 || inner <= 0) return 0;
     const BnGeo g = bn_geo(n, c, inner, nullptr);
-    return (size_t)g.splits * (size_t)c * sizeof(double2);
+    return part_bytes(g) + (size_t)c * sizeof(unsigned);
 }
 
 int lofgb_bn_stats_f32(const float* x, int64_t n, int64_t c, int64_t inner, int stat, float* mean,
@@ -385,21 +421,25 @@ int lofgb_bn_stats_f32(const float* x, int64_t n, int64_t c, int64_t inner, int 
     if (n == 0 || inner == 0) return set_error(LOFGB_ERR_SIZE, "BatchNorm statistics of no values");
     if (!mean || !dev) return set_error(LOFGB_ERR_NULL, "NULL mean or deviation output");
     const BnGeo g = bn_geo(n, c, inner, x);
-    const size_t need = (size_t)g.splits * (size_t)c * sizeof(double2);
+    const size_t need = part_bytes(g) + (size_t)c * sizeof(unsigned);
     if (!workspace || workspace_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 15))
         return set_error(LOFGB_ERR_WORKSPACE, "need %zu bytes of 16-byte aligned workspace", need);
     auto* part = static_cast<double2*>(workspace);
+    auto* tickets = reinterpret_cast<unsigned*>(static_cast<uint8_t*>(workspace) + part_bytes(g));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the tickets start every call at zero (each pass's last CTA resets them)
+    cudaError_t e = cudaMemsetAsync(tickets, 0, (size_t)c * sizeof(unsigned), st);
+    if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
     if (stat == LOFGB_BN_VARIANCE) {
-        if ((rc = run_pass<P_SHIFTED>(x, g, nullptr, part, mean, dev, running_mean, running_dev,
+        if ((rc = run_pass<P_SHIFTED>(x, g, nullptr, part, tickets, mean, dev, running_mean, running_dev,
                                       momentum, st)))
             return rc;
     } else {
-        if ((rc = run_pass<P_SUM>(x, g, nullptr, part, mean, dev, running_mean, nullptr, momentum, st)))
+        if ((rc = run_pass<P_SUM>(x, g, nullptr, part, tickets, mean, dev, running_mean, nullptr, momentum, st)))
             return rc;
         rc = stat == LOFGB_BN_MEAN_ABS_DEV
-                 ? run_pass<P_ABSDEV>(x, g, mean, part, mean, dev, nullptr, running_dev, momentum, st)
-                 : run_pass<P_MAXDEV>(x, g, mean, part, mean, dev, nullptr, running_dev, momentum, st);
+                 ? run_pass<P_ABSDEV>(x, g, mean, part, tickets, mean, dev, nullptr, running_dev, momentum, st)
+                 : run_pass<P_MAXDEV>(x, g, mean, part, tickets, mean, dev, nullptr, running_dev, momentum, st);
         if (rc) return rc;
     }
     return check_launch("BatchNorm statistics");
@@ -432,7 +472,9 @@ int lofgb_bn_apply_f32(const float* x, float* y, int64_t n, int64_t c, int64_t i
     if (inner >= 64) {
         args.vec = inner % 4 == 0 &&
                    ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0;
-        const int64_t g = std::min<int64_t>(n * c, maxg);
+        // equal row counts per CTA: ceil(rows / maxg) rows each
+        const int64_t rows = n * c, per = cdiv(rows, maxg);
+        const int64_t g = cdiv(rows, per);
         e = launch_pdl(bn_apply_rows_kernel, dim3((unsigned)g), dim3(NT), 0, st, args);
     } else {
         const int64_t g = std::max<int64_t>(1, std::min<int64_t>(cdiv(total, NT), maxg));
