@@ -509,24 +509,45 @@ def linear_fwd_bwd(torch, lg, dev):
                                              "note": "dY rounded to E5M2 by SR-A: ~2^-3 noise"}}
 
 
-def grouped_round_case(torch, lg, dev):
+def grouped_round_case(torch, lg, dev, item="auto"):
     """Config-5 part 1: 512 FP32 tensors, each with its own format and mode
-    (seed 5). Returns the grouped launch and the two generators, which part 2
-    continues."""
+    (seed 5). Returns the grouped launch, the per-tensor specs (exp and
+    mantissa bits, saturation, mode, stoch_len, seed) and the two generators,
+    which part 2 continues."""
     rng = np.random.default_rng(5)
     g = torch.Generator(device=dev).manual_seed(5)
-    ins, outs, fmts, modes, lens, seeds = [], [], [], [], [], []
+    ins, outs, fmts, modes, lens, seeds, specs = [], [], [], [], [], [], []
     for i in range(512):
         n = int(2 ** rng.uniform(10, 24))
         x = torch.randn(n, device=dev, generator=g) * float(2 ** rng.uniform(-10, 10))
         ins.append(x)
         outs.append(torch.empty_like(x))
         e, m = int(rng.integers(2, 9)), int(rng.integers(1, 11))
-        fmts.append(lg.make_format(e, m, saturating=bool(rng.integers(0, 2))))
+        sat = bool(rng.integers(0, 2))
+        fmts.append(lg.make_format(e, m, saturating=sat))
         modes.append(int(rng.choice([0, 1, 12, 3])))
         lens.append(8 if modes[-1] == 3 else 0)
         seeds.append(int(rng.integers(0, 2**62)))
-    return lg.GroupedRound(ins, outs, fmts, modes, stoch_lens=lens, seeds=seeds, item="auto"), rng, g
+        specs.append(dict(exp=e, mant=m, saturating=sat, mode=modes[-1], stoch_len=lens[-1],
+                          seed=seeds[-1]))
+    gr = lg.GroupedRound(ins, outs, fmts, modes, stoch_lens=lens, seeds=seeds, item=item)
+    return gr, specs, rng, g
+
+
+def grouped_gemm_case(torch, lg, dev, rng, g):
+    """Config-5 part 2: 64 emulated GEMMs, M, N, K in {256..4096 step 256},
+    MX-E4M3 operands (B given transposed, blocks along K), accumulator bits
+    7-12, chunk 32; continues part 1's generators."""
+    e4m3 = fmt_desc(lg, 8, 3, 7)
+    e8 = lg.create_e8m0_params()
+    tasks = []
+    for i in range(64):
+        M, N, K = (int(v) for v in rng.integers(1, 17, 3) * 256)
+        A = lg.virtual_mx_round(torch.randn(M, K, device=dev, generator=g), 32, e4m3, e8)
+        Bt = lg.virtual_mx_round(torch.randn(N, K, device=dev, generator=g), 32, e4m3, e8)
+        tasks.append(dict(A=A, B=Bt, D=torch.empty(M, N, device=dev), trans_b=1,
+                          accum_mant_bits=int(rng.integers(7, 13)), chunk=32))
+    return tasks
 
 
 def grouped_workloads(torch, lg, dev):
@@ -537,7 +558,7 @@ def grouped_workloads(torch, lg, dev):
     M,N,K in {256..4096 step 256}, MX-E4M3 operands, accumulator bits 7-12,
     one grouped tensor-core launch with the autotuned schedule, from a graph."""
     out = {}
-    gr, rng, g = grouped_round_case(torch, lg, dev)
+    gr, _, rng, g = grouped_round_case(torch, lg, dev)
     gr.capture()
     for _ in range(3):
         gr.replay()
@@ -555,15 +576,7 @@ def grouped_workloads(torch, lg, dev):
     out["grouped_round_512_tuning_ms"] = {str(k): v for k, v in gr.tuning_ms.items()}
     del gr
     torch.cuda.empty_cache()
-    e4m3 = fmt_desc(lg, 8, 3, 7)
-    e8 = lg.create_e8m0_params()
-    tasks = []
-    for i in range(64):
-        M, N, K = (int(v) for v in rng.integers(1, 17, 3) * 256)
-        A = lg.virtual_mx_round(torch.randn(M, K, device=dev, generator=g), 32, e4m3, e8)
-        Bt = lg.virtual_mx_round(torch.randn(N, K, device=dev, generator=g), 32, e4m3, e8)
-        tasks.append(dict(A=A, B=Bt, D=torch.empty(M, N, device=dev), trans_b=1,
-                          accum_mant_bits=int(rng.integers(7, 13)), chunk=32))
+    tasks = grouped_gemm_case(torch, lg, dev, rng, g)
     gg = lg.GroupedGemm(tasks, schedule="auto")
     gg.capture()
     for _ in range(2):
