@@ -242,6 +242,22 @@ int lofgb_gemm_tc_noalloc_f32(const float* A, int64_t lda, int trans_a, const fl
                               int K, int accum_mant_bits, float alpha, int chunk,
                               void* stream);
 
+/* Self-test of the tensor-core kernel's bounded waits. No counterpart in the
+ * reference, whose CUTLASS runner exits the process on an error
+ * (src/cutlass_gemms.cuh:45-50). Runs the tensor-core GEMM (A M x K, B K x N,
+ * D M x N, all row-major, 10-bit accumulator, chunk 32; workspace as
+ * lofgb_gemm_f32) with every wait limited to wait_limit_us microseconds
+ * (100..100000) while the copy producer of every CTA withholds its first
+ * pipeline stage: no copy is issued for it and nothing faults, but the MMA
+ * warp's wait for it runs out. Every CTA then takes the abort path a real
+ * stall would take: it records LOFGB_ERR_TIMEOUT in the workspace status word
+ * (its first 4 bytes), drains its own copies and MMAs, frees its tensor memory
+ * and exits; D is left incomplete. Returns the launch status; the caller reads
+ * the status word after synchronising. */
+int lofgb_gemm_tc_wait_selftest(const float* A, const float* B, float* D, int M, int N, int K,
+                                void* workspace, size_t workspace_bytes, uint32_t wait_limit_us,
+                                void* stream);
+
 /* FP64 GPU oracle GEMM used only to state the error of the tensor-core form:
  * D[i,j] = sum_k (double)A[i,k]*(double)B[k,j] in FP64, same layouts as above.
  * No counterpart in the reference (its harness compares against cuBLAS SGEMM,

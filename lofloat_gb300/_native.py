@@ -104,6 +104,8 @@ SIGNATURES = [
                                   _vp]),
     ("lofgb_bn_apply_f32", _i32, [_vp, _vp, _i64, _i64, _i64, _vp, _vp, _f32, _i32, _vp, _vp, _vp,
                                   _vp, _i32, _vp]),
+    ("lofgb_gemm_tc_wait_selftest", _i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _sz, C.c_uint32,
+                                           _vp]),
     ("lofgb_packed_size", _sz, [_i32, _i64]),
     ("lofgb_encode_f32", _i32, [_vp, _vp, _i64, C.POINTER(LofgbCodecFormat), _i32, _i32, _i32, _i32,
                                 _u64, _u64, _vp]),

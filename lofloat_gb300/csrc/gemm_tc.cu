@@ -69,6 +69,14 @@ static_assert((NBUF & (NBUF - 1)) == 0 && TMEM_COLS <= 512, "TMEM chunk buffers"
 constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + STAGES * STAGE_BYTES + 256 /*barriers*/;
 constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;
 
+// Limit of every bounded wait, and for the wait self-test the pipeline stage
+// whose copies the producer withholds (-1: none), so that the MMA warp's
+// wait for it runs out and the CTA takes its abort path.
+struct WaitCfg {
+    unsigned long long limit_ns = WAIT_LIMIT_NS;
+    int withhold = -1;
+};
+
 struct TcParams {
     float* D;
     int64_t ldd;
@@ -88,6 +96,7 @@ struct TcParams {
     RoundPlan acc_plan;
     uint32_t* range;       // exponent ranges of A and B (workspace words)
     int fast_lim;          // fast fold iff emax_a + emax_b <= fast_lim (FAST_OFF: never)
+    WaitCfg wait;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -128,13 +137,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 // Bounded wait: false if the CTA is aborting or the wait ran out of time
 // (then the abort flag is raised and the status word set).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
-                                          int* status) {
+                                          int* status, unsigned long long limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = globaltimer();
     while (true) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*abort_flag) return false;
-        if (globaltimer() - t0 > WAIT_LIMIT_NS) {
+        if (globaltimer() - t0 > limit_ns) {
             *abort_flag = 1;
             atomicExch(status, (int)LOFGB_ERR_TIMEOUT);
             return false;
@@ -143,10 +152,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
 }
 
 // Wait used while draining after an abort: bounded, result ignored.
-__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
     const unsigned long long t0 = globaltimer();
     while (!mbar_try_wait(bar, parity))
-        if (globaltimer() - t0 > WAIT_LIMIT_NS) return;
+        if (globaltimer() - t0 > limit_ns) return;
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1,
@@ -421,7 +430,7 @@ struct GroupedSrc {
 // reader count) for the next launch of the same device table.
 template <int ACCK, class Src>
 __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* smem_raw,
-                                       uint32_t* range, bool reset_range,
+                                       uint32_t* range, bool reset_range, const WaitCfg wcfg,
                                        const RoundPlan* acc_plan = nullptr) {
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                ~uintptr_t(1023));
@@ -485,7 +494,8 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                 for (int ks = 0; ks < ksteps; ++ks, ++it) {
                     const uint32_t s = it % STAGES;
                     const uint32_t ph = (it / STAGES) & 1u;
-                    if (!mbar_wait(bar_empty + 8 * s, ph ^ 1u, abort_flag, status)) { ok = false; break; }
+                    if (!mbar_wait(bar_empty + 8 * s, ph ^ 1u, abort_flag, status, wcfg.limit_ns)) { ok = false; break; }
+                    if ((int)it == wcfg.withhold) continue;  // wait self-test: this stage never fills
                     const uint32_t base = smem_u32(tiles + s * STAGE_BYTES);
                     mbar_arrive_expect_tx(bar_full + 8 * s, STAGE_BYTES);
                     tma_load_2d(base + 0 * TILE_BYTES, ti.map[0], ks * SK, ti.a_r0, bar_full + 8 * s);
@@ -497,7 +507,7 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
             if (!ok) {
                 // drain: every issued stage completes (or the drain wait expires)
                 for (uint32_t j = (it >= STAGES ? it - STAGES : 0); j < it; ++j)
-                    mbar_drain(bar_full + 8 * (j % STAGES), (j / STAGES) & 1u);
+                    mbar_drain(bar_full + 8 * (j % STAGES), (j / STAGES) & 1u, wcfg.limit_ns);
             }
         }
     } else if (warp == 1) {
@@ -519,14 +529,14 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                 const int chunk16 = ti.chunk16;
                 int pos = 0;                 // k16 step within the chunk
                 for (int ks = 0; ks < ksteps && ok; ++ks) {
-                    if (!mbar_wait(bar_full + 8 * s, sph, abort_flag, status)) { ok = false; break; }
+                    if (!mbar_wait(bar_full + 8 * s, sph, abort_flag, status, wcfg.limit_ns)) { ok = false; break; }
                     tc_fence_after();
                     const uint64_t sd = dbase + s * SSTEP;
                     const bool last_stage = ks == ksteps - 1;
 #pragma unroll
                     for (int j = 0; j < SK / 16; ++j) {
                         if (pos == 0) {
-                            if (!mbar_wait(bar_tempty + 8 * buf, bph ^ 1u, abort_flag, status)) { ok = false; break; }
+                            if (!mbar_wait(bar_tempty + 8 * buf, bph ^ 1u, abort_flag, status, wcfg.limit_ns)) { ok = false; break; }
                             tc_fence_after();
                         }
                         const uint32_t d = tmem_base + buf * TBN;
@@ -548,7 +558,7 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
             }
             // all issued MMAs complete before the TMEM is released
             umma_commit(bar_drain);
-            mbar_drain(bar_drain, 0);
+            mbar_drain(bar_drain, 0, wcfg.limit_ns);
         }
     } else {
         // ---------------- epilogue ----------------
@@ -564,7 +574,8 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
         // every lane waits; the warp goes on only when all lanes saw the phase
         // complete, reconverged for the .sync.aligned TMEM loads
         auto wait_full = [&](uint32_t g) -> bool {
-            const bool got = mbar_wait(bar_tfull + 8 * (g % NBUF), (g / NBUF) & 1u, abort_flag, status);
+            const bool got = mbar_wait(bar_tfull + 8 * (g % NBUF), (g / NBUF) & 1u, abort_flag, status,
+                                       wcfg.limit_ns);
             if (!__all_sync(0xFFFFFFFFu, got)) return false;
             __syncwarp();
             tc_fence_after();
@@ -696,14 +707,14 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
     src.m[2] = &tm_bhi;
     src.m[3] = &tm_blo;
     src.prm = prm;
-    tc_body<ACCK>(src, prm.status, smem_raw, prm.range, false, &prm.acc_plan);
+    tc_body<ACCK>(src, prm.status, smem_raw, prm.range, false, prm.wait, &prm.acc_plan);
 }
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 gemm_tc_grouped_kernel(const GroupHeader* __restrict__ h) {
     extern __shared__ uint8_t smem_raw[];
     GroupedSrc src{h};
-    tc_body<0>(src, h->status, smem_raw, const_cast<uint32_t*>(h->range), true);
+    tc_body<0>(src, h->status, smem_raw, const_cast<uint32_t*>(h->range), true, WaitCfg{});
 }
 
 // ---- operand split: FP32 -> K-major BF16 hi/lo, zero padded -----------------
@@ -847,10 +858,16 @@ int make_map(CUtensorMap* map, void* base, int rows, int Kp) {
 
 size_t gemm_tc_workspace(int M, int N, int K, int batch) { return ws_layout(M, N, K, batch).total; }
 
-int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float* B, int64_t ldb,
-                   int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M, int N, int K,
-                   int batch, int mbits, const RoundPlan* acc_fmt, float alpha, int chunk,
-                   void* workspace, size_t workspace_bytes, void* stream) {
+namespace {
+int launch_tc_presplit_cfg(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int64_t sd, int M,
+                           int N, int mbits, float alpha, int chunk, int64_t img_L,
+                           int64_t img_stride, void* stream, const RoundPlan* acc_fmt,
+                           const WaitCfg& wait);
+
+int launch_gemm_tc_cfg(const float* A, int64_t lda, int64_t sa, int ta, const float* B, int64_t ldb,
+                       int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M, int N, int K,
+                       int batch, int mbits, const RoundPlan* acc_fmt, float alpha, int chunk,
+                       void* workspace, size_t workspace_bytes, void* stream, const WaitCfg& wait) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (K == 0) {
         // no products: D = alpha * (+0), one pitched clear per batch entry
@@ -885,12 +902,31 @@ int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float*
                                                                         w.Np, w.Kp, batch, bhi, blo,
                                                                         range + 2);
     if ((rc = check_launch("split_bf16_kernel(B)"))) return rc;
-    return launch_tc_presplit(ws, w, D, ldd, sd, M, N, mbits, alpha, chunk, 0, 0, stream, acc_fmt);
+    return launch_tc_presplit_cfg(ws, w, D, ldd, sd, M, N, mbits, alpha, chunk, 0, 0, stream, acc_fmt,
+                                  wait);
+}
+}  // namespace
+
+int launch_gemm_tc(const float* A, int64_t lda, int64_t sa, int ta, const float* B, int64_t ldb,
+                   int64_t sb, int tb, float* D, int64_t ldd, int64_t sd, int M, int N, int K,
+                   int batch, int mbits, const RoundPlan* acc_fmt, float alpha, int chunk,
+                   void* workspace, size_t workspace_bytes, void* stream) {
+    return launch_gemm_tc_cfg(A, lda, sa, ta, B, ldb, sb, tb, D, ldd, sd, M, N, K, batch, mbits,
+                              acc_fmt, alpha, chunk, workspace, workspace_bytes, stream, WaitCfg{});
 }
 
 int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int64_t sd, int M,
                        int N, int mbits, float alpha, int chunk, int64_t img_L,
                        int64_t img_stride, void* stream, const RoundPlan* acc_fmt) {
+    return launch_tc_presplit_cfg(ws, w, D, ldd, sd, M, N, mbits, alpha, chunk, img_L, img_stride,
+                                  stream, acc_fmt, WaitCfg{});
+}
+
+namespace {
+int launch_tc_presplit_cfg(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, int64_t sd, int M,
+                           int N, int mbits, float alpha, int chunk, int64_t img_L,
+                           int64_t img_stride, void* stream, const RoundPlan* acc_fmt,
+                           const WaitCfg& wait) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     auto* ahi = reinterpret_cast<__nv_bfloat16*>(ws + w.ahi);
     auto* alo = reinterpret_cast<__nv_bfloat16*>(ws + w.alo);
@@ -929,6 +965,7 @@ int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, in
     }
     p.range = reinterpret_cast<uint32_t*>(ws + w.range);
     p.fast_lim = acc_fmt ? FAST_OFF : fast_fold_limit(w.Kp, chunk, mbits);
+    p.wait = wait;
 
     int dev = 0;
     cudaGetDevice(&dev);
@@ -952,6 +989,7 @@ int launch_tc_presplit(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd, in
         gemm_tc_kernel<3><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
     return check_launch("gemm_tc_kernel");
 }
+}  // namespace
 
 }  // namespace lofgb
 
@@ -1027,6 +1065,23 @@ extern "C" int lofgb_gemm_tc_noalloc_f32(const float* A, int64_t lda, int trans_
     return lofgb_gemm_f32(A, lda, trans_a, B, ldb, trans_b, D, ldd, M, N, K, accum_mant_bits,
                           LOFGB_RNE, alpha, LOFGB_GEMM_TC, chunk, scratch,
                           scratch ? NOALLOC_SCRATCH_BYTES : 0, stream);
+}
+
+// ---- bounded-wait self-test ----------------------------------------------------
+extern "C" int lofgb_gemm_tc_wait_selftest(const float* A, const float* B, float* D, int M, int N,
+                                           int K, void* workspace, size_t workspace_bytes,
+                                           uint32_t wait_limit_us, void* stream) {
+    using namespace lofgb;
+    clear_error();
+    if (M <= 0 || N <= 0 || K <= 0) return set_error(LOFGB_ERR_SIZE, "self-test needs M, N, K > 0");
+    if (!A || !B || !D) return set_error(LOFGB_ERR_NULL, "NULL operand");
+    if (wait_limit_us < 100 || wait_limit_us > 100000)
+        return set_error(LOFGB_ERR_SIZE, "wait limit %u us outside [100, 100000]", wait_limit_us);
+    WaitCfg wait;
+    wait.limit_ns = (unsigned long long)wait_limit_us * 1000ull;
+    wait.withhold = 0;  // the first stage of every CTA never fills
+    return launch_gemm_tc_cfg(A, K, 0, 0, B, N, 0, 0, D, N, 0, M, N, K, 1, 10, nullptr, 1.0f, 32,
+                              workspace, workspace_bytes, stream, wait);
 }
 
 // ---- grouped launch: host side -----------------------------------------------

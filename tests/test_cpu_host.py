@@ -312,3 +312,13 @@ def test_codec_format_fits_reference_checkers():
     import pytest
     with pytest.raises(RuntimeError):
         lg.codec_format(w)
+
+
+def test_wait_selftest_argument_checks():
+    """The wait self-test entry point validates on the host before any launch."""
+    L = _native.lib()
+    A, B, D = C.c_void_p(0x1000), C.c_void_p(0x2000), C.c_void_p(0x3000)
+    assert L.lofgb_gemm_tc_wait_selftest(A, B, D, 0, 4, 4, None, 0, 1000, None) == -2
+    assert L.lofgb_gemm_tc_wait_selftest(None, B, D, 4, 4, 4, None, 0, 1000, None) == -1
+    assert L.lofgb_gemm_tc_wait_selftest(A, B, D, 4, 4, 4, None, 0, 50, None) == -2
+    assert L.lofgb_gemm_tc_wait_selftest(A, B, D, 4, 4, 4, None, 0, 200000, None) == -2

@@ -166,3 +166,31 @@ def test_workspace_errors():
     st = L.lofgb_gemm_f32(A.data_ptr(), 64, 0, A.data_ptr(), 64, 0, D.data_ptr(), 64, 64, 64, 64, 10,
                           0, 1.0, 1, 32, None, 0, None)
     assert st == -9
+
+
+def test_bounded_wait_runs_out_and_the_next_launch_is_clean():
+    """The wait self-test: every CTA's first pipeline stage is withheld (no
+    copy issued, no fault), so the MMA warp's 1 ms wait runs out; the kernel
+    must record LOFGB_ERR_TIMEOUT, drain, free its tensor memory and return.
+    The next ordinary launch on the same stream then gives the same bits as
+    before and a clean status."""
+    rng = np.random.default_rng(9)
+    M, N, K = 256, 384, 512
+    A = to_gpu(rng.standard_normal((M, K)).astype(np.float32))
+    B = to_gpu(rng.standard_normal((K, N)).astype(np.float32))
+    before = lg.gemm(A, B, 10, variant="tc", chunk=32)
+    _status_ok()
+    L = lg._native.lib()
+    ws = torch.zeros(L.lofgb_gemm_tc_workspace_size(M, N, K), dtype=torch.uint8, device="cuda")
+    D = torch.empty(M, N, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    st = L.lofgb_gemm_tc_wait_selftest(A.data_ptr(), B.data_ptr(), D.data_ptr(), M, N, K,
+                                       ws.data_ptr(), ws.numel(), 1000, stream)
+    assert st == 0, L.lofgb_last_error_detail().decode()
+    torch.cuda.synchronize()
+    assert int(ws[:4].view(torch.int32).item()) == -10   # LOFGB_ERR_TIMEOUT
+    after = lg.gemm(A, B, 10, variant="tc", chunk=32)
+    _status_ok()
+    assert torch.equal(after, before)
+    assert L.lofgb_gemm_tc_wait_selftest(A.data_ptr(), B.data_ptr(), D.data_ptr(), M, N, K,
+                                         ws.data_ptr(), ws.numel(), 10, stream) == -2
