@@ -275,16 +275,20 @@ int lofgb_gemm_f64_ref(const float* A, int64_t lda, int trans_a, const float* B,
  *      (lofgb_gemm_grouped_workspace_size bytes, 256-byte aligned; only its
  *      address is used here) and writes a table of
  *      lofgb_gemm_grouped_table_size bytes into the caller's HOST buffer:
- *      per-task rows with their TMA descriptors, and the list of 128 x 128
- *      output tiles in the order given by `schedule`:
+ *      per-task rows with their TMA descriptors, and the list of output
+ *      tiles in the order given by `schedule`:
  *        0 = task by task, 1 = longest K first, dealt round-robin to the
  *        `grid` CTAs, 2 = longest K first, dealt boustrophedon;
+ *      tiles are 128 x 128, or 128 x 64 with LOFGB_GROUPED_TILE_N64 or-ed
+ *      into `schedule` (twice the tiles: finer load balance over uneven
+ *      GEMMs, more operand traffic per product);
  *   2. the caller copies the table to device memory (256-byte aligned) and
  *      calls lofgb_gemm_grouped_launch(): one operand-split launch and one
  *      persistent tensor-core launch of `grid` CTAs (0 = one per SM).
  * Each task computes what lofgb_gemm_f32(..., LOFGB_RNE, ..., LOFGB_GEMM_TC,
  * chunk, ...) computes for it. The first 4 bytes of the workspace receive the
  * device status (0, or LOFGB_ERR_TIMEOUT). */
+enum { LOFGB_GROUPED_TILE_N64 = 16 };
 typedef struct lofgb_gemm_task {
     const float* A;
     int64_t lda;

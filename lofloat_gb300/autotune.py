@@ -5,13 +5,17 @@ each with its own accumulator width, chunk and alpha, as one operand-split
 launch plus one persistent tcgen05 launch (lofgb_gemm_grouped_launch), and
 can capture both in a CUDA graph.
 
-The tile schedule — the order in which the persistent CTAs take the 128 x 128
-output tiles of all GEMMs — decides load balance when the GEMMs differ in
-size. ``GroupedGemm(..., schedule="auto")`` times every schedule the library
-offers (task order; longest-K first dealt round-robin; longest-K first dealt
-boustrophedon) on the actual problem, keeps the fastest, and caches the
-choice in a JSON table keyed by the problem's shape signature (bucketed to
-powers of two), so later problems of the same shape reuse it without timing.
+The tile shape (128 x 128, or 128 x 64: twice the tiles, finer load balance
+over uneven GEMMs, more operand traffic per product) and the tile schedule —
+the order in which the persistent CTAs take the output tiles of all GEMMs —
+decide load balance when the GEMMs differ in size. ``GroupedGemm(...,
+schedule="auto")`` times every (shape, schedule) pair the library offers
+(shapes 128x128 and 128x64; task order, longest-K first dealt round-robin,
+longest-K first dealt boustrophedon) on the actual problem, keeps the
+fastest, and caches the choice in a JSON table keyed by the problem's shape
+signature (bucketed to powers of two), so later problems of the same shape
+reuse it without timing. A choice is named "<shape>/<schedule>", e.g.
+"128x64/lpt_snake"; a bare schedule name means the 128 x 128 tile.
 """
 from __future__ import annotations
 
@@ -28,6 +32,14 @@ from ._native import LofgbGemmTask, check
 from .binding import _stream
 
 SCHEDULES = {"task": 0, "lpt": 1, "lpt_snake": 2}
+TILES = {"128x128": 0, "128x64": 16}   # LOFGB_GROUPED_TILE_N64 for the narrow tile
+CHOICES = [f"{t}/{s}" for t in TILES for s in SCHEDULES]
+
+
+def _code(choice: str) -> int:
+    """Library schedule code of "<shape>/<schedule>" (or a bare schedule)."""
+    tile, _, sched = choice.rpartition("/")
+    return TILES[tile or "128x128"] | SCHEDULES[sched]
 CACHE_PATH = os.environ.get(
     "LOFGB_AUTOTUNE_CACHE",
     os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json"))
@@ -106,6 +118,8 @@ class GroupedGemm:
         self.graph = None
         if schedule == "auto":
             cached = _load_cache().get(self.signature)
+            if cached is not None and cached.get("schedule") not in CHOICES:
+                cached = None   # an entry from before tile shapes were tuned
             if cached is not None:
                 self.schedule = cached["schedule"]
                 self.tuning = cached
@@ -122,7 +136,7 @@ class GroupedGemm:
         nt, si = C.c_int64(0), C.c_int64(0)
         with torch.cuda.device(self.device):
             check(L.lofgb_gemm_grouped_prepare(self._arr, len(self.tasks), self.ws.data_ptr(),
-                                               self.ws.numel(), SCHEDULES[schedule], self.grid,
+                                               self.ws.numel(), _code(schedule), self.grid,
                                                host.ctypes.data_as(C.c_void_p), self.table_bytes,
                                                C.byref(nt), C.byref(si)), "gemm_grouped_prepare")
         self.table = torch.from_numpy(host).to(self.device)
@@ -131,7 +145,7 @@ class GroupedGemm:
 
     def _tune(self, reps: int):
         times = {}
-        for name in SCHEDULES:
+        for name in CHOICES:
             self._prepare(name)
             self()  # warm up
             torch.cuda.synchronize(self.device)

@@ -54,19 +54,35 @@ namespace lofgb {
 namespace {
 
 constexpr int TBM = 128;          // output tile rows (UMMA M)
-constexpr int TBN = 128;          // output tile cols (UMMA N)
+constexpr int TBN = 128;          // widest output tile (UMMA N); operands are padded to it
 constexpr int SK = 64;            // k per pipeline stage (one 128-byte swizzle row of bf16)
-constexpr int STAGES = 3;
-constexpr int TILE_BYTES = TBM * SK * 2;       // 16 KiB per operand tile
-constexpr int STAGE_BYTES = 4 * TILE_BYTES;    // A hi, A lo, B hi, B lo
-constexpr int EPI_WARPS = 16;                  // EPI_WARPS / 4 per TMEM lane quarter
-constexpr int EPI_COLS = TBN * 4 / EPI_WARPS;  // accumulator columns per epilogue thread
-constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
-static_assert(EPI_COLS == 64 || EPI_COLS == 32, "the epilogue folds 16-column pieces, 4 or 2 per chunk");
-constexpr int NBUF = 4;                        // TMEM chunk buffers (all 512 columns)
-constexpr int TMEM_COLS = NBUF * TBN;
-static_assert((NBUF & (NBUF - 1)) == 0 && TMEM_COLS <= 512, "TMEM chunk buffers");
-constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + STAGES * STAGE_BYTES + 256 /*barriers*/;
+constexpr int TILE_A = TBM * SK * 2;           // 16 KiB per A operand tile
+constexpr int PIPE_BYTES = 192 * 1024;         // shared memory of the stage ring
+
+// Tile shapes of the persistent kernel: 128 x BN outputs per tile.
+//   BN = 128: stages of 64 KiB (A hi, A lo, B hi, B lo), 3 stages; four
+//             128-column TMEM chunk buffers; 16 epilogue warps of 32 columns;
+//   BN = 64:  stages of 48 KiB, 4 stages; eight 64-column chunk buffers; 8
+//             epilogue warps of 32 columns (the grouped kernel's narrow tile,
+//             more tiles for load balance across uneven GEMMs).
+template <int BN>
+struct TileShape {
+    static constexpr int TILE_B = BN * SK * 2;
+    static constexpr int STAGE_BYTES = 2 * TILE_A + 2 * TILE_B;
+    static constexpr int STAGES = PIPE_BYTES / STAGE_BYTES;
+    static constexpr int EPI_WARPS = BN == 128 ? 16 : 8;   // EPI_WARPS / 4 per TMEM lane quarter
+    static constexpr int EPI_COLS = BN * 4 / EPI_WARPS;    // accumulator columns per epilogue thread
+    static constexpr int NBUF = 512 / BN;                  // TMEM chunk buffers (all 512 columns)
+    // Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+    // (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
+    static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) |
+                                      ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
+    static_assert(EPI_COLS == 64 || EPI_COLS == 32, "the epilogue folds 16-column pieces, 4 or 2 per chunk");
+    static_assert((NBUF & (NBUF - 1)) == 0 && NBUF * BN == 512, "TMEM chunk buffers");
+    static_assert(STAGES * STAGE_BYTES <= PIPE_BYTES && STAGES >= 3, "stage ring");
+};
+constexpr int NUM_THREADS = 32 * (2 + 16);     // launch size of every shape (idle warps exit)
+constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + PIPE_BYTES + 256 /*barriers*/;
 constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;
 
 // Limit of every bounded wait, and for the wait self-test the pipeline stage
@@ -180,11 +196,7 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
     return d;
 }
 
-// Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
-// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TBN >> 3) << 17) |
-                           ((uint32_t)(TBM >> 4) << 24);
-
+template <uint32_t IDESC>
 __device__ __forceinline__ void umma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -380,7 +392,7 @@ struct SplitRow {
     int32_t kmajor, rows, K, R, Kp, operand;  // operand: 0 = A, 1 = B
 };
 struct GroupHeader {   // at the start of the device table; offsets from its base
-    int32_t ntasks, ntiles, nsplit, pad;
+    int32_t ntasks, ntiles, nsplit, tile_n;   // tile_n: 128 or 64 output columns per tile
     int64_t split_items;
     int64_t rows_off, tiles_off, splits_off;
     int* status;
@@ -428,10 +440,15 @@ struct GroupedSrc {
 // largest field, 255 - its smallest non-zero field, the same for B);
 // reset_range: the last CTA to read them clears them (and range[4], the
 // reader count) for the next launch of the same device table.
-template <int ACCK, class Src>
+template <int ACCK, int BN, class Src>
 __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* smem_raw,
                                        uint32_t* range, bool reset_range, const WaitCfg wcfg,
                                        const RoundPlan* acc_plan = nullptr) {
+    using Shape = TileShape<BN>;
+    constexpr int TBN = BN, STAGES = Shape::STAGES, STAGE_BYTES = Shape::STAGE_BYTES;
+    constexpr int TILE_B = Shape::TILE_B, EPI_WARPS = Shape::EPI_WARPS, EPI_COLS = Shape::EPI_COLS;
+    constexpr int NBUF = Shape::NBUF, TMEM_COLS = NBUF * TBN;
+    constexpr uint32_t IDESC = Shape::IDESC;
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                ~uintptr_t(1023));
     uint8_t* tiles = smem;
@@ -498,10 +515,11 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                     if ((int)it == wcfg.withhold) continue;  // wait self-test: this stage never fills
                     const uint32_t base = smem_u32(tiles + s * STAGE_BYTES);
                     mbar_arrive_expect_tx(bar_full + 8 * s, STAGE_BYTES);
-                    tma_load_2d(base + 0 * TILE_BYTES, ti.map[0], ks * SK, ti.a_r0, bar_full + 8 * s);
-                    tma_load_2d(base + 1 * TILE_BYTES, ti.map[1], ks * SK, ti.a_r0, bar_full + 8 * s);
-                    tma_load_2d(base + 2 * TILE_BYTES, ti.map[2], ks * SK, ti.b_r0, bar_full + 8 * s);
-                    tma_load_2d(base + 3 * TILE_BYTES, ti.map[3], ks * SK, ti.b_r0, bar_full + 8 * s);
+                    tma_load_2d(base, ti.map[0], ks * SK, ti.a_r0, bar_full + 8 * s);
+                    tma_load_2d(base + TILE_A, ti.map[1], ks * SK, ti.a_r0, bar_full + 8 * s);
+                    tma_load_2d(base + 2 * TILE_A, ti.map[2], ks * SK, ti.b_r0, bar_full + 8 * s);
+                    tma_load_2d(base + 2 * TILE_A + TILE_B, ti.map[3], ks * SK, ti.b_r0,
+                                bar_full + 8 * s);
                 }
             }
             if (!ok) {
@@ -519,7 +537,8 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
         // memory is below 256 KiB).
         if (lane == 0) {
             const uint64_t dbase = smem_desc_sw128(smem_u32(tiles));
-            constexpr uint64_t TSTEP = TILE_BYTES >> 4, SSTEP = STAGE_BYTES >> 4;
+            constexpr uint64_t ALO = TILE_A >> 4, BHI = (2 * TILE_A) >> 4;
+            constexpr uint64_t BLO = (2 * TILE_A + TILE_B) >> 4, SSTEP = STAGE_BYTES >> 4;
             uint32_t s = 0, sph = 0;         // stage and its phase
             uint32_t buf = 0, bph = 0;       // TMEM chunk buffer and its phase
             bool ok = true;
@@ -540,11 +559,11 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                             tc_fence_after();
                         }
                         const uint32_t d = tmem_base + buf * TBN;
-                        const uint64_t ahi = sd + 2 * j, alo = sd + TSTEP + 2 * j;
-                        const uint64_t bhi = sd + 2 * TSTEP + 2 * j, blo = sd + 3 * TSTEP + 2 * j;
-                        umma_f16(d, ahi, bhi, pos > 0 ? 1u : 0u);
-                        umma_f16(d, ahi, blo, 1u);
-                        umma_f16(d, alo, bhi, 1u);
+                        const uint64_t ahi = sd + 2 * j, alo = sd + ALO + 2 * j;
+                        const uint64_t bhi = sd + BHI + 2 * j, blo = sd + BLO + 2 * j;
+                        umma_f16<IDESC>(d, ahi, bhi, pos > 0 ? 1u : 0u);
+                        umma_f16<IDESC>(d, ahi, blo, 1u);
+                        umma_f16<IDESC>(d, alo, bhi, 1u);
                         if (++pos == chunk16 || (last_stage && j == SK / 16 - 1)) {
                             umma_commit(bar_tfull + 8 * buf);
                             pos = 0;
@@ -560,7 +579,7 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
             umma_commit(bar_drain);
             mbar_drain(bar_drain, 0, wcfg.limit_ns);
         }
-    } else {
+    } else if (warp < 2 + EPI_WARPS) {
         // ---------------- epilogue ----------------
         const int ew = warp - 2;              // 0 .. EPI_WARPS-1
         const int quarter = warp & 3;         // TMEM lane quarter this warp may access
@@ -707,14 +726,18 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
     src.m[2] = &tm_bhi;
     src.m[3] = &tm_blo;
     src.prm = prm;
-    tc_body<ACCK>(src, prm.status, smem_raw, prm.range, false, prm.wait, &prm.acc_plan);
+    tc_body<ACCK, 128>(src, prm.status, smem_raw, prm.range, false, prm.wait, &prm.acc_plan);
 }
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 gemm_tc_grouped_kernel(const GroupHeader* __restrict__ h) {
     extern __shared__ uint8_t smem_raw[];
     GroupedSrc src{h};
-    tc_body<0>(src, h->status, smem_raw, const_cast<uint32_t*>(h->range), true, WaitCfg{});
+    // the tile width the table was prepared for (uniform over the launch)
+    if (h->tile_n == 64)
+        tc_body<0, 64>(src, h->status, smem_raw, const_cast<uint32_t*>(h->range), true, WaitCfg{});
+    else
+        tc_body<0, 128>(src, h->status, smem_raw, const_cast<uint32_t*>(h->range), true, WaitCfg{});
 }
 
 // ---- operand split: FP32 -> K-major BF16 hi/lo, zero padded -----------------
@@ -840,12 +863,12 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-int make_map(CUtensorMap* map, void* base, int rows, int Kp) {
+int make_map(CUtensorMap* map, void* base, int rows, int Kp, int box_rows = TBM) {
     auto fn = encode_fn();
     if (!fn) return set_error(LOFGB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
-    cuuint32_t box[2] = {(cuuint32_t)SK, (cuuint32_t)TBM};
+    cuuint32_t box[2] = {(cuuint32_t)SK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -1135,7 +1158,7 @@ GroupLayout group_layout(const lofgb_gemm_task* tasks, int n) {
         g.alo.push_back(off); off = align_up(off + a, 1024);
         g.bhi.push_back(off); off = align_up(off + b, 1024);
         g.blo.push_back(off); off = align_up(off + b, 1024);
-        g.tiles += (int64_t)(Mp / TBM) * (Np / TBN);
+        g.tiles += (int64_t)(Mp / TBM) * (Np / 64);  // room for the narrow tile's count
         g.split_items += (int64_t)(Mp / 32) * (Kp / 64) + (int64_t)(Np / 32) * (Kp / 64);
     }
     g.ws_total = off;
@@ -1169,6 +1192,8 @@ int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* w
     if (ntasks <= 0) return set_error(LOFGB_ERR_SIZE, "need at least one task");
     if (!tasks || !table || !workspace || !num_tiles || !split_items)
         return set_error(LOFGB_ERR_NULL, "NULL tasks, workspace, table or output count");
+    const int tile_n = (schedule & LOFGB_GROUPED_TILE_N64) ? 64 : 128;
+    schedule &= ~LOFGB_GROUPED_TILE_N64;
     if (schedule < 0 || schedule > 2) return set_error(LOFGB_ERR_UNSUPPORTED, "schedule %d", schedule);
     for (int i = 0; i < ntasks; ++i) {
         const int st = check_task(tasks[i], i);
@@ -1185,7 +1210,7 @@ int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* w
     uint8_t* ws = static_cast<uint8_t*>(workspace);
     GroupHeader* h = reinterpret_cast<GroupHeader*>(tb);
     h->ntasks = ntasks;
-    h->ntiles = (int32_t)g.tiles;
+    h->tile_n = tile_n;
     h->nsplit = 2 * ntasks;
     h->split_items = g.split_items;
     h->rows_off = (int64_t)g.rows_off;
@@ -1228,12 +1253,12 @@ int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* w
         int rc;
         if ((rc = make_map(&r.map[0], ahi, g.Mp[i], g.Kp[i]))) return rc;
         if ((rc = make_map(&r.map[1], alo, g.Mp[i], g.Kp[i]))) return rc;
-        if ((rc = make_map(&r.map[2], bhi, g.Np[i], g.Kp[i]))) return rc;
-        if ((rc = make_map(&r.map[3], blo, g.Np[i], g.Kp[i]))) return rc;
+        if ((rc = make_map(&r.map[2], bhi, g.Np[i], g.Kp[i], tile_n))) return rc;
+        if ((rc = make_map(&r.map[3], blo, g.Np[i], g.Kp[i], tile_n))) return rc;
         const int nchunks = (g.Kp[i] / 16 + r.chunk16 - 1) / r.chunk16;
         const int64_t cost = 4 * (int64_t)nchunks + g.Kp[i] / SK;
         for (int mt = 0; mt < g.Mp[i] / TBM; ++mt)
-            for (int nt = 0; nt < g.Np[i] / TBN; ++nt) cands.push_back({i, mt * TBM, nt * TBN, cost});
+            for (int nt = 0; nt < g.Np[i] / tile_n; ++nt) cands.push_back({i, mt * TBM, nt * tile_n, cost});
     }
     if (schedule >= 1)
         std::stable_sort(cands.begin(), cands.end(),
@@ -1251,6 +1276,7 @@ int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* w
         }
         tl[pidx] = TileRef{cands[src_idx].task, cands[src_idx].m0, cands[src_idx].n0, 0};
     }
+    h->ntiles = (int32_t)nt;
     *num_tiles = nt;
     *split_items = g.split_items;
     return LOFGB_OK;

@@ -1,7 +1,8 @@
 """Grouped tensor-core GEMM: every task equals the single-GEMM tensor-core
-path bit for bit (same MMA sequence per tile), under every schedule, from a
-captured CUDA graph, and with ragged shapes; the autotuner picks and caches a
-schedule."""
+path bit for bit (the same products summed per output, whether a tile is
+128 or 64 columns wide), under every tile shape and schedule, from a
+captured CUDA graph, and with ragged shapes; the autotuner picks and caches
+a (tile shape, schedule) pair."""
 import json
 
 import pytest
@@ -34,7 +35,8 @@ def _reference(t):
                    trans_b=bool(t["trans_b"]), alpha=t["alpha"], variant="tc", chunk=t["chunk"])
 
 
-@pytest.mark.parametrize("schedule", ["task", "lpt", "lpt_snake"])
+@pytest.mark.parametrize("schedule", ["task", "lpt", "lpt_snake", "128x64/task", "128x64/lpt",
+                                      "128x64/lpt_snake"])
 def test_grouped_matches_single(schedule):
     tasks = _tasks(10, 1)
     gg = lg.GroupedGemm(tasks, schedule=schedule)
@@ -46,9 +48,10 @@ def test_grouped_matches_single(schedule):
         assert torch.equal(t["D"], _reference(t)), i
 
 
-def test_grouped_ragged_and_graph():
+@pytest.mark.parametrize("schedule", ["lpt_snake", "128x64/lpt_snake"])
+def test_grouped_ragged_and_graph(schedule):
     tasks = _tasks(7, 2, dims=(1, 300), ragged=True)
-    gg = lg.GroupedGemm(tasks, schedule="lpt_snake", grid=37)
+    gg = lg.GroupedGemm(tasks, schedule=schedule, grid=37)
     gg.capture()
     for t in tasks:
         t["D"].zero_()
@@ -63,9 +66,9 @@ def test_autotuner_caches(tmp_path, monkeypatch):
     monkeypatch.setattr(autotune, "CACHE_PATH", str(tmp_path / "tune.json"))
     tasks = _tasks(6, 3)
     gg = lg.GroupedGemm(tasks, schedule="auto", tune_reps=2)
-    assert gg.schedule in autotune.SCHEDULES
+    assert gg.schedule in autotune.CHOICES
     cache = json.loads((tmp_path / "tune.json").read_text())
-    assert gg.signature in cache and set(cache[gg.signature]["ms"]) == set(autotune.SCHEDULES)
+    assert gg.signature in cache and set(cache[gg.signature]["ms"]) == set(autotune.CHOICES)
     again = lg.GroupedGemm(tasks, schedule="auto")
     assert again.schedule == gg.schedule
     again()
