@@ -140,6 +140,16 @@ int lofgb_mx_round_f32(const float* in, float* out, int64_t n, int block_size,
                        int mode, int scale_mode, int stoch_len, uint64_t seed,
                        uint64_t offset, void* stream);
 
+/* The same MX rounding of a BF16 tensor (bit patterns, uint16_t), written as
+ * FP32: equal to lofgb_mx_round_f32 on the tensor widened to FP32 (widening
+ * is exact), without that copy. No counterpart in the reference, whose MX op
+ * takes FP32 only (src/LoPy_bind.cpp:172); it serves BF16 master weights and
+ * activations (the linear-layer workload). Input and output may not overlap. */
+int lofgb_mx_round_bf16(const uint16_t* in, float* out, int64_t n, int block_size,
+                        const lofgb_format* elem_fmt, const lofgb_format* scale_fmt,
+                        int mode, int scale_mode, int stoch_len, uint64_t seed,
+                        uint64_t offset, void* stream);
+
 /* ---- (c) emulated-accumulation GEMM --------------------------------------
  * Replaces LoF_gemm (src/Lof_kernel.cu:96-154) → lo_float::Gemm::run_scaled
  * (src/cutlass_gemms.cuh:1777-1787) with the OpLoFMultiplyAdd leaf

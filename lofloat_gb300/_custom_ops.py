@@ -64,7 +64,7 @@ def _define():
     @virtual_mx_round_op.register_fake
     def _(input, block_size, element_format_id, scale_format_id, round_mode, scale_round_mode,
           stoch_len):
-        return torch.empty_like(input)
+        return torch.empty_like(input, dtype=torch.float32)  # bfloat16 inputs give float32
 
     @torch.library.custom_op("lofloat::lof_gemm", mutates_args=())
     def lof_gemm_op(A: torch.Tensor, B: torch.Tensor, accum_mant_bits: int, round_mode: int,

@@ -67,6 +67,8 @@ SIGNATURES = [
     ("lofgb_round_mantissa_f16", _i32, [_vp, _vp, _i64, _i32, _i32, _i32, _f32, _u64, _u64, _vp]),
     ("lofgb_mx_round_f32", _i32, [_vp, _vp, _i64, _i32, _FP, _FP, _i32, _i32, _i32, _u64, _u64,
                                   _vp]),
+    ("lofgb_mx_round_bf16", _i32, [_vp, _vp, _i64, _i32, _FP, _FP, _i32, _i32, _i32, _u64, _u64,
+                                   _vp]),
     ("lofgb_gemm_f32", _i32, [_vp, _i64, _i32, _vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32,
                               _i32, _i32, _f32, _i32, _i32, _vp, _sz, _vp]),
     ("lofgb_gemm_tc_workspace_size", _sz, [_i32, _i32, _i32]),

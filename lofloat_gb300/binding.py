@@ -211,28 +211,31 @@ def virtual_mx_round(input: torch.Tensor, block_size: int, element_format: Float
                      offset: int | None = None) -> torch.Tensor:
     """MX block fake-quantisation (src/LoPy_bind.cpp:165-217): contiguous blocks
     of `block_size`, one shared scale per block in `scale_format`, elements
-    rounded into `element_format` and rescaled. float32 only."""
-    if input.dtype != torch.float32:
-        raise RuntimeError("virtual_mx_round: float32 tensors only")
+    rounded into `element_format` and rescaled. float32 input (the reference's
+    only type), or bfloat16 input rounded exactly as its float32 copy would
+    be, without making it (lofgb_mx_round_bf16); the result is float32."""
+    if input.dtype not in (torch.float32, torch.bfloat16):
+        raise RuntimeError("virtual_mx_round: float32 or bfloat16 tensors only")
     if int(block_size) <= 0:
         raise RuntimeError("virtual_mx_round: block_size must be positive")
     _require_cuda(input, "virtual_mx_round")
     x = input.contiguous()
-    y = torch.empty_like(x) if out is None else out
-    if y.shape != x.shape or y.dtype != x.dtype or not y.is_contiguous() or y.device != x.device:
-        raise RuntimeError("virtual_mx_round: out must be a contiguous float32 tensor like input")
+    y = torch.empty(x.shape, dtype=torch.float32, device=x.device) if out is None else out
+    if y.shape != x.shape or y.dtype != torch.float32 or not y.is_contiguous() or y.device != x.device:
+        raise RuntimeError("virtual_mx_round: out must be a contiguous float32 tensor of the input's shape")
     n = x.numel()
     mode = int(round_mode)
     if seed is None:
         s, o = _take_counters(mode, n)
     else:
         s, o = int(seed), int(offset or 0)
+    fn = "lofgb_mx_round_bf16" if x.dtype == torch.bfloat16 else "lofgb_mx_round_f32"
     with torch.cuda.device(x.device):
-        check(_native.lib().lofgb_mx_round_f32(
+        check(getattr(_native.lib(), fn)(
             x.data_ptr(), y.data_ptr(), n, int(block_size), C.byref(element_format.c_format),
             C.byref(scale_format.c_format), mode, int(scale_round_mode), int(stoch_len), s, o,
             _stream(x)), "virtual_mx_round")
-    return y.view_as(input)
+    return y.view(input.shape)
 
 
 def gemm_alpha(scale_a: float, scale_b: float) -> float:

@@ -305,6 +305,50 @@ LOFGB_ROUND_MANT(lofgb_round_mantissa_f32, float, 32, float)
 LOFGB_ROUND_MANT(lofgb_round_mantissa_f64, double, 64, double)
 LOFGB_ROUND_MANT(lofgb_round_mantissa_f16, uint16_t, 16, float)
 
+// Shared by the FP32 and BF16 MX entry points: validation, plans, pmn.
+static int mx_prepare(int64_t n, int block_size, const lofgb_format* elem_fmt,
+                      const lofgb_format* scale_fmt, int mode, int scale_mode, int stoch_len,
+                      RoundPlan* pe, RoundPlan* ps, float* inv_pmn) {
+    if (!(block_size == 8 || block_size == 16 || block_size == 32 || block_size == 64 ||
+          block_size == 128 || block_size == 256))
+        return set_error(LOFGB_ERR_BLOCK, "unsupported MX block size %d", block_size);
+    int st;
+    if ((st = make_round_plan(pe, elem_fmt, 32, mode, stoch_len))) return st;
+    if ((st = make_round_plan(ps, scale_fmt, 32, scale_mode, 0))) return st;
+    (void)n;
+    const int m = elem_fmt->mantissa_bits;
+    const int me = (elem_fmt->signedness == LOFGB_SIGNED)
+                       ? (1 << (elem_fmt->bitwidth - m - 1)) - 1 - elem_fmt->bias
+                       : (1 << (elem_fmt->bitwidth - m)) - 1 - elem_fmt->bias;
+    volatile float a = std::ldexp(1.0f, me);
+    volatile float b = 2.0f - std::ldexp(1.0f, -m);
+    volatile float pmn = a * b;
+    *inv_pmn = 1.0f / pmn;
+    return LOFGB_OK;
+}
+
+int lofgb_mx_round_bf16(const uint16_t* in, float* out, int64_t n, int block_size,
+                        const lofgb_format* elem_fmt, const lofgb_format* scale_fmt, int mode,
+                        int scale_mode, int stoch_len, uint64_t seed, uint64_t offset,
+                        void* stream) {
+    g_detail[0] = 0;
+    if (n < 0) return set_error(LOFGB_ERR_SIZE, "negative element count");
+    if (n > 0 && (!in || !out)) return set_error(LOFGB_ERR_NULL, "NULL data pointer");
+    if (n > 0) {
+        // a 2n-byte input and a 4n-byte output must not overlap at all
+        const char* a = reinterpret_cast<const char*>(in);
+        const char* b = reinterpret_cast<const char*>(out);
+        if (a < b + 4 * n && b < a + 2 * n)
+            return set_error(LOFGB_ERR_ALIAS, "input and output overlap");
+    }
+    RoundPlan pe, ps;
+    float inv;
+    int st = mx_prepare(n, block_size, elem_fmt, scale_fmt, mode, scale_mode, stoch_len, &pe, &ps, &inv);
+    if (st) return st;
+    if (n == 0) return LOFGB_OK;
+    return launch_mx_bf16(in, out, n, block_size, pe, ps, inv, seed, offset, stream);
+}
+
 int lofgb_mx_round_f32(const float* in, float* out, int64_t n, int block_size,
                        const lofgb_format* elem_fmt, const lofgb_format* scale_fmt, int mode,
                        int scale_mode, int stoch_len, uint64_t seed, uint64_t offset,

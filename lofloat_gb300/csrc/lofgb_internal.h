@@ -138,6 +138,10 @@ int launch_round(int src_bits, bool fmt, const void* in, void* out, int64_t n,
 int launch_mx(const float* in, float* out, int64_t n, int block, const RoundPlan& pe,
               const RoundPlan& ps, float pmn, float inv_pmn, uint64_t seed, uint64_t offset,
               void* stream);
+// MX rounding of BF16 bit patterns (widened to FP32 on load) to FP32 output.
+int launch_mx_bf16(const uint16_t* in, float* out, int64_t n, int block, const RoundPlan& pe,
+                   const RoundPlan& ps, float inv_pmn, uint64_t seed, uint64_t offset,
+                   void* stream);
 // Strided batches: GEMM z reads A + z*sa, B + z*sb and writes D + z*sd.
 // acc_fmt (optional, RNE plan of an f32 source) rounds the accumulator into a
 // whole format after every MAC / chunk instead of to mbits mantissa bits.

@@ -32,14 +32,45 @@ constexpr int RING = 3;  // cp.async stages per thread (RING - 1 runs prefetched
 
 constexpr uint64_t SCALE_SALT = 0x5CA1E5CA1E5CA1E5ull;
 
-template <bool ALIGNED>
-__device__ __forceinline__ float4 load4(const float* in, int64_t e, int64_t n) {
-    if (ALIGNED && e + 3 < n) return __ldcs(reinterpret_cast<const float4*>(in + e));
+// Element sources: FP32, or BF16 bit patterns widened to FP32 on load (exact),
+// so that rounding a BF16 tensor equals rounding its FP32 copy without
+// making one. Raw is what one lane's four elements occupy in memory.
+template <typename T> struct Src;
+template <> struct Src<float> {
+    using Raw = float4;
+    static __device__ __forceinline__ float4 cvt(Raw r) { return r; }
+    static __device__ __forceinline__ float one(float v) { return v; }
+};
+template <> struct Src<uint16_t> {
+    using Raw = uint2;
+    static __device__ __forceinline__ float4 cvt(Raw r) {
+        return make_float4(__uint_as_float(r.x << 16), __uint_as_float(r.x & 0xFFFF0000u),
+                           __uint_as_float(r.y << 16), __uint_as_float(r.y & 0xFFFF0000u));
+    }
+    static __device__ __forceinline__ float one(uint16_t v) { return __uint_as_float((uint32_t)v << 16); }
+};
+
+template <typename T>
+__device__ __forceinline__ void cp_async_raw(void* smem, const T* gmem) {
+    if constexpr (sizeof(typename Src<T>::Raw) == 16) {
+        cp_async16(smem, gmem);
+    } else {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(smem)),
+                     "l"(gmem)
+                     : "memory");
+    }
+}
+
+template <typename T, bool ALIGNED>
+__device__ __forceinline__ float4 load4(const T* in, int64_t e, int64_t n) {
+    if (ALIGNED && e + 3 < n)
+        return Src<T>::cvt(__ldcs(reinterpret_cast<const typename Src<T>::Raw*>(in + e)));
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (e + 0 < n) v.x = __ldcs(in + e + 0);
-    if (e + 1 < n) v.y = __ldcs(in + e + 1);
-    if (e + 2 < n) v.z = __ldcs(in + e + 2);
-    if (e + 3 < n) v.w = __ldcs(in + e + 3);
+    if (e + 0 < n) v.x = Src<T>::one(__ldcs(in + e + 0));
+    if (e + 1 < n) v.y = Src<T>::one(__ldcs(in + e + 1));
+    if (e + 2 < n) v.z = Src<T>::one(__ldcs(in + e + 2));
+    if (e + 3 < n) v.w = Src<T>::one(__ldcs(in + e + 3));
     return v;
 }
 
@@ -202,9 +233,9 @@ __device__ __forceinline__ void mx_full_slots(const float4 (&v)[MxGeo<BS>::U][Mx
 // The float-grid instantiations fit 5 CTAs of 256 threads per SM (<= 48
 // registers, the occupancy the HBM stream needs); the general ones would
 // spill under that bound.
-template <int BS, int EMODE, int SMODE, bool ALIGNED, int UNI = 0>
+template <typename T, int BS, int EMODE, int SMODE, bool ALIGNED, int UNI = 0>
 __global__ void __launch_bounds__(MT, UNI != 0 ? 5 : 1)
-mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, float inv_pmn,
+mx_kernel(const T* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, float inv_pmn,
           uint64_t seed, uint64_t offset) {
     pdl_wait();
     using G = MxGeo<BS>;
@@ -222,14 +253,14 @@ mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, fl
         // shared memory with cp.async while it rounds the current run, so the
         // HBM reads in flight do not occupy registers; a thread only reads
         // back what it copied itself, so no CTA barrier is needed.
-        __shared__ float4 ring[RING][U * VPT][MT];
+        __shared__ typename Src<T>::Raw ring[RING][U * VPT][MT];
         auto issue = [&](int stage, int64_t s) {
 #pragma unroll
             for (int u = 0; u < U; ++u)
 #pragma unroll
                 for (int j = 0; j < VPT; ++j)
-                    cp_async16(&ring[stage][u * VPT + j][threadIdx.x],
-                               in + (s + u) * SLOT + j * 128 + lane * 4);
+                    cp_async_raw(&ring[stage][u * VPT + j][threadIdx.x],
+                                 in + (s + u) * SLOT + j * 128 + lane * 4);
         };
         int64_t sp = s0;  // next run to prefetch
 #pragma unroll
@@ -246,7 +277,7 @@ mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, fl
 #pragma unroll
             for (int u = 0; u < U; ++u)
 #pragma unroll
-                for (int j = 0; j < VPT; ++j) v[u][j] = ring[stage][u * VPT + j][threadIdx.x];
+                for (int j = 0; j < VPT; ++j) v[u][j] = Src<T>::cvt(ring[stage][u * VPT + j][threadIdx.x]);
             mx_full_slots<BS, EMODE, SMODE, UNI>(v, out, s0, lane, pe, ps, inv_pmn, seed, offset);
             stage = stage == RING - 1 ? 0 : stage + 1;
         }
@@ -260,7 +291,7 @@ mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, fl
 #pragma unroll
             for (int j = 0; j < VPT; ++j) {
                 const int64_t e = (s0 + u) * SLOT + j * 128 + lane * 4;
-                v[u][j] = (s0 + u < nslots) ? load4<ALIGNED>(in, e, n) : make_float4(0.f, 0.f, 0.f, 0.f);
+                v[u][j] = (s0 + u < nslots) ? load4<T, ALIGNED>(in, e, n) : make_float4(0.f, 0.f, 0.f, 0.f);
             }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -287,6 +318,37 @@ mx_kernel(const float* in, float* out, int64_t n, RoundPlan pe, RoundPlan ps, fl
 
 template <int BS>
 int launch_bs(const float* in, float* out, int64_t n, const RoundPlan& pe, const RoundPlan& ps,
+              float inv_pmn, uint64_t seed, uint64_t offset, cudaStream_t st);
+
+// BF16 sources: the float-grid RNE instantiations when the buffers allow
+// vectors (input 8-byte, output 16-byte aligned), the general one otherwise.
+template <int BS>
+int launch_bs_bf16(const uint16_t* in, float* out, int64_t n, const RoundPlan& pe,
+                   const RoundPlan& ps, float inv_pmn, uint64_t seed, uint64_t offset,
+                   cudaStream_t st) {
+    constexpr int VPT = BS >= 256 ? BS / 128 : 1;
+    constexpr int SLOT = 128 * VPT;
+    constexpr int U = VPT == 1 ? 4 : 2;
+    const int64_t warps_needed = ((n + SLOT - 1) / SLOT + U - 1) / U;
+    int64_t g = (warps_needed + (MT / 32) - 1) / (MT / 32);
+    const int maxg = sm_count() * (2048 / MT);
+    const int grid = (int)(g < 1 ? 1 : (g < maxg ? g : maxg));
+    const bool aligned = ((reinterpret_cast<uintptr_t>(in) & 7) | (reinterpret_cast<uintptr_t>(out) & 15)) == 0;
+    const bool rne = pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE && pe.uni == 1;
+    if (aligned && rne && BS == 32 && pe.saturating)
+        launch_pdl(mx_kernel<uint16_t, 32, LOFGB_RNE, LOFGB_RNE, true, 4>, grid, MT, 0, st, in, out, n,
+                   pe, ps, inv_pmn, seed, offset);
+    else if (aligned && rne)
+        launch_pdl(mx_kernel<uint16_t, BS, LOFGB_RNE, LOFGB_RNE, true, 1>, grid, MT, 0, st, in, out, n,
+                   pe, ps, inv_pmn, seed, offset);
+    else
+        launch_pdl(mx_kernel<uint16_t, BS, -1, -1, false>, grid, MT, 0, st, in, out, n, pe, ps,
+                   inv_pmn, seed, offset);
+    return check_launch("mx_kernel(bf16)");
+}
+
+template <int BS>
+int launch_bs(const float* in, float* out, int64_t n, const RoundPlan& pe, const RoundPlan& ps,
               float inv_pmn, uint64_t seed, uint64_t offset, cudaStream_t st) {
     constexpr int VPT = BS >= 256 ? BS / 128 : 1;
     constexpr int SLOT = 128 * VPT;
@@ -298,17 +360,17 @@ int launch_bs(const float* in, float* out, int64_t n, const RoundPlan& pe, const
     const int grid = (int)(g < 1 ? 1 : (g < maxg ? g : maxg));
     const bool aligned = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15) == 0;
     if (!aligned)
-        launch_pdl(mx_kernel<BS, -1, -1, false>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<float, BS, -1, -1, false>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (BS == 32 && pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE && pe.uni == 1 && pe.saturating)
-        launch_pdl(mx_kernel<32, LOFGB_RNE, LOFGB_RNE, true, 4>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<float, 32, LOFGB_RNE, LOFGB_RNE, true, 4>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE && pe.uni == 1)
-        launch_pdl(mx_kernel<BS, LOFGB_RNE, LOFGB_RNE, true, 1>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<float, BS, LOFGB_RNE, LOFGB_RNE, true, 1>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (pe.mode == LOFGB_RNE && ps.mode == LOFGB_RNE)
-        launch_pdl(mx_kernel<BS, LOFGB_RNE, LOFGB_RNE, true>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<float, BS, LOFGB_RNE, LOFGB_RNE, true>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else if (ps.mode == LOFGB_RNE)
-        launch_pdl(mx_kernel<BS, -1, LOFGB_RNE, true>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<float, BS, -1, LOFGB_RNE, true>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     else
-        launch_pdl(mx_kernel<BS, -1, -1, true>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
+        launch_pdl(mx_kernel<float, BS, -1, -1, true>, grid, MT, 0, st, in, out, n, pe, ps, inv_pmn, seed, offset);
     return check_launch("mx_kernel");
 }
 
@@ -326,6 +388,21 @@ int launch_mx(const float* in, float* out, int64_t n, int block, const RoundPlan
     case 64: return launch_bs<64>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
     case 128: return launch_bs<128>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
     case 256: return launch_bs<256>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    default: return set_error(LOFGB_ERR_BLOCK, "unsupported MX block size %d", block);
+    }
+}
+
+int launch_mx_bf16(const uint16_t* in, float* out, int64_t n, int block, const RoundPlan& pe,
+                   const RoundPlan& ps, float inv_pmn, uint64_t seed, uint64_t offset,
+                   void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (block) {
+    case 8: return launch_bs_bf16<8>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    case 16: return launch_bs_bf16<16>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    case 32: return launch_bs_bf16<32>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    case 64: return launch_bs_bf16<64>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    case 128: return launch_bs_bf16<128>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
+    case 256: return launch_bs_bf16<256>(in, out, n, pe, ps, inv_pmn, seed, offset, st);
     default: return set_error(LOFGB_ERR_BLOCK, "unsupported MX block size %d", block);
     }
 }

@@ -201,7 +201,7 @@ class LinearConfig:
 
 def _mx(t, fmt, cfg):
     if fmt is None:
-        return t.contiguous()
+        return t.float().contiguous()
     return lof.virtual_mx_round(t.contiguous(), cfg.mx_block, fmt, cfg.scale_format,
                                 round_mode=cfg.round_mode)
 
@@ -218,10 +218,9 @@ class LoFLinearFunction(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, x, w, cfg: LinearConfig):
-        x32 = x.float()
-        w32 = w.float()
-        xq = _mx(x32, cfg.act_format, cfg)
-        wq = _mx(w32, cfg.weight_format, cfg)
+        # MX rounding reads BF16 masters directly (no FP32 copy first)
+        xq = _mx(x, cfg.act_format, cfg)
+        wq = _mx(w, cfg.weight_format, cfg)
         y = lof.gemm(xq, wq, cfg.accum_mant_bits, trans_b=True, alpha=cfg.alpha, variant=cfg.variant,
                      chunk=cfg.chunk, accum_format=cfg.accum_format)
         ctx.save_for_backward(xq, wq)
@@ -234,11 +233,12 @@ class LoFLinearFunction(torch.autograd.Function):
         xq, wq = ctx.saved_tensors
         cfg = ctx.cfg
         dy = dy.float().contiguous()
-        if cfg.alpha != 1.0:
-            dy = dy * cfg.alpha
         if cfg.grad_format is not None:
+            # alpha rides in the rounding kernel's input scale: round(alpha * dY)
             dy = lof.virtual_round(dy, cfg.grad_format, round_mode=cfg.grad_round_mode,
-                                   stoch_len=cfg.grad_stoch_len)
+                                   stoch_len=cfg.grad_stoch_len, scale=cfg.alpha)
+        elif cfg.alpha != 1.0:
+            dy = dy * cfg.alpha
         dx = dw = None
         if ctx.needs_input_grad[0]:
             dx = lof.gemm(dy, wq, cfg.accum_mant_bits, variant=cfg.grad_variant, chunk=cfg.chunk,

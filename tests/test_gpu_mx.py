@@ -131,3 +131,34 @@ def test_exact_block_roundtrip_and_errors():
         lg.virtual_mx_round(exact, 48, e4m3, lg.create_e8m0_params())
     with pytest.raises(RuntimeError):
         lg.virtual_mx_round(exact, 0, e4m3, lg.create_e8m0_params())
+
+
+@pytest.mark.parametrize("bs", [8, 32, 64, 256])
+@pytest.mark.parametrize("mode", [0, 1, 3])
+@pytest.mark.parametrize("skew", [0, 1, 2])
+def test_bf16_source_equals_fp32_copy(bs, mode, skew):
+    """lofgb_mx_round_bf16 on BF16 bit patterns equals lofgb_mx_round_f32 on the
+    same values widened to FP32, bit for bit: every block size class, a
+    deterministic and a stochastic mode, and inputs offset by 0, 2 or 4
+    bytes (vector and scalar paths), with a ragged last block."""
+    g = torch.Generator(device="cuda").manual_seed(bs * 10 + mode)
+    n = 40 * bs + 5
+    base = (torch.randn(n + skew, device="cuda", generator=g) *
+            torch.exp2(torch.randint(-12, 13, (n + skew,), device="cuda", generator=g).float()))
+    xb = base.bfloat16()[skew:]
+    e4m3, e8 = lg.create_p3109_params(8, 4), lg.create_e8m0_params()
+    got = lg.virtual_mx_round(xb, bs, e4m3, e8, round_mode=mode, stoch_len=8 if mode == 3 else 0,
+                              seed=3, offset=11)
+    want = lg.virtual_mx_round(xb.float(), bs, e4m3, e8, round_mode=mode,
+                               stoch_len=8 if mode == 3 else 0, seed=3, offset=11)
+    assert got.dtype == torch.float32
+    assert torch.equal(got.view(torch.int32), want.view(torch.int32))
+
+
+def test_bf16_source_config4_operands():
+    """The linear layer's MX-E4M3 rounding of BF16 masters (8192 x 4096) read
+    directly equals rounding the FP32 copy."""
+    g = torch.Generator(device="cuda").manual_seed(4)
+    X = torch.randn(8192, 4096, device="cuda", generator=g).bfloat16()
+    e4m3, e8 = lg.create_p3109_params(8, 4), lg.create_e8m0_params()
+    assert torch.equal(lg.virtual_mx_round(X, 32, e4m3, e8), lg.virtual_mx_round(X.float(), 32, e4m3, e8))
