@@ -52,6 +52,11 @@ struct CodecArg {
     uint32_t min_norm_bits;   // FP32 bits of the smallest target normal, 2^(1-bias)
     uint32_t code_off;        // normal code = (bits >> (23 - m)) - code_off
     float sub_c;              // 2^23 * tiny: subnormal code = bits(v + sub_c) - bits(sub_c)
+    // Veltkamp form of the fast encode (velt, formats with 1..22 mantissa
+    // bits): the normal range rounds |x| to m bits as t - (t - |x|),
+    // t = |x| * sigma, sigma = 2^(23 - m) + 1, on the FMA pipe
+    int velt;
+    float sigma;
     uint32_t max_finite, ovf_code, inf_code, neg_zero_code, neg_code, sign_mask;
     uint32_t neg_keep, neg_or, neg_zero;  // a negative finite code: code ? (code & keep) | or : zero
     // Fast decode: every finite value is a normal FP32 number or an exact
@@ -193,6 +198,44 @@ __device__ __forceinline__ uint32_t codec_encode_fast(float from, const CodecArg
     return (neg && !a.is_signed) ? a.neg_code : code;
 }
 
+// The fast encode with the target-normal range rounded by Veltkamp's split:
+// for a normal FP32 |x| and 1 <= 23 - m <= 22, t - (t - |x|) with
+// t = |x| (2^(23-m) + 1) is |x| rounded to m bits, ties to even, whenever t
+// is finite (checked over every FP32 pattern), which is codec_encode_fast's
+// float-grid result; a t that overflows only happens far above the largest
+// finite code, and its NaN or infinity bits give a code above ovf_code, which
+// the min clamps as before. Inputs below the smallest target normal take the
+// tiny grid as in codec_encode_fast (a value that rounds up to 2^to_min
+// there gives the first normal code, 2^m). Fewer ALU-pipe operations than
+// the clamped grid constant.
+template <bool SPECIAL>
+__device__ __forceinline__ uint32_t codec_encode_velt(float from, const CodecArg& a) {
+    const uint32_t fb = __float_as_uint(from);
+    const bool neg = (fb >> 31) != 0;
+    const uint32_t mb = fb & 0x7FFFFFFFu;
+    const float ax = __uint_as_float(mb);
+    const float t = __fmul_rn(ax, a.sigma);
+    const float v = __fmaf_rn(__fmaf_rn(ax, -1.0f, t), -1.0f, t);
+    const uint32_t nrm = (__float_as_uint(v) >> (23 - a.m)) - a.code_off;
+    const uint32_t sub = __float_as_uint(__fadd_rn(ax, a.sub_c)) - __float_as_uint(a.sub_c);
+    uint32_t code = min(mb < a.min_norm_bits ? sub : nrm, a.ovf_code);
+    if (!SPECIAL) {
+        const uint32_t ns = code == 0u ? a.neg_zero : ((code & a.neg_keep) | a.neg_or);
+        return neg ? ns : code;
+    }
+    code = mb == 0x7F800000u ? a.inf_code : code;
+    code = (neg && a.is_signed) ? (code == 0u ? a.neg_zero_code : (code | a.sign_mask)) : code;
+    code = mb > 0x7F800000u ? a.qnan : code;
+    return (neg && !a.is_signed) ? a.neg_code : code;
+}
+
+// The fast encode of one value: Veltkamp form where it applies, else the
+// clamped float grid (a.velt is uniform over the launch).
+template <bool SPECIAL>
+__device__ __forceinline__ uint32_t encode_fast_any(float from, const CodecArg& a) {
+    return a.velt ? codec_encode_velt<SPECIAL>(from, a) : codec_encode_fast<SPECIAL>(from, a);
+}
+
 // convert_rep_to_float for formats whose values FP32 holds exactly
 // (CodecArg::dec_fast).
 __device__ __forceinline__ float codec_decode_fast(uint32_t rep, const CodecArg& a) {
@@ -226,6 +269,14 @@ __device__ __forceinline__ float codec_decode(uint32_t rep, const CodecArg& a) {
     const int x = (e == 0 ? 1 : (int)e) - a.bias - a.m;
     const float v = ldexpf(__uint2float_rn(k), x < -300 ? -300 : (x > 300 ? 300 : x));
     return sign ? -v : v;
+}
+
+// One code's value: the direct bit construction for the formats that allow
+// it, else the general restatement.
+template <bool FAST>
+__device__ __forceinline__ float decode_one(uint32_t rep, const CodecArg& a) {
+    if constexpr (FAST) return codec_decode_fast(rep, a);
+    else return codec_decode(rep, a);
 }
 
 constexpr int cgcd(int x, int y) { return y == 0 ? x : cgcd(y, x % y); }
@@ -372,7 +423,10 @@ __device__ __forceinline__ void encode4(const float (&x)[4], uint32_t (&c)[4], c
         for (int q = 0; q < 4; ++q) sp |= (__float_as_uint(x[q]) & 0x7FFFFFFFu) >= 0x7F800000u;
         if (__any_sync(__activemask(), sp)) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) c[q] = codec_encode_fast<true>(x[q], a);
+            for (int q = 0; q < 4; ++q) c[q] = encode_fast_any<true>(x[q], a);
+        } else if (a.velt) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) c[q] = codec_encode_velt<false>(x[q], a);
         } else {
 #pragma unroll
             for (int q = 0; q < 4; ++q) c[q] = codec_encode_fast<false>(x[q], a);
@@ -463,7 +517,7 @@ decode_direct_kernel(const uint8_t* __restrict__ src, float4* __restrict__ dst, 
             unpack4<N, REV>(w[u], c);
             float y[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) y[q] = FAST ? codec_decode_fast(c[q], a) : codec_decode(c[q], a);
+            for (int q = 0; q < 4; ++q) y[q] = decode_one<FAST>(c[q], a);
             __stcs(dst + v, make_float4(y[0], y[1], y[2], y[3]));
         }
     }
@@ -506,7 +560,10 @@ __device__ __forceinline__ void encode_chunk(const float (&x)[ChunkGeo<N>::G], u
         for (int i = 0; i < G; ++i) sp |= (__float_as_uint(x[i]) & 0x7FFFFFFFu) >= 0x7F800000u;
         if (__any_sync(__activemask(), sp)) {
 #pragma unroll
-            for (int i = 0; i < G; ++i) c[i] = codec_encode_fast<true>(x[i], a);
+            for (int i = 0; i < G; ++i) c[i] = encode_fast_any<true>(x[i], a);
+        } else if (a.velt) {
+#pragma unroll
+            for (int i = 0; i < G; ++i) c[i] = codec_encode_velt<false>(x[i], a);
         } else {
 #pragma unroll
             for (int i = 0; i < G; ++i) c[i] = codec_encode_fast<false>(x[i], a);
@@ -581,7 +638,7 @@ __device__ __forceinline__ void decode_chunk(const uint32_t (&in)[ChunkGeo<N>::W
         const uint32_t code = (uint32_t)buf & ((1u << N) - 1u);
         buf >>= N;
         avail -= N;
-        y[slot_element<N, REV>(sl)] = FAST ? codec_decode_fast(code, a) : codec_decode(code, a);
+        y[slot_element<N, REV>(sl)] = decode_one<FAST>(code, a);
     }
 }
 
@@ -757,6 +814,12 @@ int make_codec_arg(CodecArg* a, const lofgb_codec_format* f, int mode, int sat, 
         a->min_norm_bits = (uint32_t)(to_min + 127) << 23;
         a->code_off = (uint32_t)(127 - bias) << m;
         a->sub_c = std::ldexp(1.0f, to_min - m + 23);
+    }
+    a->velt = 0;
+    a->sigma = 0.0f;
+    if (a->enc_fast == 1 && m >= 1 && m <= 22) {
+        a->velt = 1;
+        a->sigma = (float)((1u << (23 - m)) + 1u);
     }
     a->dec_fast = 0;
     if (to_min + 127 >= 1 && to_max + 127 <= 254 && to_min - m >= -149 && to_min - m + 23 <= 127) {
