@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--only", default=None,
                     choices=["mx", "round_rne", "round_sr", "gemm_plain", "gemm_tc", "conv_plain",
                              "conv_tc", "pwl", "encode", "decode", "encode_fp6", "decode_fp6",
-                             "grouped_round", "bn_train", "bn_eval"],
+                             "grouped_round", "bn_train", "bn_eval", "mx_encode"],
                     help="run one workload's kernel warmup+steps times and exit (for ncu captures)")
     ap.add_argument("--size", default="full", choices=["full", "small"],
                     help="with --only: full-size workload or a small case (GEMM 1024^3)")
@@ -460,6 +460,19 @@ def codec_workloads(torch, lg, dev, peaks):
             gbs = n * (4 + bits / 8) / (ms * 1e-3) / 1e9
             out[f"codec_{tag}_{name}_2^26_GBs"] = round(gbs, 1)
             out[f"codec_{tag}_{name}_2^26_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)
+    # MX storage of the config-2 matrix in one pass: E4M3 / FP6 element codes
+    # and E8M0 block scales (4 B read, bits/8 + 1/32 B written per value)
+    del x, y
+    xm = config2_input(torch, None).to(dev)
+    e8 = lg.create_e8m0_params()
+    for name, fmt in (("e4m3", lg.create_p3109_params(8, 4)), ("p3109_6p3", lg.create_p3109_params(6, 3))):
+        fn = lambda: lg.mx_encode(xm, fmt, e8)  # noqa: E731
+        for _ in range(3):
+            fn()
+        ms = time_batched(torch, fn, stream)
+        nbytes = xm.numel() * (4 + fmt.total_bits / 8 + 1 / 32)
+        out[f"mx_encode_{name}_8192^2_GBs"] = round(nbytes / (ms * 1e-3) / 1e9, 1)
+        out[f"mx_encode_{name}_8192^2_frac_hbm"] = round(nbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)
     return out
 
 
@@ -875,6 +888,10 @@ def run_only(args):
         fn = (lambda: lg.lof_encode(x, fmt, out=packed)) if args.only.startswith("encode") else \
             (lambda: lg.lof_decode(packed, n, fmt, out=y))  # noqa: E731
         work, unit = n * (4 + bits / 8), "GB/s"
+    elif args.only == "mx_encode":
+        x = config2_input(torch, None).to(dev)
+        fn = lambda: lg.mx_encode(x, e4m3, e8)  # noqa: E731
+        work, unit = x.numel() * (4 + 1 + 1 / 32), "GB/s"
     elif args.only in ("bn_train", "bn_eval"):
         x = torch.randn(*BN_SHAPE, device=dev) * 2 + 0.5
         m = lg.L1BatchNorm(BN_SHAPE[1]).to(dev).train(args.only == "bn_train")

@@ -508,6 +508,28 @@ int lofgb_encode_f32(uint8_t* dst, const float* src, int64_t count, const lofgb_
 int lofgb_decode_f32(float* dst, const uint8_t* src, int64_t count, const lofgb_codec_format* fmt,
                      int reverse, void* stream);
 
+/* MX storage in one pass: MX block rounding (as lofgb_mx_round_f32, blocks of
+ * 32) whose outputs are stored as codes instead of rescaled values. Per block
+ * of 32 values: the scale s = virtual_round(amax * (1/pmn), scale format,
+ * scale_mode) and the rounded quotients q_i = virtual_round(x_i / s, element
+ * format, mode) (+0 when s is not positive); `codes` receives the q_i as
+ * element codes and `scales` one code per block for s, both encoded as
+ * lofgb_encode_f32 encodes (RNE, sat_mode; forward groups, so the element
+ * codes are lofgb_packed_size(bits, count) bytes and the scale codes
+ * ceil(count / 32) bytes). decode(code_i) * decode(scale code) is the MX
+ * rounding's output wherever q_i is a value of the element format (every q_i
+ * but the saturating pass-through of an overflowing quotient, which the
+ * codec's sat_mode maps to the largest finite code or infinity). Element
+ * codes of 4, 6 or 8 bits, 8-bit scale codes (E8M0). No counterpart in the
+ * reference, which rounds MX in FP32 (src/mx_round.cuh:27-214) and packs
+ * per-element formats only (src/lo_pack.hpp:474-500); this writes the two
+ * together as MX storage, one HBM read and (bits + 1/4) / 8 bytes written per
+ * value. */
+int lofgb_mx_encode_f32(const float* src, uint8_t* codes, uint8_t* scales, int64_t count,
+                        int block_size, const lofgb_codec_format* elem_fmt,
+                        const lofgb_codec_format* scale_fmt, int mode, int scale_mode,
+                        int sat_mode, int stoch_len, uint64_t seed, uint64_t offset, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,8 +18,8 @@ from . import _custom_ops  # noqa: F401  (registers torch.ops.lofloat.*)
 from .binding import (FloatFormatDescriptor, InfBehavior, NaNBehavior, RoundingMode, Signedness,
                       SaturationMode, codec_format, conv2d, conv2d_alpha, gemm, gemm_alpha,
                       gemm_f64_reference, get_rng_state, lof_conv2d, lof_decode, lof_encode, lof_gemm,
-                      packed_size, pwl_silu, set_rng_state, set_seed, virtual_mx_round,
-                      virtual_round)
+                      mx_decode, mx_encode, packed_size, pwl_silu, set_rng_state, set_seed,
+                      virtual_mx_round, virtual_round)
 from .formats import (create_e8m0_params, create_half_params, create_p3109_params,
                       create_single_params, make_format)
 from .layers import (LinearConfig, LoF_Conv2d, LoF_Linear, LoF_MultiHeadAttention, LoF_Quantize,
@@ -39,6 +39,7 @@ __all__ = [
     "mantissa_quantize", "exp_mant_quantize",
     "register_format", "get_format", "GroupedRound", "GroupedGemm", "lof_conv2d", "conv2d",
     "conv2d_alpha", "pwl_silu", "LoF_Conv2d", "PWLSiLU", "LoF_MultiHeadAttention",
-    "SaturationMode", "codec_format", "packed_size", "lof_encode", "lof_decode",
+    "SaturationMode", "codec_format", "packed_size", "lof_encode", "lof_decode", "mx_encode",
+    "mx_decode",
     "L1BatchNorm", "LinfBatchNorm", "FISRBatchNorm", "PWLBatchNorm",
 ]

@@ -585,13 +585,29 @@ class SaturationMode(enum.IntEnum):
     SatPropagate = 2
 
 
+_codec_cache: dict = {}
+
+
 def codec_format(params: FloatFormatDescriptor, neg_to_nan: bool = False):
     """lofgb_codec_format for `params`: the checkers' predicates are evaluated
     over every code of the format (at most 2^16) and matched to the forms the
     kernels evaluate — IsInf(rep) <=> (rep | inf_or) == inf_match; IsNaN as a
     single pattern, the IEEE exponent-all-ones range, or never. Raises for a
     checker that fits neither (the reference's P3109, IEEE-style, OCP, E8M0
-    and trivial checkers all fit)."""
+    and trivial checkers all fit). Cached per (format fields, checker
+    objects, neg_to_nan): the scan costs about as much as a kernel launch."""
+    key = (params.total_bits, params.mantissa_bits, params.bias, int(params.inf_behavior),
+           int(params.nan_behavior), int(params.signedness), id(params.is_inf_checker),
+           id(params.is_nan_checker), bool(neg_to_nan))
+    hit = _codec_cache.get(key)
+    if hit is None:
+        # the checkers stay referenced with their entry, so their ids stay theirs
+        hit = (_codec_format_scan(params, neg_to_nan), params.is_inf_checker, params.is_nan_checker)
+        _codec_cache[key] = hit
+    return hit[0]
+
+
+def _codec_format_scan(params: FloatFormatDescriptor, neg_to_nan: bool):
     n, m = params.total_bits, params.mantissa_bits
     if not 1 <= n <= 16:
         raise RuntimeError(f"codec: bitwidth {n} outside [1, 16]")
@@ -664,6 +680,47 @@ def lof_encode(input: torch.Tensor, params: FloatFormatDescriptor,
                                              mode, int(saturation), int(stoch_len), int(reverse),
                                              s, o, _stream(x)), "lof_encode")
     return y
+
+
+def mx_encode(input: torch.Tensor, element_format: FloatFormatDescriptor,
+              scale_format: FloatFormatDescriptor, round_mode=RoundingMode.RoundToNearestEven,
+              scale_round_mode=RoundingMode.RoundToNearestEven,
+              saturation=SaturationMode.SatFinite, stoch_len: int = 0, *, block_size: int = 32,
+              seed: int | None = None, offset: int | None = None):
+    """MX storage of a float32 tensor in one pass (lofgb_mx_encode_f32):
+    returns (element codes, block-scale codes) as uint8 tensors — the MX
+    block rounding's quotients as packed `element_format` codes (4, 6 or 8
+    bits) and one `scale_format` code (8 bits, e.g. E8M0) per block of 32."""
+    if input.dtype != torch.float32:
+        raise RuntimeError("mx_encode: float32 input only")
+    _require_cuda(input, "mx_encode")
+    x = input.contiguous()
+    ef, sf = codec_format(element_format), codec_format(scale_format)
+    n = x.numel()
+    codes = torch.empty(packed_size(element_format.total_bits, n), dtype=torch.uint8, device=x.device)
+    scales = torch.empty((n + block_size - 1) // max(1, block_size), dtype=torch.uint8, device=x.device)
+    mode = int(round_mode)
+    if seed is None:
+        s, o = _take_counters(mode, n)
+    else:
+        s, o = int(seed), int(offset or 0)
+    with torch.cuda.device(x.device):
+        check(_native.lib().lofgb_mx_encode_f32(x.data_ptr(), codes.data_ptr(), scales.data_ptr(), n,
+                                                int(block_size), C.byref(ef), C.byref(sf), mode,
+                                                int(scale_round_mode), int(saturation), int(stoch_len),
+                                                s, o, _stream(x)), "mx_encode")
+    return codes, scales
+
+
+def mx_decode(codes: torch.Tensor, scales: torch.Tensor, count: int,
+              element_format: FloatFormatDescriptor, scale_format: FloatFormatDescriptor, *,
+              block_size: int = 32) -> torch.Tensor:
+    """Values of MX storage: decoded element codes times their block's decoded
+    scale (a float32 tensor of `count` values)."""
+    q = lof_decode(codes, count, element_format)
+    nb = (count + block_size - 1) // block_size
+    sc = lof_decode(scales, nb, scale_format)
+    return (q.view(-1)[:count] * sc.repeat_interleave(block_size)[:count])
 
 
 def lof_decode(packed: torch.Tensor, count: int, params: FloatFormatDescriptor, *,

@@ -246,6 +246,17 @@ int check_gemm_args(const void* A, int64_t lda, int ta, const void* B, int64_t l
     return LOFGB_OK;
 }
 
+// 1 / pmn of an MX element format (src/mx_round.cuh:52-56), in FP32.
+float mx_inv_pmn(const lofgb_format* ef) {
+    const int m = ef->mantissa_bits;
+    const int me = (ef->signedness == LOFGB_SIGNED) ? (1 << (ef->bitwidth - m - 1)) - 1 - ef->bias
+                                                    : (1 << (ef->bitwidth - m)) - 1 - ef->bias;
+    volatile float a = std::ldexp(1.0f, me);
+    volatile float b = 2.0f - std::ldexp(1.0f, -m);
+    volatile float pmn = a * b;
+    return 1.0f / pmn;
+}
+
 }  // namespace lofgb
 
 using namespace lofgb;

@@ -29,6 +29,7 @@
 #include <cmath>
 
 #include "lof_round.cuh"
+#include "mx_common.cuh"
 
 namespace lofgb {
 
@@ -951,6 +952,143 @@ int launch_decode_n(const uint8_t* src, float* dst, int64_t count, int reverse, 
     case 15: return FN<15>(__VA_ARGS__); default: return FN<16>(__VA_ARGS__);                 \
     }
 
+
+// ---- MX storage: round to MX and encode, one pass --------------------------------
+// A warp step covers 4 blocks of 32 values; lane l holds values 4l..4l+3 of
+// the step, so each block lives in 8 lanes (amax by a 3-step butterfly) and
+// each lane's 4 codes are one whole group of the forward packing for 4-, 6-
+// and 8-bit codes (2, 3 or 4 bytes at byte offset 4l N / 8). A warp loads
+// four steps before it computes; the 16 block scales of those steps are
+// rounded one per lane and shuffled back. Per block: the MX scale
+// (mx_common.cuh), the rounded quotients q = vr(x / scale, elem) (+0 when the
+// scale is not positive), their codes under RNE and the codec's saturation
+// (the infinity / NaN checks only in warps that hold one), and the scale's
+// code, one byte per block. Values past the end take code bits 0, the
+// codec's zero padding.
+template <int N, bool UNI>
+__global__ void __launch_bounds__(256)
+mx_encode_kernel(const float* __restrict__ in, uint8_t* __restrict__ codes,
+                 uint8_t* __restrict__ scales, int64_t n, RoundPlan pe, RoundPlan ps,
+                 float inv_pmn, CodecArg ea, CodecArg sa, uint64_t seed, uint64_t offset, int vec,
+                 int64_t code_bytes) {
+    pdl_wait();
+    static_assert(N == 4 || N == 6 || N == 8, "MX storage codes of 4, 6 or 8 bits");
+    constexpr int U = 4;  // steps of 128 values per warp iteration, loaded up front
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * 256 + threadIdx.x) >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * 8;
+    const int64_t steps = (n + 127) / 128;
+    for (int64_t s0 = warp * U; s0 < steps; s0 += nwarps * U) {
+        float x[U][4];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t e = (s0 + u) * 128 + lane * 4;
+            if (vec && e + 3 < n) {
+                const float4 v = __ldcs(reinterpret_cast<const float4*>(in + e));
+                x[u][0] = v.x; x[u][1] = v.y; x[u][2] = v.z; x[u][3] = v.w;
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) x[u][q] = e + q < n ? __ldcs(in + e + q) : 0.0f;
+            }
+        }
+        // block amax in the 8 lanes of each block, then one scale per block:
+        // lane j < 16 rounds the scale of (step j / 4, block j % 4) and every
+        // lane fetches its own blocks' scale bits
+        float amax[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            amax[u] = fmaxf(fmaxf(fabsf(x[u][0]), fabsf(x[u][1])), fmaxf(fabsf(x[u][2]), fabsf(x[u][3])));
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1) amax[u] = fmaxf(amax[u], __shfl_xor_sync(0xFFFFFFFFu, amax[u], o));
+        }
+        const int uj = (lane >> 2) & 3, bj = lane & 3;
+        float aj = 0.0f;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const float g = __shfl_sync(0xFFFFFFFFu, amax[u], bj * 8);
+            aj = u == uj ? g : aj;
+        }
+        const int64_t blkj = (s0 + uj) * 128 + (int64_t)bj * 32;
+        const BlockScale bsj = block_scale<-1>(aj, ps, inv_pmn, seed, offset + (uint64_t)blkj);
+        const uint32_t sbj = __float_as_uint(bsj.scale);
+        if (lane < 16 && blkj < n)
+            scales[blkj / 32] = (uint8_t)codec_encode<LOFGB_RNE>(bsj.scale, sa, 0ull);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t e = (s0 + u) * 128 + lane * 4;
+            if ((s0 + u) * 128 >= n) break;  // warp-uniform
+            const BlockScale b = scale_from_bits(__shfl_sync(0xFFFFFFFFu, sbj, u * 4 + (lane >> 3)));
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                w[q] = __float_as_uint(b.pow2 ? __fmul_rn(x[u][q], b.inv) : __fdiv_rn(x[u][q], b.scale));
+            if constexpr (UNI) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) w[q] = vr_uni_f32<LOFGB_RNE, 1>(w[q], pe);
+            } else {
+                uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
+                if (mode_is_stochastic(pe.mode)) rng_elem4(seed, offset + (uint64_t)e, pe.rng_lg, r);
+                vr_format_f32x4<-1, false>(w, pe, r);
+            }
+            float qv[4];
+            bool sp = false;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                qv[q] = b.pos ? __uint_as_float(w[q]) : 0.0f;
+                sp |= (__float_as_uint(qv[q]) & 0x7FFFFFFFu) >= 0x7F800000u;
+            }
+            uint32_t c[4];
+            if (!ea.enc_fast) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) c[q] = codec_encode<LOFGB_RNE>(qv[q], ea, 0ull);
+            } else if (__any_sync(0xFFFFFFFFu, sp)) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) c[q] = encode_fast_any<true>(qv[q], ea);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) c[q] = encode_fast_any<false>(qv[q], ea);
+            }
+            uint32_t packed = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) packed |= (e + q < n ? (c[q] & ((1u << N) - 1u)) : 0u) << (q * N);
+            constexpr int BYTES = N / 2;  // 4 codes of N bits
+            const int64_t off = e / 4 * BYTES;
+            if (off < code_bytes) {
+                uint8_t* dst = codes + off;
+                const bool whole = off + BYTES <= code_bytes;
+                if (N == 8 && whole && (reinterpret_cast<uintptr_t>(dst) & 3) == 0) {
+                    *reinterpret_cast<uint32_t*>(dst) = packed;
+                } else if (N == 4 && whole && (reinterpret_cast<uintptr_t>(dst) & 1) == 0) {
+                    *reinterpret_cast<uint16_t*>(dst) = (uint16_t)packed;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < BYTES; ++k)
+                        if (off + k < code_bytes) dst[k] = (uint8_t)(packed >> (8 * k));
+                }
+            }
+        }
+    }
+}
+
+template <int N>
+int launch_mx_encode_n(const float* in, uint8_t* codes, uint8_t* scales, int64_t n,
+                       const RoundPlan& pe, const RoundPlan& ps, float inv_pmn, const CodecArg& ea,
+                       const CodecArg& sa, uint64_t seed, uint64_t offset, cudaStream_t st) {
+    const int64_t steps = (n + 127) / 128;
+    const int64_t need = (steps + 31) / 32;   // 8 warps x 4 steps per CTA iteration
+    const int64_t maxg = (int64_t)sm_count() * 8;
+    const int grid = (int)(need < 1 ? 1 : (need < maxg ? need : maxg));
+    const int vec = (reinterpret_cast<uintptr_t>(in) & 15) == 0;
+    const int64_t cb = packed_bytes(N, n);
+    if (pe.mode == LOFGB_RNE && pe.uni == 1)
+        launch_pdl(mx_encode_kernel<N, true>, grid, 256, 0, st, in, codes, scales, n, pe, ps, inv_pmn,
+                   ea, sa, seed, offset, vec, cb);
+    else
+        launch_pdl(mx_encode_kernel<N, false>, grid, 256, 0, st, in, codes, scales, n, pe, ps, inv_pmn,
+                   ea, sa, seed, offset, vec, cb);
+    return check_launch("mx_encode_kernel");
+}
+
 int codec_pointers(const void* a, const void* b, int64_t count) {
     if (count < 0) return set_error(LOFGB_ERR_SIZE, "negative count");
     if (count > 0 && (!a || !b)) return set_error(LOFGB_ERR_NULL, "NULL buffer");
@@ -991,6 +1129,43 @@ int lofgb_encode_f32(uint8_t* dst, const float* src, int64_t count, const lofgb_
     const int n = a.n;
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
     LOFGB_BY_N(launch_encode_n, src, dst, count, reverse, a, cs)
+}
+
+
+int lofgb_mx_encode_f32(const float* src, uint8_t* codes, uint8_t* scales, int64_t count,
+                        int block_size, const lofgb_codec_format* elem_fmt,
+                        const lofgb_codec_format* scale_fmt, int mode, int scale_mode,
+                        int sat_mode, int stoch_len, uint64_t seed, uint64_t offset, void* stream) {
+    clear_error();
+    if (block_size != 32) return set_error(LOFGB_ERR_BLOCK, "MX storage blocks are 32 values (got %d)", block_size);
+    if (!elem_fmt || !scale_fmt) return set_error(LOFGB_ERR_NULL, "NULL codec format");
+    const int nb = elem_fmt->fmt.bitwidth;
+    if (nb != 4 && nb != 6 && nb != 8)
+        return set_error(LOFGB_ERR_UNSUPPORTED, "MX storage element codes of %d bits (4, 6 or 8 supported)", nb);
+    if (scale_fmt->fmt.bitwidth != 8)
+        return set_error(LOFGB_ERR_UNSUPPORTED, "MX storage scale codes must be 8 bits");
+    CodecArg ea, sa;
+    int st = make_codec_arg(&ea, elem_fmt, LOFGB_RNE, sat_mode, 0);
+    if (!st) st = make_codec_arg(&sa, scale_fmt, LOFGB_RNE, sat_mode, 0);
+    if (st) return st;
+    RoundPlan pe, ps;
+    if ((st = make_round_plan(&pe, &elem_fmt->fmt, 32, mode, stoch_len))) return st;
+    if ((st = make_round_plan(&ps, &scale_fmt->fmt, 32, scale_mode, 0))) return st;
+    if (count < 0) return set_error(LOFGB_ERR_SIZE, "negative count");
+    if (count == 0) return LOFGB_OK;
+    if (!src || !codes || !scales) return set_error(LOFGB_ERR_NULL, "NULL data pointer");
+    const int64_t cbytes = packed_bytes(nb, count), sbytes = (count + 31) / 32;
+    const char* s = reinterpret_cast<const char*>(src);
+    const char* c = reinterpret_cast<const char*>(codes);
+    const char* k = reinterpret_cast<const char*>(scales);
+    if ((s < c + cbytes && c < s + count * 4) || (s < k + sbytes && k < s + count * 4) ||
+        (c < k + sbytes && k < c + cbytes))
+        return set_error(LOFGB_ERR_ALIAS, "input, codes and scales must not overlap");
+    const float inv = mx_inv_pmn(&elem_fmt->fmt);
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    if (nb == 4) return launch_mx_encode_n<4>(src, codes, scales, count, pe, ps, inv, ea, sa, seed, offset, cs);
+    if (nb == 6) return launch_mx_encode_n<6>(src, codes, scales, count, pe, ps, inv, ea, sa, seed, offset, cs);
+    return launch_mx_encode_n<8>(src, codes, scales, count, pe, ps, inv, ea, sa, seed, offset, cs);
 }
 
 int lofgb_decode_f32(float* dst, const uint8_t* src, int64_t count, const lofgb_codec_format* fmt,

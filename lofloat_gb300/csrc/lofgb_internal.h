@@ -138,6 +138,9 @@ int launch_round(int src_bits, bool fmt, const void* in, void* out, int64_t n,
 int launch_mx(const float* in, float* out, int64_t n, int block, const RoundPlan& pe,
               const RoundPlan& ps, float pmn, float inv_pmn, uint64_t seed, uint64_t offset,
               void* stream);
+// 1 / pmn of an MX element format, pmn = 2^emax (2 - 2^-m) in FP32
+// (src/mx_round.cuh:52-56): the scale is virtual_round(amax * (1 / pmn)).
+float mx_inv_pmn(const lofgb_format* ef);
 // MX rounding of BF16 bit patterns (widened to FP32 on load) to FP32 output.
 int launch_mx_bf16(const uint16_t* in, float* out, int64_t n, int block, const RoundPlan& pe,
                    const RoundPlan& ps, float inv_pmn, uint64_t seed, uint64_t offset,

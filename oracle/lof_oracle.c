@@ -600,20 +600,56 @@ int orc_round_mantissa_f16(const uint16_t* in, uint16_t* out, int64_t n, int mbi
 /* ------------------------------------------------------------------------ */
 #define ORC_SCALE_SALT 0x5CA1E5CA1E5CA1E5ull
 
+/* One MX block (cnt <= block values from element b0): its scale and the
+ * rounded quotients q_i = vr(x_i / scale) (+0 when the scale is not
+ * positive). out = q_i * scale is the MX round; the MX encode stores q_i and
+ * the scale as codes. */
+static float mx_block(const float* in, int64_t b0, int64_t cnt, const fconst_t* ce,
+                      const fconst_t* cs, float pmn, float inv, int mode, int scale_mode, int len,
+                      int lg, uint64_t seed, uint64_t offset, int scale_formula, float* q) {
+    float amax = 0.0f;
+    for (int64_t i = 0; i < cnt; ++i) amax = fmaxf(amax, fabsf(in[b0 + i]));
+    const float sin = scale_formula ? amax / pmn : amax * inv;
+    uint64_t rs = orc_rng(seed ^ ORC_SCALE_SALT, offset + (uint64_t)b0);
+    const float scale =
+        u2f((uint32_t)vr_fmt(f2u(sin), &SRC_F32, cs, scale_mode, 0, rs, usamp_of(rs)));
+    for (int64_t i = 0; i < cnt; ++i) {
+        if (!(scale > 0.0f)) {
+            q[i] = 0.0f;
+            continue;
+        }
+        const float x = in[b0 + i] / scale;
+        uint64_t rb = orc_rng_elem(seed, offset + (uint64_t)(b0 + i), lg);
+        q[i] = u2f((uint32_t)vr_fmt(f2u(x), &SRC_F32, ce, mode, len, rb, usamp_of(rb)));
+    }
+    return scale;
+}
+
+static int mx_check(const float* in, int64_t n, int block, const lofgb_format* ef,
+                    const lofgb_format* sf, int mode, int scale_mode, int len) {
+    if (n < 0) return LOFGB_ERR_SIZE;
+    if (n > 0 && !in) return LOFGB_ERR_NULL;
+    int st = orc_validate_format(ef, 23);
+    if (!st) st = orc_validate_format(sf, 23);
+    if (!st) st = validate_mode(mode, len);
+    if (!st) st = validate_mode(scale_mode, 0);
+    if (!st && block <= 0) st = LOFGB_ERR_BLOCK;
+    return st;
+}
+
+static float mx_pmn(const fconst_t* ce, const lofgb_format* ef) {
+    return ldexpf(1.0f, ce->to_max_exp) * (2.0f - ldexpf(1.0f, -ef->mantissa_bits));
+}
+
 int orc_mx_round_f32(const float* in, float* out, int64_t n, int block,
                      const lofgb_format* ef, const lofgb_format* sf, int mode,
                      int scale_mode, int len, uint64_t seed, uint64_t offset,
                      int scale_formula, int nthreads) {
     int st = check_arrays(in, out, n);
-    if (!st) st = orc_validate_format(ef, 23);
-    if (!st) st = orc_validate_format(sf, 23);
-    if (!st) st = validate_mode(mode, len);
-    if (!st) st = validate_mode(scale_mode, 0);
-    if (!st && block <= 0) st = LOFGB_ERR_BLOCK;
+    if (!st) st = mx_check(in, n, block, ef, sf, mode, scale_mode, len);
     if (st) return st;
     fconst_t ce = make_consts(ef), cs = make_consts(sf);
-    const int me = ce.to_max_exp;
-    const float pmn = ldexpf(1.0f, me) * (2.0f - ldexpf(1.0f, -ef->mantissa_bits));
+    const float pmn = mx_pmn(&ce, ef);
     const float inv = 1.0f / pmn;
     const int64_t nb = (n + block - 1) / block;
     const int lg = orc_rng_lanes_log2(mode, len);
@@ -621,25 +657,48 @@ int orc_mx_round_f32(const float* in, float* out, int64_t n, int block,
     for (int64_t b = 0; b < nb; ++b) {
         const int64_t b0 = b * block;
         const int64_t cnt = (n - b0) < block ? (n - b0) : block;
-        float amax = 0.0f;
-        for (int64_t i = 0; i < cnt; ++i) amax = fmaxf(amax, fabsf(in[b0 + i]));
-        const float sin = scale_formula ? amax / pmn : amax * inv;
-        uint64_t rs = orc_rng(seed ^ ORC_SCALE_SALT, offset + (uint64_t)b0);
-        const float scale =
-            u2f((uint32_t)vr_fmt(f2u(sin), &SRC_F32, &cs, scale_mode, 0, rs, usamp_of(rs)));
-        if (!(scale > 0.0f)) {
-            for (int64_t i = 0; i < cnt; ++i) out[b0 + i] = 0.0f;
-            continue;
-        }
-        for (int64_t i = 0; i < cnt; ++i) {
-            const float q = in[b0 + i] / scale;
-            uint64_t rb = orc_rng_elem(seed, offset + (uint64_t)(b0 + i), lg);
-            const float qr =
-                u2f((uint32_t)vr_fmt(f2u(q), &SRC_F32, &ce, mode, len, rb, usamp_of(rb)));
-            out[b0 + i] = qr * scale;
-        }
+        /* the rounded quotients go straight into out, then get rescaled */
+        const float scale = mx_block(in, b0, cnt, &ce, &cs, pmn, inv, mode, scale_mode, len, lg,
+                                     seed, offset, scale_formula, out + b0);
+        for (int64_t i = 0; i < cnt; ++i) out[b0 + i] = scale > 0.0f ? out[b0 + i] * scale : 0.0f;
     }
     return 0;
+}
+
+/* MX storage: the block scales and rounded quotients of orc_mx_round_f32 (GPU
+ * scale form), encoded with the storage codec under RNE and `sat`: element
+ * codes packed as orc_encode_f32 packs them (forward groups), one scale code
+ * per block packed likewise. codes holds orc_packed_size(ef bits, n) bytes,
+ * scales orc_packed_size(sf bits, ceil(n / block)). */
+int orc_mx_encode_f32(const float* in, int64_t n, int block, const lofgb_codec_format* ef,
+                      const lofgb_codec_format* sf, int mode, int scale_mode, int len, int sat,
+                      uint64_t seed, uint64_t offset, uint8_t* codes, uint8_t* scales) {
+    if (!ef || !sf) return LOFGB_ERR_NULL;
+    int st = mx_check(in, n, block, &ef->fmt, &sf->fmt, mode, scale_mode, len);
+    if (st) return st;
+    fconst_t ce = make_consts(&ef->fmt), cs = make_consts(&sf->fmt);
+    const float pmn = mx_pmn(&ce, &ef->fmt);
+    const float inv = 1.0f / pmn;
+    const int64_t nb = (n + block - 1) / block;
+    const int lg = orc_rng_lanes_log2(mode, len);
+    float* q = (float*)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+    float* sc = (float*)malloc(sizeof(float) * (size_t)(nb > 0 ? nb : 1));
+    if (!q || !sc) {
+        free(q);
+        free(sc);
+        return LOFGB_ERR_SIZE;
+    }
+    for (int64_t b = 0; b < nb; ++b) {
+        const int64_t b0 = b * block;
+        const int64_t cnt = (n - b0) < block ? (n - b0) : block;
+        sc[b] = mx_block(in, b0, cnt, &ce, &cs, pmn, inv, mode, scale_mode, len, lg, seed, offset, 0,
+                         q + b0);
+    }
+    st = orc_encode_f32(codes, q, n, ef, LOFGB_RNE, sat, 0, 0, 0, 0);
+    if (!st) st = orc_encode_f32(scales, sc, nb, sf, LOFGB_RNE, sat, 0, 0, 0, 0);
+    free(q);
+    free(sc);
+    return st;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -93,6 +93,12 @@ int orc_mx_round_f32(const float* in, float* out, int64_t n, int block,
                      int scale_mode, int len, uint64_t seed, uint64_t offset,
                      int scale_formula, int nthreads);
 
+/* MX storage (lofgb_mx_encode_f32 semantics): the block scales and rounded
+ * quotients of orc_mx_round_f32 encoded with the storage codec (RNE, `sat`). */
+int orc_mx_encode_f32(const float* in, int64_t n, int block, const lofgb_codec_format* ef,
+                      const lofgb_codec_format* sf, int mode, int scale_mode, int len, int sat,
+                      uint64_t seed, uint64_t offset, uint8_t* codes, uint8_t* scales);
+
 /* Emulated-accumulation GEMM, sequential k, device round-to-odd FMA.
  * Same layout arguments as lofgb_gemm_f32. */
 int orc_gemm_f32(const float* A, int64_t lda, int trans_a, const float* B, int64_t ldb,

@@ -89,6 +89,7 @@ def lib():
         L.orc_packed_size.argtypes = [i32, i64]
         L.orc_encode_f32.argtypes = [vp, vp, i64, CP, i32, i32, i32, i32, u64, u64]
         L.orc_decode_f32.argtypes = [vp, vp, i64, CP, i32]
+        L.orc_mx_encode_f32.argtypes = [vp, i64, i32, CP, CP, i32, i32, i32, i32, u64, u64, vp, vp]
         L.orc_gemm_accfmt_f32.argtypes = [vp, i64, i32, vp, i64, i32, vp, i64, i32, i32, i32, P,
                                           f32, i32]
         L.orc_rto_fma.restype = f32
@@ -327,6 +328,18 @@ def encode(x, f: CodecFormat, mode: int = 0, sat: int = 0, stoch_len: int = 0,
     _check(lib().orc_encode_f32(_p(out), _p(x), x.size, C.byref(f), mode, sat, stoch_len, reverse,
                                 seed, offset))
     return out
+
+
+def mx_encode(x, block: int, ef: CodecFormat, sf: CodecFormat, mode: int = 0, scale_mode: int = 0,
+              stoch_len: int = 0, sat: int = 1, seed: int = 0, offset: int = 0):
+    """MX storage of x: (packed element codes, packed block-scale codes)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    nb = (x.size + block - 1) // block
+    codes = np.zeros(packed_size(ef.fmt.bitwidth, x.size), np.uint8)
+    scales = np.zeros(packed_size(sf.fmt.bitwidth, nb), np.uint8)
+    _check(lib().orc_mx_encode_f32(_p(x), x.size, block, C.byref(ef), C.byref(sf), mode, scale_mode,
+                                   stoch_len, sat, seed, offset, _p(codes), _p(scales)))
+    return codes, scales
 
 
 def decode(packed, count: int, f: CodecFormat, reverse: int = 0) -> np.ndarray:
