@@ -355,7 +355,7 @@ int launch_conv_tc(const ConvGeo& g, int mbits, float alpha, int chunk, void* wo
     int rc = check_launch("split_conv_weight_kernel");
     if (rc) return rc;
     split_im2col_kernel<ORDER><<<(int)(ib < maxg ? ib : maxg), 256, 0, st>>>(g, w.Np, w.Kp, bhi, blo,
-                                                                          range + 2);
+                                                                          range + 3);
     if ((rc = check_launch("split_im2col_kernel"))) return rc;
     return launch_tc_presplit(ws, w, g.y, g.L, 0, g.K, g.ncols, mbits, alpha, chunk, g.L,
                               (int64_t)g.K * g.L, stream);

@@ -16,11 +16,14 @@
 // padded by a split kernel. Each k-step of 16 issues three MMAs
 // (hi·hi, hi·lo, lo·hi); the dropped lo·lo term is below 2^-16 relative.
 // Values that are exact in 8 significant bits (E4M3/E5M2/E2M1 times a
-// power-of-two scale) have lo = 0 and enter exactly.
+// power-of-two scale) have lo = 0 and enter exactly; the split kernels flag
+// an operand whose lo parts are all zero, and its lo tiles are then neither
+// loaded nor multiplied (MX operands: one MMA per k-step, half the bytes).
 //
 // Kernel layout (one CTA per SM, persistent over 128 x 128 output tiles):
-//   warp 0      TMA producer: 4 tiles (A hi/lo, B hi/lo) of 64 k per stage,
-//               3 stages, 128-byte swizzle, one mbarrier per stage;
+//   warp 0      TMA producer: up to 4 tiles (A hi/lo, B hi/lo) of 64 k per
+//               stage, 3 to 6 stages in 192 KiB (more when lo tiles are
+//               left out), 128-byte swizzle, one mbarrier per stage;
 //   warp 1      TMEM owner and MMA issuer (one elected lane):
 //               tcgen05.mma.cta_group::1.kind::f16, M=128 N=128 K=16,
 //               chunk sums in four 128-column TMEM buffers (all 512
@@ -60,9 +63,11 @@ constexpr int TILE_A = TBM * SK * 2;           // 16 KiB per A operand tile
 constexpr int PIPE_BYTES = 192 * 1024;         // shared memory of the stage ring
 
 // Tile shapes of the persistent kernel: 128 x BN outputs per tile.
-//   BN = 128: stages of 64 KiB (A hi, A lo, B hi, B lo), 3 stages; four
-//             128-column TMEM chunk buffers; 16 epilogue warps of 32 columns;
-//   BN = 64:  stages of 48 KiB, 4 stages; eight 64-column chunk buffers; 8
+//   BN = 128: stages of 64 KiB (A hi, A lo, B hi, B lo), 3 stages (6 of
+//             32 KiB without lo tiles); four 128-column TMEM chunk buffers;
+//             16 epilogue warps of 32 columns;
+//   BN = 64:  stages of 48 KiB, 4 stages (8 without lo tiles); eight
+//             64-column chunk buffers; 8
 //             epilogue warps of 32 columns (the grouped kernel's narrow tile,
 //             more tiles for load balance across uneven GEMMs).
 template <int BN>
@@ -70,6 +75,7 @@ struct TileShape {
     static constexpr int TILE_B = BN * SK * 2;
     static constexpr int STAGE_BYTES = 2 * TILE_A + 2 * TILE_B;
     static constexpr int STAGES = PIPE_BYTES / STAGE_BYTES;
+    static constexpr int MAXST = PIPE_BYTES / (TILE_A + TILE_B);   // stages of hi tiles only
     static constexpr int EPI_WARPS = BN == 128 ? 16 : 8;   // EPI_WARPS / 4 per TMEM lane quarter
     static constexpr int EPI_COLS = BN * 4 / EPI_WARPS;    // accumulator columns per epilogue thread
     static constexpr int NBUF = 512 / BN;                  // TMEM chunk buffers (all 512 columns)
@@ -80,9 +86,10 @@ struct TileShape {
     static_assert(EPI_COLS == 64 || EPI_COLS == 32, "the epilogue folds 16-column pieces, 4 or 2 per chunk");
     static_assert((NBUF & (NBUF - 1)) == 0 && NBUF * BN == 512, "TMEM chunk buffers");
     static_assert(STAGES * STAGE_BYTES <= PIPE_BYTES && STAGES >= 3, "stage ring");
+    static_assert(2 * MAXST + 2 * NBUF + 1 <= 56, "barrier area");
 };
 constexpr int NUM_THREADS = 32 * (2 + 16);     // launch size of every shape (idle warps exit)
-constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + PIPE_BYTES + 256 /*barriers*/;
+constexpr size_t SMEM_BYTES = 1024 /*align slack*/ + PIPE_BYTES + 512 /*barriers, flags*/;
 constexpr unsigned long long WAIT_LIMIT_NS = 2000000000ull;
 
 // Limit of every bounded wait, and for the wait self-test the pipeline stage
@@ -396,12 +403,13 @@ struct GroupHeader {   // at the start of the device table; offsets from its bas
     int64_t split_items;
     int64_t rows_off, tiles_off, splits_off;
     int* status;
-    // exponent ranges of all A and all B operands (zero in the prepared
-    // table; the split kernel raises them, the GEMM kernel reads them and its
-    // last CTA clears them, and the reader count, for the next launch)
-    uint32_t range[4];
+    // exponent ranges and lo flags of all A and all B operands (zero in the
+    // prepared table; the split kernel raises them, the GEMM kernel reads
+    // them and its last CTA clears them, and the reader count, for the next
+    // launch)
+    uint32_t range[6];
     uint32_t range_readers;
-    uint32_t pad2[3];
+    uint32_t pad2[1];
 };
 
 struct GroupedSrc {
@@ -436,38 +444,40 @@ struct GroupedSrc {
 // ---- the persistent tensor-core body (shared by both launches) ---------------
 // ACCK: 0 RNE to ro mantissa bits; 2 / 3 a whole-format accumulator (acc_plan)
 // by the whole-range float rounding / by the integer rounding core.
-// range: the four exponent-range words the split kernels published (A's
-// largest field, 255 - its smallest non-zero field, the same for B);
-// reset_range: the last CTA to read them clears them (and range[4], the
-// reader count) for the next launch of the same device table.
+// range: the six words the split kernels published (A's largest field,
+// 255 - its smallest non-zero field, whether a lo part is non-zero; the
+// same for B); reset_range: the last CTA to read them clears them (and
+// range[6], the reader count) for the next launch of the same device table.
+// An operand whose lo parts are all zero has its lo tiles neither loaded nor
+// multiplied: one, two or three MMAs per k step of 16.
 template <int ACCK, int BN, class Src>
 __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* smem_raw,
                                        uint32_t* range, bool reset_range, const WaitCfg wcfg,
                                        const RoundPlan* acc_plan = nullptr) {
     using Shape = TileShape<BN>;
-    constexpr int TBN = BN, STAGES = Shape::STAGES, STAGE_BYTES = Shape::STAGE_BYTES;
+    constexpr int TBN = BN, MAXST = Shape::MAXST;
     constexpr int TILE_B = Shape::TILE_B, EPI_WARPS = Shape::EPI_WARPS, EPI_COLS = Shape::EPI_COLS;
     constexpr int NBUF = Shape::NBUF, TMEM_COLS = NBUF * TBN;
     constexpr uint32_t IDESC = Shape::IDESC;
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                ~uintptr_t(1023));
     uint8_t* tiles = smem;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
-    // bars: full[STAGES], empty[STAGES], tfull[NBUF], tempty[NBUF], drain
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 2 * NBUF + 1);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + PIPE_BYTES);
+    // bars: full[MAXST], empty[MAXST], tfull[NBUF], tempty[NBUF], drain
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * MAXST + 2 * NBUF + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-    uint32_t* range_s = tmem_slot + 2;  // four words
+    uint32_t* range_s = tmem_slot + 2;  // six words
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const uint32_t bar_full = smem_u32(bars);
-    const uint32_t bar_empty = smem_u32(bars + STAGES);
-    const uint32_t bar_tfull = smem_u32(bars + 2 * STAGES);
-    const uint32_t bar_tempty = smem_u32(bars + 2 * STAGES + NBUF);
-    const uint32_t bar_drain = smem_u32(bars + 2 * STAGES + 2 * NBUF);
+    const uint32_t bar_empty = smem_u32(bars + MAXST);
+    const uint32_t bar_tfull = smem_u32(bars + 2 * MAXST);
+    const uint32_t bar_tempty = smem_u32(bars + 2 * MAXST + NBUF);
+    const uint32_t bar_drain = smem_u32(bars + 2 * MAXST + 2 * NBUF);
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
+        for (int s = 0; s < MAXST; ++s) {
             mbar_init(bar_full + 8 * s, 1);
             mbar_init(bar_empty + 8 * s, 1);
         }
@@ -478,12 +488,12 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
         mbar_init(bar_drain, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < 6; ++i)
             range_s[i] = range ? *reinterpret_cast<volatile uint32_t*>(range + i) : 255u;
         if (range && reset_range) {
             __threadfence();
-            if (atomicAdd(range + 4, 1u) == gridDim.x - 1) {
-                for (int i = 0; i < 5; ++i) range[i] = 0;
+            if (atomicAdd(range + 6, 1u) == gridDim.x - 1) {
+                for (int i = 0; i < 7; ++i) range[i] = 0;
             }
         }
     }
@@ -499,33 +509,39 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
     const int num_tiles = src.count();
+    // Stage layout [A hi][A lo][B hi][B lo], the lo tiles only for operands
+    // that have non-zero lo parts; as many stages as the ring holds.
+    const bool use_alo = range_s[2] != 0u, use_blo = range_s[5] != 0u;
+    const uint32_t o_bhi = TILE_A * (use_alo ? 2 : 1), o_blo = o_bhi + TILE_B;
+    const uint32_t stage_bytes = o_bhi + TILE_B * (use_blo ? 2 : 1);
+    const uint32_t nst = min((uint32_t)MAXST, (uint32_t)PIPE_BYTES / stage_bytes);
 
     if (warp == 0) {
         // ---------------- TMA producer ----------------
         if (lane == 0) {
-            uint32_t it = 0;
+            uint32_t it = 0, s = 0, ph = 0;   // stages issued; stage and its phase
             bool ok = true;
             for (int tile = blockIdx.x; tile < num_tiles && ok; tile += gridDim.x) {
                 const TileInfo ti = src.get(tile);
                 const int ksteps = ti.Kp / SK;
                 for (int ks = 0; ks < ksteps; ++ks, ++it) {
-                    const uint32_t s = it % STAGES;
-                    const uint32_t ph = (it / STAGES) & 1u;
                     if (!mbar_wait(bar_empty + 8 * s, ph ^ 1u, abort_flag, status, wcfg.limit_ns)) { ok = false; break; }
-                    if ((int)it == wcfg.withhold) continue;  // wait self-test: this stage never fills
-                    const uint32_t base = smem_u32(tiles + s * STAGE_BYTES);
-                    mbar_arrive_expect_tx(bar_full + 8 * s, STAGE_BYTES);
-                    tma_load_2d(base, ti.map[0], ks * SK, ti.a_r0, bar_full + 8 * s);
-                    tma_load_2d(base + TILE_A, ti.map[1], ks * SK, ti.a_r0, bar_full + 8 * s);
-                    tma_load_2d(base + 2 * TILE_A, ti.map[2], ks * SK, ti.b_r0, bar_full + 8 * s);
-                    tma_load_2d(base + 2 * TILE_A + TILE_B, ti.map[3], ks * SK, ti.b_r0,
-                                bar_full + 8 * s);
+                    if ((int)it != wcfg.withhold) {   // wait self-test: the withheld stage never fills
+                        const uint32_t base = smem_u32(tiles + s * stage_bytes);
+                        const uint32_t fb = bar_full + 8 * s;
+                        mbar_arrive_expect_tx(fb, stage_bytes);
+                        tma_load_2d(base, ti.map[0], ks * SK, ti.a_r0, fb);
+                        if (use_alo) tma_load_2d(base + TILE_A, ti.map[1], ks * SK, ti.a_r0, fb);
+                        tma_load_2d(base + o_bhi, ti.map[2], ks * SK, ti.b_r0, fb);
+                        if (use_blo) tma_load_2d(base + o_blo, ti.map[3], ks * SK, ti.b_r0, fb);
+                    }
+                    if (++s == nst) { s = 0; ph ^= 1u; }
                 }
             }
             if (!ok) {
                 // drain: every issued stage completes (or the drain wait expires)
-                for (uint32_t j = (it >= STAGES ? it - STAGES : 0); j < it; ++j)
-                    mbar_drain(bar_full + 8 * (j % STAGES), (j / STAGES) & 1u, wcfg.limit_ns);
+                for (uint32_t j = (it >= nst ? it - nst : 0); j < it; ++j)
+                    mbar_drain(bar_full + 8 * (j % nst), (j / nst) & 1u, wcfg.limit_ns);
             }
         }
     } else if (warp == 1) {
@@ -537,8 +553,8 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
         // memory is below 256 KiB).
         if (lane == 0) {
             const uint64_t dbase = smem_desc_sw128(smem_u32(tiles));
-            constexpr uint64_t ALO = TILE_A >> 4, BHI = (2 * TILE_A) >> 4;
-            constexpr uint64_t BLO = (2 * TILE_A + TILE_B) >> 4, SSTEP = STAGE_BYTES >> 4;
+            constexpr uint64_t ALO = TILE_A >> 4;
+            const uint64_t BHI = o_bhi >> 4, BLO = o_blo >> 4, SSTEP = stage_bytes >> 4;
             uint32_t s = 0, sph = 0;         // stage and its phase
             uint32_t buf = 0, bph = 0;       // TMEM chunk buffer and its phase
             bool ok = true;
@@ -562,8 +578,8 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                         const uint64_t ahi = sd + 2 * j, alo = sd + ALO + 2 * j;
                         const uint64_t bhi = sd + BHI + 2 * j, blo = sd + BLO + 2 * j;
                         umma_f16<IDESC>(d, ahi, bhi, pos > 0 ? 1u : 0u);
-                        umma_f16<IDESC>(d, ahi, blo, 1u);
-                        umma_f16<IDESC>(d, alo, bhi, 1u);
+                        if (use_blo) umma_f16<IDESC>(d, ahi, blo, 1u);
+                        if (use_alo) umma_f16<IDESC>(d, alo, bhi, 1u);
                         if (++pos == chunk16 || (last_stage && j == SK / 16 - 1)) {
                             umma_commit(bar_tfull + 8 * buf);
                             pos = 0;
@@ -572,7 +588,7 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                     }
                     if (!ok) break;
                     umma_commit(bar_empty + 8 * s);  // stage's smem free once its MMAs finish
-                    if (++s == STAGES) { s = 0; sph ^= 1u; }
+                    if (++s == nst) { s = 0; sph ^= 1u; }
                 }
             }
             // all issued MMAs complete before the TMEM is released
@@ -587,9 +603,7 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
         const uint32_t lane_base = tmem_base + ((uint32_t)(quarter * 32) << 16) + slice * EPI_COLS;
         uint32_t cg = 0;
         bool ok = true;
-        uint32_t rng[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) rng[i] = range_s[i];
+        const uint32_t rng[4] = {range_s[0], range_s[1], range_s[3], range_s[4]};
         // every lane waits; the warp goes on only when all lanes saw the phase
         // complete, reconverged for the .sync.aligned TMEM loads
         auto wait_full = [&](uint32_t g) -> bool {
@@ -819,10 +833,11 @@ split_grouped_kernel(const GroupHeader* __restrict__ h) {
         ExpRange& dst = r.operand ? erb : era;
         dst.emax = max(dst.emax, cur.emax);
         dst.emin_c = max(dst.emin_c, cur.emin_c);
+        dst.lo |= cur.lo;
     }
     uint32_t* range = const_cast<uint32_t*>(h->range);
     range_flush(range, era);
-    range_flush(range + 2, erb);
+    range_flush(range + 3, erb);
 }
 
 // ---- host side ---------------------------------------------------------------
@@ -923,7 +938,7 @@ int launch_gemm_tc_cfg(const float* A, int64_t lda, int64_t sa, int ta, const fl
     if (rc) return rc;
     split_bf16_kernel<<<dim3(w.Kp / 64, w.Np / 32, gz), sb256, 0, st>>>(B, ldb, sb, tb ? 1 : 0, N, K,
                                                                         w.Np, w.Kp, batch, bhi, blo,
-                                                                        range + 2);
+                                                                        range + 3);
     if ((rc = check_launch("split_bf16_kernel(B)"))) return rc;
     return launch_tc_presplit_cfg(ws, w, D, ldd, sd, M, N, mbits, alpha, chunk, 0, 0, stream, acc_fmt,
                                   wait);

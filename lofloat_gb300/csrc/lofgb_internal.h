@@ -110,10 +110,12 @@ int check_gemm_args(const void* A, int64_t lda, int ta, const void* B, int64_t l
 // (Mp, Np multiples of 128, Kp of 64), each 1024-byte aligned.
 // A strided batch of GEMMs stacks `batch` such splits (A rows b*Mp.., B rows
 // b*Np..) in each operand region.
-// Four words after the status word hold the exponent ranges of A and B
-// (tc_split.cuh ExpRange: largest field, 255 - smallest non-zero field),
-// which the split kernels publish and the epilogue reads to pick its fold;
-// the host clears WS_HEADER_CLEAR bytes from the status word before a launch.
+// Six words after the status word hold the exponent ranges and lo flags of
+// A (words 0-2) and B (words 3-5) (tc_split.cuh ExpRange: largest field,
+// 255 - smallest non-zero field, any non-zero lo part), which the split
+// kernels publish and the GEMM reads to pick its fold and its MMAs per k
+// step; the host clears WS_HEADER_CLEAR bytes from the status word before a
+// launch.
 struct WsLayout {
     size_t status, range, ahi, alo, bhi, blo, total;
     int Mp, Np, Kp, batch;

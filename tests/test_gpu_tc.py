@@ -157,6 +157,34 @@ def test_config3_error_vs_fp64():
     assert rel_tc.mean().item() < 2e-2
 
 
+@pytest.mark.parametrize("extra", ["none", "a", "b", "ab"])
+def test_lo_tiles_left_out_bit_identical(extra):
+    """Operands exact in BF16 have all-zero lo parts, and the GEMM then
+    neither loads their lo tiles nor issues their MMAs (one MMA per k step
+    instead of three, a deeper stage ring). One extra row of A (column of B)
+    holding a value that BF16 does not hold turns that operand's lo MMAs back
+    on; the outputs of every other row and column must not change by a bit,
+    since the MMAs left out add only zero products."""
+    g = torch.Generator(device="cuda").manual_seed(71)
+    M, N, K = 300, 260, 1000
+    A = torch.randn(M + 1, K, generator=g, device="cuda").bfloat16().float()
+    B = torch.randn(K, N + 1, generator=g, device="cuda").bfloat16().float()
+    base = lg.gemm(A[:M].contiguous(), B[:, :N].contiguous(), 10, variant="tc", chunk=32)
+    _status_ok()
+    A2, B2 = A.clone(), B.clone()
+    if "a" in extra:
+        A2[M, 7] = 1.0 + 2.0**-12
+    if "b" in extra:
+        B2[11, N] = -3.0 - 2.0**-11
+    full = lg.gemm(A2, B2, 10, variant="tc", chunk=32)
+    _status_ok()
+    assert torch.equal(full[:M, :N], base)
+    # the extra row / column itself against the CPU chunked model
+    Ah, Bh, Dh = from_gpu(A2), from_gpu(B2), from_gpu(full)
+    want = O.gemm_chunked(Ah[M:], Bh, 10, 32)
+    assert np.all(_err_units(Dh[M:], want, Ah[M:], Bh, 10) <= 4.0)
+
+
 def test_workspace_errors():
     A = torch.randn(64, 64, device="cuda")
     L = lg._native.lib()
@@ -168,16 +196,20 @@ def test_workspace_errors():
     assert st == -9
 
 
-def test_bounded_wait_runs_out_and_the_next_launch_is_clean():
+@pytest.mark.parametrize("exact", [False, True])
+def test_bounded_wait_runs_out_and_the_next_launch_is_clean(exact):
     """The wait self-test: every CTA's first pipeline stage is withheld (no
     copy issued, no fault), so the MMA warp's 1 ms wait runs out; the kernel
     must record LOFGB_ERR_TIMEOUT, drain, free its tensor memory and return.
     The next ordinary launch on the same stream then gives the same bits as
-    before and a clean status."""
+    before and a clean status. Operands with and without lo parts (three
+    stages of four tiles, six stages of two)."""
     rng = np.random.default_rng(9)
     M, N, K = 256, 384, 512
     A = to_gpu(rng.standard_normal((M, K)).astype(np.float32))
     B = to_gpu(rng.standard_normal((K, N)).astype(np.float32))
+    if exact:
+        A, B = A.bfloat16().float(), B.bfloat16().float()
     before = lg.gemm(A, B, 10, variant="tc", chunk=32)
     _status_ok()
     L = lg._native.lib()
