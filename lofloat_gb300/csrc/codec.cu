@@ -965,7 +965,13 @@ int launch_decode_n(const uint8_t* src, float* dst, int64_t count, int reverse, 
 // (the infinity / NaN checks only in warps that hold one), and the scale's
 // code, one byte per block. Values past the end take code bits 0, the
 // codec's zero padding.
-template <int N, bool UNI>
+// DIRECT (RNE into a saturating element format, whose rounding returns an
+// overflowing input unchanged): the code of the rounded quotient equals the
+// codec's RNE code of the quotient itself for every finite quotient (the
+// codec rounds onto the same grid and saturates what overflows), so warps
+// without an infinity or NaN encode the quotients directly and only the
+// others round first (a NaN quotient must become the canonical NaN).
+template <int N, bool UNI, bool DIRECT>
 __global__ void __launch_bounds__(256)
 mx_encode_kernel(const float* __restrict__ in, uint8_t* __restrict__ codes,
                  uint8_t* __restrict__ scales, int64_t n, RoundPlan pe, RoundPlan ps,
@@ -978,6 +984,7 @@ mx_encode_kernel(const float* __restrict__ in, uint8_t* __restrict__ codes,
     const int64_t warp = ((int64_t)blockIdx.x * 256 + threadIdx.x) >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * 8;
     const int64_t steps = (n + 127) / 128;
+    const bool codes_aligned = (reinterpret_cast<uintptr_t>(codes) & 3) == 0;
     for (int64_t s0 = warp * U; s0 < steps; s0 += nwarps * U) {
         float x[U][4];
 #pragma unroll
@@ -1018,42 +1025,91 @@ mx_encode_kernel(const float* __restrict__ in, uint8_t* __restrict__ codes,
             const int64_t e = (s0 + u) * 128 + lane * 4;
             if ((s0 + u) * 128 >= n) break;  // warp-uniform
             const BlockScale b = scale_from_bits(__shfl_sync(0xFFFFFFFFu, sbj, u * 4 + (lane >> 3)));
-            uint32_t w[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                w[q] = __float_as_uint(b.pow2 ? __fmul_rn(x[u][q], b.inv) : __fdiv_rn(x[u][q], b.scale));
-            if constexpr (UNI) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) w[q] = vr_uni_f32<LOFGB_RNE, 1>(w[q], pe);
-            } else {
-                uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
-                if (mode_is_stochastic(pe.mode)) rng_elem4(seed, offset + (uint64_t)e, pe.rng_lg, r);
-                vr_format_f32x4<-1, false>(w, pe, r);
-            }
-            float qv[4];
-            bool sp = false;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                qv[q] = b.pos ? __uint_as_float(w[q]) : 0.0f;
-                sp |= (__float_as_uint(qv[q]) & 0x7FFFFFFFu) >= 0x7F800000u;
-            }
             uint32_t c[4];
-            if (!ea.enc_fast) {
+            if constexpr (DIRECT) {
+                uint32_t w[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) c[q] = codec_encode<LOFGB_RNE>(qv[q], ea, 0ull);
-            } else if (__any_sync(0xFFFFFFFFu, sp)) {
+                for (int q = 0; q < 4; ++q)
+                    w[q] = __float_as_uint(b.pow2 ? __fmul_rn(x[u][q], b.inv) : __fdiv_rn(x[u][q], b.scale));
+                float qv[4];
+                bool sp = false;
 #pragma unroll
-                for (int q = 0; q < 4; ++q) c[q] = encode_fast_any<true>(qv[q], ea);
+                for (int q = 0; q < 4; ++q) {
+                    qv[q] = b.pos ? __uint_as_float(w[q]) : 0.0f;
+                    sp |= (__float_as_uint(qv[q]) & 0x7FFFFFFFu) >= 0x7F800000u;
+                }
+                const bool any_sp = __any_sync(0xFFFFFFFFu, sp);
+                if (any_sp) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        qv[q] = b.pos ? __uint_as_float(vr_uni_f32<LOFGB_RNE, 1>(w[q], pe)) : 0.0f;
+                }
+                if (!ea.enc_fast) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) c[q] = codec_encode<LOFGB_RNE>(qv[q], ea, 0ull);
+                } else if (any_sp) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) c[q] = encode_fast_any<true>(qv[q], ea);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) c[q] = encode_fast_any<false>(qv[q], ea);
+                }
+            } else {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    w[q] = __float_as_uint(b.pow2 ? __fmul_rn(x[u][q], b.inv) : __fdiv_rn(x[u][q], b.scale));
+                float qv[4];
+                bool sp = false;
+                if constexpr (UNI) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) w[q] = vr_uni_f32<LOFGB_RNE, 1>(w[q], pe);
+                } else {
+                    uint64_t r[4] = {0ull, 0ull, 0ull, 0ull};
+                    if (mode_is_stochastic(pe.mode)) rng_elem4(seed, offset + (uint64_t)e, pe.rng_lg, r);
+                    vr_format_f32x4<-1, false>(w, pe, r);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    qv[q] = b.pos ? __uint_as_float(w[q]) : 0.0f;
+                    sp |= (__float_as_uint(qv[q]) & 0x7FFFFFFFu) >= 0x7F800000u;
+                }
+                if (!ea.enc_fast) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) c[q] = codec_encode<LOFGB_RNE>(qv[q], ea, 0ull);
+                } else if (__any_sync(0xFFFFFFFFu, sp)) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) c[q] = encode_fast_any<true>(qv[q], ea);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) c[q] = encode_fast_any<false>(qv[q], ea);
+                }
+            }
+            // values of this step in the tensor: 128 except in the last step
+            const int rem = (int)min((int64_t)128, n - (s0 + u) * 128);
+            constexpr uint32_t CM = (1u << N) - 1u;
+            uint32_t packed = 0;
+            if (rem == 128) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) packed |= (c[q] & CM) << (q * N);
             } else {
 #pragma unroll
-                for (int q = 0; q < 4; ++q) c[q] = encode_fast_any<false>(qv[q], ea);
+                for (int q = 0; q < 4; ++q) packed |= (lane * 4 + q < rem ? (c[q] & CM) : 0u) << (q * N);
             }
-            uint32_t packed = 0;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) packed |= (e + q < n ? (c[q] & ((1u << N) - 1u)) : 0u) << (q * N);
             constexpr int BYTES = N / 2;  // 4 codes of N bits
             const int64_t off = e / 4 * BYTES;
-            if (off < code_bytes) {
+            if (rem == 128 && codes_aligned) {
+                // a whole step lies inside the stream: plain stores
+                uint8_t* dst = codes + off;
+                if constexpr (N == 8) {
+                    *reinterpret_cast<uint32_t*>(dst) = packed;
+                } else if constexpr (N == 4) {
+                    *reinterpret_cast<uint16_t*>(dst) = (uint16_t)packed;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < BYTES; ++k) dst[k] = (uint8_t)(packed >> (8 * k));
+                }
+            } else if (off < code_bytes) {
                 uint8_t* dst = codes + off;
                 const bool whole = off + BYTES <= code_bytes;
                 if (N == 8 && whole && (reinterpret_cast<uintptr_t>(dst) & 3) == 0) {
@@ -1070,22 +1126,39 @@ mx_encode_kernel(const float* __restrict__ in, uint8_t* __restrict__ codes,
     }
 }
 
+// One co-resident wave of mx_encode_kernel CTAs (fewer for small inputs):
+// the grid-stride loop then has no second, partial wave.
+template <int N, bool UNI, bool DIRECT>
+int mx_encode_grid(int64_t n) {
+    static const int per_sm = [] {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, mx_encode_kernel<N, UNI, DIRECT>, 256, 0) !=
+                cudaSuccess || b < 1)
+            b = 1;
+        return b;
+    }();
+    const int64_t steps = (n + 127) / 128;
+    const int64_t need = (steps + 31) / 32;   // 8 warps x 4 steps per CTA iteration
+    const int64_t maxg = (int64_t)sm_count() * per_sm;
+    return (int)(need < 1 ? 1 : (need < maxg ? need : maxg));
+}
+
 template <int N>
 int launch_mx_encode_n(const float* in, uint8_t* codes, uint8_t* scales, int64_t n,
                        const RoundPlan& pe, const RoundPlan& ps, float inv_pmn, const CodecArg& ea,
                        const CodecArg& sa, uint64_t seed, uint64_t offset, cudaStream_t st) {
-    const int64_t steps = (n + 127) / 128;
-    const int64_t need = (steps + 31) / 32;   // 8 warps x 4 steps per CTA iteration
-    const int64_t maxg = (int64_t)sm_count() * 8;
-    const int grid = (int)(need < 1 ? 1 : (need < maxg ? need : maxg));
     const int vec = (reinterpret_cast<uintptr_t>(in) & 15) == 0;
     const int64_t cb = packed_bytes(N, n);
-    if (pe.mode == LOFGB_RNE && pe.uni == 1)
-        launch_pdl(mx_encode_kernel<N, true>, grid, 256, 0, st, in, codes, scales, n, pe, ps, inv_pmn,
-                   ea, sa, seed, offset, vec, cb);
+    const bool uni = pe.mode == LOFGB_RNE && pe.uni == 1;
+    if (uni && pe.sat_and == 0xFFFFFFFFu && pe.sat_or == 0u)
+        launch_pdl(mx_encode_kernel<N, true, true>, mx_encode_grid<N, true, true>(n), 256, 0, st, in,
+                   codes, scales, n, pe, ps, inv_pmn, ea, sa, seed, offset, vec, cb);
+    else if (uni)
+        launch_pdl(mx_encode_kernel<N, true, false>, mx_encode_grid<N, true, false>(n), 256, 0, st, in,
+                   codes, scales, n, pe, ps, inv_pmn, ea, sa, seed, offset, vec, cb);
     else
-        launch_pdl(mx_encode_kernel<N, false>, grid, 256, 0, st, in, codes, scales, n, pe, ps, inv_pmn,
-                   ea, sa, seed, offset, vec, cb);
+        launch_pdl(mx_encode_kernel<N, false, false>, mx_encode_grid<N, false, false>(n), 256, 0, st,
+                   in, codes, scales, n, pe, ps, inv_pmn, ea, sa, seed, offset, vec, cb);
     return check_launch("mx_encode_kernel");
 }
 

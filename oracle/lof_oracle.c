@@ -607,8 +607,14 @@ int orc_round_mantissa_f16(const uint16_t* in, uint16_t* out, int64_t n, int mbi
 static float mx_block(const float* in, int64_t b0, int64_t cnt, const fconst_t* ce,
                       const fconst_t* cs, float pmn, float inv, int mode, int scale_mode, int len,
                       int lg, uint64_t seed, uint64_t offset, int scale_formula, float* q) {
+    /* amax ignores NaNs of both kinds, as the reference's device fmaxf does
+       (src/mx_round.cuh:101-106); a host fmaxf may return NaN for a
+       signaling NaN operand */
     float amax = 0.0f;
-    for (int64_t i = 0; i < cnt; ++i) amax = fmaxf(amax, fabsf(in[b0 + i]));
+    for (int64_t i = 0; i < cnt; ++i) {
+        const float a = fabsf(in[b0 + i]);
+        if (a > amax) amax = a;
+    }
     const float sin = scale_formula ? amax / pmn : amax * inv;
     uint64_t rs = orc_rng(seed ^ ORC_SCALE_SALT, offset + (uint64_t)b0);
     const float scale =

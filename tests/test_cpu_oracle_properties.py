@@ -451,3 +451,29 @@ def test_mx_encode_composes_mx_round_and_codec():
     diff = back != ref
     assert diff.mean() < 0.08
     assert np.array_equal(np.abs(back[diff]), (top * np.repeat(sc, 32)[: x.size])[diff])
+
+
+@pytest.mark.parametrize("k,p", [(8, 4), (8, 3), (6, 3), (6, 2), (4, 2)])
+@pytest.mark.parametrize("signed", [True, False])
+def test_codec_rne_of_rounded_equals_codec_rne_saturating(k, p, signed):
+    """For a saturating format under RNE, the codec's code of virtual_round(w)
+    equals the codec's code of w itself for every finite w (same grid; the
+    rounding returns an overflowing input unchanged and the codec saturates
+    it). The MX storage encode relies on this to encode MX quotients without
+    rounding them first; NaN quotients, where it fails for unsigned formats
+    (the sign decides the code), take the rounding path."""
+    rng = np.random.default_rng(k * 10 + p + signed)
+    ef = O.codec_p3109(k, p, signed=signed)
+    n = 1 << 18
+    e = rng.integers(127 - ef.fmt.bias - 30, 127 + (1 << (k - p)) - ef.fmt.bias + 4, n)
+    sh = rng.integers(0, 24, n)
+    m = rng.integers(0, 1 << 23, n)
+    kind = rng.integers(0, 4, n)
+    low = np.where(kind == 0, 0, np.where(kind == 1, 1 << np.maximum(sh - 1, 0),
+                                          np.where(kind == 2, (1 << sh) - 1, m & ((1 << sh) - 1))))
+    mm = (((m >> sh) << sh) | low) & 0x7FFFFF
+    s = rng.integers(0, 2, n).astype(np.uint32) << 31
+    w = (s | (e.astype(np.uint32) << 23) | mm.astype(np.uint32)).view(np.float32)
+    w = np.concatenate([w, np.array([0.0, -0.0, np.inf, -np.inf], np.float32)])
+    for sat in (0, 1, 2):
+        assert np.array_equal(O.encode(w, ef, 0, sat), O.encode(O.round(w, ef.fmt, 0), ef, 0, sat))

@@ -60,6 +60,34 @@ def test_against_oracle(name, ef, n, sat):
     assert np.array_equal(got_s, want_s)
 
 
+SPECIAL_FORMATS = FORMATS + [("e4m3_unsigned", O.codec_p3109(8, 4, signed=False)),
+                             ("fp6_unsigned", O.codec_p3109(6, 3, signed=False)),
+                             ("e4m3_nonsat", O.codec_p3109(8, 4, saturating=False)),
+                             ("e5m2_nonsat", O.codec_p3109(8, 3, saturating=False))]
+
+
+@pytest.mark.parametrize("name,ef", SPECIAL_FORMATS)
+@pytest.mark.parametrize("sat", [0, 1, 2])
+def test_specials_signs_and_formats(name, ef, sat):
+    """Infinities, NaNs of both signs and with payloads, -0 and overflowing
+    values inside otherwise ordinary blocks; signed, unsigned and
+    non-saturating element formats, every saturation mode. Saturating
+    formats under RNE encode quotients without rounding them first except in
+    warps that hold an infinity or NaN; the others round first."""
+    rng = np.random.default_rng(len(name) * 7 + sat)
+    n = 32 * 512 + 19
+    x = (rng.standard_normal(n) * np.exp2(rng.integers(-10, 11, n))).astype(np.float32)
+    specials = np.array([0x7F800000, 0xFF800000, 0x7FC00000, 0xFFC00000, 0x7F800001, 0xFFFFFFFF,
+                         0x80000000, 0x7F7FFFFF, 0xFF7FFFFF], np.uint32).view(np.float32)
+    idx = rng.choice(n, 60, replace=False)
+    x[idx] = specials[rng.integers(0, specials.size, idx.size)]
+    x[-7:] = -x[-7:]
+    got_c, got_s = _gpu_mx_encode(x, ef, sat=sat)
+    want_c, want_s = O.mx_encode(x, 32, ef, E8M0_O, sat=sat)
+    assert np.array_equal(got_s, want_s)
+    assert np.array_equal(got_c, want_c), np.count_nonzero(got_c != want_c)
+
+
 @pytest.mark.parametrize("skew", [1, 2, 3])
 @pytest.mark.parametrize("mode,ln", [(0, 0), (3, 8), (1, 0)])
 def test_modes_and_misaligned_buffers(skew, mode, ln):
