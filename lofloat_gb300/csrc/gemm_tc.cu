@@ -45,6 +45,7 @@
 #include <cudaTypedefs.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -76,7 +77,7 @@ struct TileShape {
     static constexpr int STAGE_BYTES = 2 * TILE_A + 2 * TILE_B;
     static constexpr int STAGES = PIPE_BYTES / STAGE_BYTES;
     static constexpr int MAXST = PIPE_BYTES / (TILE_A + TILE_B);   // stages of hi tiles only
-    static constexpr int EPI_WARPS = BN == 128 ? 16 : 8;   // EPI_WARPS / 4 per TMEM lane quarter
+    static constexpr int EPI_WARPS = BN == 64 ? 8 : 16;    // EPI_WARPS / 4 per TMEM lane quarter
     static constexpr int EPI_COLS = BN * 4 / EPI_WARPS;    // accumulator columns per epilogue thread
     static constexpr int NBUF = 512 / BN;                  // TMEM chunk buffers (all 512 columns)
     // Instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
@@ -85,7 +86,7 @@ struct TileShape {
                                       ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TBM >> 4) << 24);
     static_assert(EPI_COLS == 64 || EPI_COLS == 32, "the epilogue folds 16-column pieces, 4 or 2 per chunk");
     static_assert((NBUF & (NBUF - 1)) == 0 && NBUF * BN == 512, "TMEM chunk buffers");
-    static_assert(STAGES * STAGE_BYTES <= PIPE_BYTES && STAGES >= 3, "stage ring");
+    static_assert(STAGES * STAGE_BYTES <= PIPE_BYTES && STAGES >= 2, "stage ring");
     static_assert(2 * MAXST + 2 * NBUF + 1 <= 56, "barrier area");
 };
 constexpr int NUM_THREADS = 32 * (2 + 16);     // launch size of every shape (idle warps exit)
@@ -105,6 +106,7 @@ struct TcParams {
     int64_t ldd;
     int M, N, Kp;          // Kp: padded K (multiple of SK)
     int tiles_m, tiles_n;
+    int tile_n;            // output columns per tile (128 or 256)
     int chunk16;           // chunk length in 16-k steps
     int ro;                // 23 - accum_mant_bits
     float alpha;
@@ -249,6 +251,29 @@ __device__ __forceinline__ void tmem_ld_wait16(uint32_t (&r)[16]) {
                  : "memory");
 }
 
+// 8-column forms of the two above, for the 64-column epilogue slices of the
+// 128 x 256 tile (64 accumulators plus two 8-register pieces per thread).
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait8(uint32_t (&r)[8]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                   "+r"(r[6]), "+r"(r[7])
+                 :
+                 : "memory");
+}
+template <int OFF, int N>
+__device__ __forceinline__ void pin8(float (&a)[N]) {
+    static_assert(OFF + 8 <= N, "pin8 range");
+    asm volatile(""
+                 : "+f"(a[OFF + 0]), "+f"(a[OFF + 1]), "+f"(a[OFF + 2]), "+f"(a[OFF + 3]),
+                   "+f"(a[OFF + 4]), "+f"(a[OFF + 5]), "+f"(a[OFF + 6]), "+f"(a[OFF + 7]));
+}
+
 // Scheduling pin for the pipelined epilogue: an empty asm that takes 16
 // accumulators as in/out operands. Placed after a TMEM load it keeps the fold
 // of those accumulators after the load is issued; placed before a TMEM wait it
@@ -362,7 +387,7 @@ struct SingleSrc {
         ti.M = prm.M;
         ti.N = prm.N;
         ti.m0 = (r / prm.tiles_n) * TBM;
-        ti.n0 = (r % prm.tiles_n) * TBN;
+        ti.n0 = (r % prm.tiles_n) * prm.tile_n;
         ti.a_r0 = b * prm.Mp + ti.m0;
         ti.b_r0 = b * prm.Np + ti.n0;
         ti.Kp = prm.Kp;
@@ -646,10 +671,67 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                         acc[off + i] = fold_fmt<ACCK>(acc[off + i], __uint_as_float(r[i]), *acc_plan);
                 }
             };
-            // EPI_COLS / 16 pieces of 16 columns per chunk, software-pipelined
-            // over two register sets: each piece loads while the previous one
-            // is folded, and piece 0 of chunk c+1 loads during the last piece
-            // of chunk c.
+            auto fold8 = [&](int off, const uint32_t (&r)[8]) {
+                if constexpr (ACCK == 0) {
+                    if (fast) {
+#pragma unroll
+                        for (int i = 0; i < 8; i += 2)
+                            fold2_fast(acc[off + i], acc[off + i + 1], __uint_as_float(r[i]),
+                                       __uint_as_float(r[i + 1]), sigma);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 8; ++i)
+                            acc[off + i] = fold(acc[off + i], __uint_as_float(r[i]), ro, sh, two, half_m1, mask);
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        acc[off + i] = fold_fmt<ACCK>(acc[off + i], __uint_as_float(r[i]), *acc_plan);
+                }
+            };
+            if constexpr (EPI_COLS == 64) {
+                // 64-column slices: eight pieces of 8 columns per chunk over
+                // two 8-register sets, each piece loading while the previous
+                // one is folded, piece 0 of chunk c+1 during piece 7 of chunk c
+                uint32_t qa[8], qb[8];
+                if (!wait_full(cg)) { ok = false; break; }
+                tmem_ld8(lane_base + (cg % NBUF) * TBN, qa);
+                tmem_ld_wait8(qa);
+                for (int c = 0; c < nchunks; ++c) {
+                    const uint32_t col = lane_base + (cg % NBUF) * TBN;
+#define LOFGB_EPI8(LD, DST, OFF, SRC)  \
+    tmem_ld8(col + (LD), DST);         \
+    pin8<OFF>(acc);                    \
+    fold8(OFF, SRC);                   \
+    pin8<OFF>(acc);                    \
+    tmem_ld_wait8(DST);
+                    LOFGB_EPI8(8, qb, 0, qa)
+                    LOFGB_EPI8(16, qa, 8, qb)
+                    LOFGB_EPI8(24, qb, 16, qa)
+                    LOFGB_EPI8(32, qa, 24, qb)
+                    LOFGB_EPI8(40, qb, 32, qa)
+                    LOFGB_EPI8(48, qa, 40, qb)
+                    LOFGB_EPI8(56, qb, 48, qa)
+#undef LOFGB_EPI8
+                    tc_fence_before();
+                    mbar_arrive(bar_tempty + 8 * (cg % NBUF));   // all of chunk c is in registers
+                    ++cg;
+                    const bool more = c + 1 < nchunks;
+                    if (more) {
+                        if (!wait_full(cg)) { ok = false; break; }
+                        tmem_ld8(lane_base + (cg % NBUF) * TBN, qa);
+                    }
+                    pin8<56>(acc);
+                    fold8(56, qb);
+                    pin8<56>(acc);
+                    if (more) tmem_ld_wait8(qa);
+                }
+            } else {
+            // EPI_COLS / 16 = 2 pieces of 16 columns per chunk, software-
+            // pipelined over two register sets: each piece loads while the
+            // previous one is folded, and piece 0 of chunk c+1 loads during
+            // the last piece of chunk c.
+            static_assert(EPI_COLS == 32, "32- or 64-column epilogue slices");
             uint32_t ra[16], rb[16];
             if (!wait_full(cg)) { ok = false; break; }
             tmem_ld16(lane_base + (cg % NBUF) * TBN, ra);
@@ -661,18 +743,6 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                 fold16(0, ra);
                 pin16<0>(acc);
                 tmem_ld_wait16(rb);
-                if constexpr (EPI_COLS == 64) {
-                    tmem_ld16(col + 32, ra);
-                    pin16<16>(acc);
-                    fold16(16, rb);
-                    pin16<16>(acc);
-                    tmem_ld_wait16(ra);
-                    tmem_ld16(col + 48, rb);
-                    pin16<32>(acc);
-                    fold16(32, ra);
-                    pin16<32>(acc);
-                    tmem_ld_wait16(rb);
-                }
                 tc_fence_before();
                 mbar_arrive(bar_tempty + 8 * (cg % NBUF));   // all of chunk c is in registers
                 ++cg;
@@ -681,10 +751,11 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
                     if (!wait_full(cg)) { ok = false; break; }
                     tmem_ld16(lane_base + (cg % NBUF) * TBN, ra);
                 }
-                pin16<EPI_COLS - 16>(acc);
-                fold16(EPI_COLS - 16, rb);
-                pin16<EPI_COLS - 16>(acc);
+                pin16<16>(acc);
+                fold16(16, rb);
+                pin16<16>(acc);
                 if (more) tmem_ld_wait16(ra);
+            }
             }
             if (!ok) break;
             const int row = ti.m0 + quarter * 32 + lane;
@@ -728,7 +799,7 @@ __device__ __forceinline__ void tc_body(const Src& src, int* status, uint8_t* sm
     }
 }
 
-template <int ACCK>
+template <int ACCK, int BN>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant__ CUtensorMap tm_alo,
                const __grid_constant__ CUtensorMap tm_bhi, const __grid_constant__ CUtensorMap tm_blo,
@@ -740,7 +811,7 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
     src.m[2] = &tm_bhi;
     src.m[3] = &tm_blo;
     src.prm = prm;
-    tc_body<ACCK, 128>(src, prm.status, smem_raw, prm.range, false, prm.wait, &prm.acc_plan);
+    tc_body<ACCK, BN>(src, prm.status, smem_raw, prm.range, false, prm.wait, &prm.acc_plan);
 }
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
@@ -970,12 +1041,30 @@ int launch_tc_presplit_cfg(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd
     auto* alo = reinterpret_cast<__nv_bfloat16*>(ws + w.alo);
     auto* bhi = reinterpret_cast<__nv_bfloat16*>(ws + w.bhi);
     auto* blo = reinterpret_cast<__nv_bfloat16*>(ws + w.blo);
+    // Output tile 128 x 256 (one MMA covers twice the columns, halving the
+    // MMA instructions per output) or 128 x 128, for the mantissa
+    // accumulator: the persistent grid takes ceil(tiles / SMs) tile times,
+    // and a wide tile measured about 1.1x the outputs per second of two
+    // narrow ones (4096^3: 183 vs 167 TFLOP/s per full wave), so the wide
+    // tile is taken only where its fewer, coarser waves still come out
+    // ahead (not at 4096^2: 4 wide waves against 7 narrow ones).
+    // LOFGB_TC_TILE_N=128|256 overrides the choice (tests, tuning).
+    const int64_t tiles_m = w.Mp / TBM;
+    const int64_t sms = sm_count();
+    const int64_t t128 = (int64_t)w.batch * tiles_m * (w.Np / 128);
+    const int64_t t256 = (int64_t)w.batch * tiles_m * ((w.Np + 255) / 256);
+    const int64_t waves128 = (t128 + sms - 1) / sms, waves256 = (t256 + sms - 1) / sms;
+    int tile_n = (!acc_fmt && waves256 * 20 < waves128 * 11) ? 256 : 128;
+    if (const char* ov = std::getenv("LOFGB_TC_TILE_N")) {
+        if (std::strcmp(ov, "128") == 0) tile_n = 128;
+        else if (std::strcmp(ov, "256") == 0 && !acc_fmt) tile_n = 256;
+    }
     int rc;
     CUtensorMap m_ahi, m_alo, m_bhi, m_blo;
     if ((rc = make_map(&m_ahi, ahi, w.batch * w.Mp, w.Kp))) return rc;
     if ((rc = make_map(&m_alo, alo, w.batch * w.Mp, w.Kp))) return rc;
-    if ((rc = make_map(&m_bhi, bhi, w.batch * w.Np, w.Kp))) return rc;
-    if ((rc = make_map(&m_blo, blo, w.batch * w.Np, w.Kp))) return rc;
+    if ((rc = make_map(&m_bhi, bhi, w.batch * w.Np, w.Kp, tile_n))) return rc;
+    if ((rc = make_map(&m_blo, blo, w.batch * w.Np, w.Kp, tile_n))) return rc;
 
     TcParams p;
     p.D = D;
@@ -983,8 +1072,9 @@ int launch_tc_presplit_cfg(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd
     p.M = M;
     p.N = N;
     p.Kp = w.Kp;
-    p.tiles_m = w.Mp / TBM;
-    p.tiles_n = w.Np / TBN;
+    p.tiles_m = (int)tiles_m;
+    p.tile_n = tile_n;
+    p.tiles_n = (w.Np + tile_n - 1) / tile_n;
     p.chunk16 = chunk / 16;
     p.ro = 23 - mbits;
     p.alpha = alpha;
@@ -1007,11 +1097,12 @@ int launch_tc_presplit_cfg(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd
 
     int dev = 0;
     cudaGetDevice(&dev);
-    static bool attr_set[3][64] = {};
-    const int ki = p.acc_kind == 0 ? 0 : p.acc_kind - 1;
+    static bool attr_set[4][64] = {};
+    const int ki = p.acc_kind == 0 ? (tile_n == 256 ? 3 : 0) : p.acc_kind - 1;
+    const void* fn = ki == 3 ? (const void*)gemm_tc_kernel<0, 256>
+                     : ki == 0 ? (const void*)gemm_tc_kernel<0, 128>
+                     : ki == 1 ? (const void*)gemm_tc_kernel<2, 128> : (const void*)gemm_tc_kernel<3, 128>;
     if (dev < 0 || dev >= 64 || !attr_set[ki][dev]) {
-        const void* fn = p.acc_kind == 0 ? (const void*)gemm_tc_kernel<0>
-                         : p.acc_kind == 2 ? (const void*)gemm_tc_kernel<2> : (const void*)gemm_tc_kernel<3>;
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
         if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
         if (dev >= 0 && dev < 64) attr_set[ki][dev] = true;
@@ -1019,12 +1110,14 @@ int launch_tc_presplit_cfg(uint8_t* ws, const WsLayout& w, float* D, int64_t ldd
     const int64_t tiles = (int64_t)p.batch * p.tiles_m * p.tiles_n;
     if (tiles >= ((int64_t)1 << 31)) return set_error(LOFGB_ERR_SIZE, "too many output tiles");
     const int grid = tiles < sm_count() ? (int)tiles : sm_count();
-    if (p.acc_kind == 0)
-        gemm_tc_kernel<0><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
-    else if (p.acc_kind == 2)
-        gemm_tc_kernel<2><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
+    if (ki == 3)
+        gemm_tc_kernel<0, 256><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
+    else if (ki == 0)
+        gemm_tc_kernel<0, 128><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
+    else if (ki == 1)
+        gemm_tc_kernel<2, 128><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
     else
-        gemm_tc_kernel<3><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
+        gemm_tc_kernel<3, 128><<<grid, NUM_THREADS, SMEM_BYTES, st>>>(m_ahi, m_alo, m_bhi, m_blo, p);
     return check_launch("gemm_tc_kernel");
 }
 }  // namespace

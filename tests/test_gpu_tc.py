@@ -185,6 +185,44 @@ def test_lo_tiles_left_out_bit_identical(extra):
     assert np.all(_err_units(Dh[M:], want, Ah[M:], Bh, 10) <= 4.0)
 
 
+@pytest.mark.parametrize("shape", [(256, 512, 256), (200, 300, 300), (129, 257, 33), (384, 640, 1000)])
+@pytest.mark.parametrize("chunk", [32, 64])
+def test_wide_tile(shape, chunk, monkeypatch):
+    """The 128 x 256 output tile (LOFGB_TC_TILE_N=256; the launch picks it for
+    large GEMMs): one MMA covers 256 columns and the epilogue folds 64-column
+    slices in 8-column pieces. Against the CPU chunked model with the usual
+    bound, and bit-identical to the 128 x 128 tile (every output sees the
+    same chunk sums)."""
+    M, N, K = shape
+    rng = np.random.default_rng(M * 3 + N + K + chunk)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((K, N)).astype(np.float32)
+    monkeypatch.setenv("LOFGB_TC_TILE_N", "256")
+    wide = lg.gemm(to_gpu(A), to_gpu(B), 10, variant="tc", chunk=chunk)
+    _status_ok()
+    monkeypatch.setenv("LOFGB_TC_TILE_N", "128")
+    narrow = lg.gemm(to_gpu(A), to_gpu(B), 10, variant="tc", chunk=chunk)
+    _status_ok()
+    got = from_gpu(wide)
+    d = _err_units(got, O.gemm_chunked(A, B, 10, chunk), A, B, 10)
+    assert np.all(d <= 4.0), d.max()
+    assert torch.equal(wide, narrow)
+
+
+def test_wide_tile_batched_and_exact(monkeypatch):
+    """Strided batch through the wide tile (a B box that runs past one batch
+    entry's rows reads the next entry's, for columns that are not stored)
+    and exactly representable inputs equal to the CUDA-core form."""
+    monkeypatch.setenv("LOFGB_TC_TILE_N", "256")
+    rng = np.random.default_rng(17)
+    A = rng.integers(-3, 4, (3, 130, 200)).astype(np.float32)
+    B = rng.integers(-3, 4, (3, 200, 300)).astype(np.float32)
+    tc = lg.gemm(to_gpu(A), to_gpu(B), 23, variant="tc", chunk=32)
+    _status_ok()
+    pl = lg.gemm(to_gpu(A), to_gpu(B), 23)
+    assert torch.equal(tc, pl)
+
+
 def test_workspace_errors():
     A = torch.randn(64, 64, device="cuda")
     L = lg._native.lib()
