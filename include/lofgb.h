@@ -169,9 +169,13 @@ int lofgb_mx_round_bf16(const uint16_t* in, float* out, int64_t n, int block_siz
  * variant LOFGB_GEMM_TC: tcgen05 tensor cores; each k-chunk of `chunk`
  * (multiple of 16) is summed in FP32 in TMEM and then rounded into the
  * emulated accumulator: acc = RNE_m(rto(acc + chunk_sum)). Operands are split
- * into BF16 hi+lo pairs (3 MMAs per k-step; the lo·lo term is dropped). Not
+ * into BF16 hi+lo pairs (3 MMAs per k-step; the lo·lo term is dropped; an
+ * operand whose values are all exact in BF16 skips its lo MMAs). Not
  * bit-exact; error is stated against lofgb_gemm_f64_ref. Needs `workspace` of
- * lofgb_gemm_tc_workspace_size(M,N,K) bytes (256-byte aligned). */
+ * lofgb_gemm_tc_workspace_size(M,N,K) bytes (256-byte aligned). The output
+ * tile is 128 x 128 or 128 x 256 by the launch's wave count (bit-identical
+ * results); the environment variable LOFGB_TC_TILE_N=128|256 overrides the
+ * choice for the mantissa accumulator. */
 enum lofgb_gemm_variant { LOFGB_GEMM_PLAIN = 0, LOFGB_GEMM_TC = 1 };
 
 int lofgb_gemm_f32(const float* A, int64_t lda, int trans_a, const float* B, int64_t ldb,
