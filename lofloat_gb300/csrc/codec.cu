@@ -26,6 +26,7 @@
 // HBM-bound: 4 + n/8 bytes per element either way.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "lof_round.cuh"
@@ -674,6 +675,44 @@ decode_chunk_kernel(const uint32_t* __restrict__ src, float4* __restrict__ dst, 
     }
 }
 
+// Direct-bits decode for widths N <= 7 that one float4 per lane can serve:
+// the four codes of values 4q..4q+3 are the 4N bits at bit 4Nq of the
+// stream, read from the two words that cover them (neighbouring lanes read
+// neighbouring words, mostly from L1), and the lane writes one float4, so a
+// warp's store is 512 contiguous bytes. REV (reversed groups) only where a
+// group is exactly four codes (N = 2, 6). nq: quads whose two-word window
+// lies inside the input; the rest of the values are decoded by one thread.
+template <int N, bool REV, bool FAST>
+__global__ void __launch_bounds__(256)
+decode_quad_kernel(const uint32_t* __restrict__ src, float4* __restrict__ dst, int64_t nq,
+                   int64_t count, int64_t in_bytes, CodecArg a) {
+    pdl_wait();
+    static_assert(N <= 7 && (!REV || Group<N>::GC == 4), "quad decode");
+    constexpr uint32_t CM = (1u << N) - 1u;
+    for (int64_t q = (int64_t)blockIdx.x * 256 + threadIdx.x; q < nq; q += (int64_t)gridDim.x * 256) {
+        const int64_t b = 4 * N * q;
+        const int64_t w0 = b >> 5;
+        const uint64_t win = ((uint64_t)__ldg(src + w0 + 1) << 32) | __ldg(src + w0);
+        const uint32_t bits = (uint32_t)(win >> (b & 31));
+        float y[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) y[REV ? 3 - k : k] = decode_one<FAST>((bits >> (N * k)) & CM, a);
+        __stcs(dst + q, make_float4(y[0], y[1], y[2], y[3]));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint8_t* s8 = reinterpret_cast<const uint8_t*>(src);
+        float* d = reinterpret_cast<float*>(dst);
+        for (int64_t i = nq * 4; i < count; ++i) {
+            const int64_t sl = REV ? (i & ~(int64_t)3) + (3 - (i & 3)) : i;   // stream slot of value i
+            const int64_t bit = sl * N;
+            uint32_t v = 0;
+            for (int k = 0; k < 2; ++k)
+                if ((bit >> 3) + k < in_bytes) v |= (uint32_t)s8[(bit >> 3) + k] << (8 * k);
+            d[i] = decode_one<FAST>((v >> (bit & 7)) & CM, a);
+        }
+    }
+}
+
 template <int N, bool REV, bool FAST>
 __global__ void __launch_bounds__(CT)
 decode_kernel(const uint32_t* __restrict__ src, float* __restrict__ dst, int64_t count,
@@ -919,6 +958,27 @@ int launch_decode_n(const uint8_t* src, float* dst, int64_t count, int reverse, 
         }
     } else {
         // direct-bits decode (formats FP32 holds exactly); others stay staged
+        if constexpr (N <= 7) {
+            if (a.dec_fast && (reinterpret_cast<uintptr_t>(dst) & 15) == 0 &&
+                (!reverse || Group<N>::GC == 4)) {
+                // quads whose two-word window [w0, w0 + 1] lies inside the input
+                const int64_t words = ib / 4;
+                const int64_t qlim = words >= 2 ? (8 * (words - 1) + N - 1) / N : 0;
+                const int64_t nq = std::min(count / 4, qlim);
+                const int64_t need = (nq + 255) / 256;
+                const int64_t maxg = (int64_t)sm_count() * 8;
+                const int gq = (int)(need < 1 ? 1 : (need < maxg ? need : maxg));
+                float4* d4 = reinterpret_cast<float4*>(dst);
+                const uint32_t* s32 = reinterpret_cast<const uint32_t*>(src);
+                if (reverse) {
+                    if constexpr (Group<N>::GC == 4)
+                        launch_pdl(decode_quad_kernel<N, true, true>, gq, 256, 0, st, s32, d4, nq, count, ib, a);
+                } else {
+                    launch_pdl(decode_quad_kernel<N, false, true>, gq, 256, 0, st, s32, d4, nq, count, ib, a);
+                }
+                return check_launch("decode_quad_kernel");
+            }
+        }
         if (a.dec_fast && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
             float4* d4 = reinterpret_cast<float4*>(dst);
             const uint32_t* s32 = reinterpret_cast<const uint32_t*>(src);

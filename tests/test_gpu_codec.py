@@ -163,13 +163,15 @@ def test_python_api_and_errors():
         lg.lof_encode(x.cpu(), e4m3)
 
 
-@pytest.mark.parametrize("bits", [4, 8, 16])
+@pytest.mark.parametrize("bits", [4, 8, 16, 6, 2, 3])
 def test_direct_path_and_unaligned_fallback(bits):
     """4-, 8- and 16-bit codes take the one-float4-per-thread kernels when the
-    buffers allow 16-byte loads; buffers that are only 4-byte aligned take the
-    staged kernels. Both write the oracle's bytes."""
+    buffers allow 16-byte loads (2- and 6-bit decodes too, reversed groups
+    included; 3-bit reversed groups span eight codes and take the chunk
+    decode); buffers that are only 4-byte aligned take the staged kernels.
+    Both write the oracle's bytes."""
     f = O.codec_p3109(bits, max(1, bits // 2))
-    n = 70_003
+    n = 70_003 if bits != 6 else 70_001
     x = _wide(n, bits)
     want = O.encode(x, f, reverse=1)
     nb = lg.packed_size(bits, n)
