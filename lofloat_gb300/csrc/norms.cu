@@ -329,24 +329,33 @@ __device__ __forceinline__ float normalise(float x, const ChanFactors& f, const 
 
 // Row path: CTAs stride over the n * c rows; per row the channel factors
 // once, then the row's values as 16-byte vectors (or scalars).
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, 6)
 bn_apply_rows_kernel(ApplyArgs a) {
     pdl_wait();
     const int64_t rows = a.n * a.c;
     for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
-        const ChanFactors f = chan_factors(a, row % a.c);
         const float* xr = a.x + row * a.inner;
         float* yr = a.y + row * a.inner;
         if (a.vec) {
             const int64_t nv = a.inner / 4;
             const float4* xv = reinterpret_cast<const float4*>(xr);
             float4* yv = reinterpret_cast<float4*>(yr);
-            for (int64_t i0 = threadIdx.x; i0 < nv; i0 += (int64_t)NT * UNR) {
-                float4 q[UNR];
+            // the row's first vectors are requested before the channel
+            // factors, so the two reads overlap
+            float4 q[UNR];
 #pragma unroll
-                for (int u = 0; u < UNR; ++u) {
-                    const int64_t i = i0 + (int64_t)u * NT;
-                    if (i < nv) q[u] = __ldcs(xv + i);
+            for (int u = 0; u < UNR; ++u) {
+                const int64_t i = threadIdx.x + (int64_t)u * NT;
+                if (i < nv) q[u] = __ldcs(xv + i);
+            }
+            const ChanFactors f = chan_factors(a, row % a.c);
+            for (int64_t i0 = threadIdx.x; i0 < nv; i0 += (int64_t)NT * UNR) {
+                if (i0 != threadIdx.x) {
+#pragma unroll
+                    for (int u = 0; u < UNR; ++u) {
+                        const int64_t i = i0 + (int64_t)u * NT;
+                        if (i < nv) q[u] = __ldcs(xv + i);
+                    }
                 }
 #pragma unroll
                 for (int u = 0; u < UNR; ++u) {
@@ -361,6 +370,7 @@ bn_apply_rows_kernel(ApplyArgs a) {
                 }
             }
         } else {
+            const ChanFactors f = chan_factors(a, row % a.c);
             for (int64_t i = threadIdx.x; i < a.inner; i += NT) yr[i] = normalise(xr[i], f, a);
         }
     }
