@@ -295,14 +295,15 @@ int lofgb_gemm_f64_ref(const float* A, int64_t lda, int trans_a, const float* B,
  *        `grid` CTAs, 2 = longest K first, dealt boustrophedon;
  *      tiles are 128 x 128, or 128 x 64 with LOFGB_GROUPED_TILE_N64 or-ed
  *      into `schedule` (twice the tiles: finer load balance over uneven
- *      GEMMs, more operand traffic per product);
+ *      GEMMs, more operand traffic per product), or 128 x 256 with
+ *      LOFGB_GROUPED_TILE_N256 (half the tiles, one MMA per 256 columns);
  *   2. the caller copies the table to device memory (256-byte aligned) and
  *      calls lofgb_gemm_grouped_launch(): one operand-split launch and one
  *      persistent tensor-core launch of `grid` CTAs (0 = one per SM).
  * Each task computes what lofgb_gemm_f32(..., LOFGB_RNE, ..., LOFGB_GEMM_TC,
  * chunk, ...) computes for it. The first 4 bytes of the workspace receive the
  * device status (0, or LOFGB_ERR_TIMEOUT). */
-enum { LOFGB_GROUPED_TILE_N64 = 16 };
+enum { LOFGB_GROUPED_TILE_N64 = 16, LOFGB_GROUPED_TILE_N256 = 32 };
 typedef struct lofgb_gemm_task {
     const float* A;
     int64_t lda;

@@ -10,7 +10,7 @@ over uneven GEMMs, more operand traffic per product) and the tile schedule —
 the order in which the persistent CTAs take the output tiles of all GEMMs —
 decide load balance when the GEMMs differ in size. ``GroupedGemm(...,
 schedule="auto")`` times every (shape, schedule) pair the library offers
-(shapes 128x128 and 128x64; task order, longest-K first dealt round-robin,
+(shapes 128x128, 128x64 and 128x256; task order, longest-K first dealt round-robin,
 longest-K first dealt boustrophedon) on the actual problem, keeps the
 fastest, and caches the choice in a JSON table keyed by the problem's shape
 signature (bucketed to powers of two), so later problems of the same shape
@@ -32,7 +32,7 @@ from ._native import LofgbGemmTask, check
 from .binding import _stream
 
 SCHEDULES = {"task": 0, "lpt": 1, "lpt_snake": 2}
-TILES = {"128x128": 0, "128x64": 16}   # LOFGB_GROUPED_TILE_N64 for the narrow tile
+TILES = {"128x128": 0, "128x64": 16, "128x256": 32}   # LOFGB_GROUPED_TILE_N64 / _N256
 CHOICES = [f"{t}/{s}" for t in TILES for s in SCHEDULES]
 
 

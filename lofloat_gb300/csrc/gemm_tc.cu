@@ -424,7 +424,7 @@ struct SplitRow {
     int32_t kmajor, rows, K, R, Kp, operand;  // operand: 0 = A, 1 = B
 };
 struct GroupHeader {   // at the start of the device table; offsets from its base
-    int32_t ntasks, ntiles, nsplit, tile_n;   // tile_n: 128 or 64 output columns per tile
+    int32_t ntasks, ntiles, nsplit, tile_n;   // tile_n: 64, 128 or 256 output columns per tile
     int64_t split_items;
     int64_t rows_off, tiles_off, splits_off;
     int* status;
@@ -814,15 +814,22 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant
     tc_body<ACCK, BN>(src, prm.status, smem_raw, prm.range, false, prm.wait, &prm.acc_plan);
 }
 
+// One body per tile width, each compiled as its own function so that its
+// registers are allocated for it alone (inlined together, the widest
+// shape's register pressure spilled the others).
+template <int BN>
+__device__ __noinline__ void grouped_body(const GroupHeader* h, uint8_t* smem_raw) {
+    GroupedSrc src{h};
+    tc_body<0, BN>(src, h->status, smem_raw, const_cast<uint32_t*>(h->range), true, WaitCfg{});
+}
+
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 gemm_tc_grouped_kernel(const GroupHeader* __restrict__ h) {
     extern __shared__ uint8_t smem_raw[];
-    GroupedSrc src{h};
     // the tile width the table was prepared for (uniform over the launch)
-    if (h->tile_n == 64)
-        tc_body<0, 64>(src, h->status, smem_raw, const_cast<uint32_t*>(h->range), true, WaitCfg{});
-    else
-        tc_body<0, 128>(src, h->status, smem_raw, const_cast<uint32_t*>(h->range), true, WaitCfg{});
+    if (h->tile_n == 64) grouped_body<64>(h, smem_raw);
+    else if (h->tile_n == 256) grouped_body<256>(h, smem_raw);
+    else grouped_body<128>(h, smem_raw);
 }
 
 // ---- operand split: FP32 -> K-major BF16 hi/lo, zero padded -----------------
@@ -1300,8 +1307,10 @@ int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* w
     if (ntasks <= 0) return set_error(LOFGB_ERR_SIZE, "need at least one task");
     if (!tasks || !table || !workspace || !num_tiles || !split_items)
         return set_error(LOFGB_ERR_NULL, "NULL tasks, workspace, table or output count");
-    const int tile_n = (schedule & LOFGB_GROUPED_TILE_N64) ? 64 : 128;
-    schedule &= ~LOFGB_GROUPED_TILE_N64;
+    if ((schedule & LOFGB_GROUPED_TILE_N64) && (schedule & LOFGB_GROUPED_TILE_N256))
+        return set_error(LOFGB_ERR_UNSUPPORTED, "one tile width per table");
+    const int tile_n = (schedule & LOFGB_GROUPED_TILE_N64) ? 64 : (schedule & LOFGB_GROUPED_TILE_N256) ? 256 : 128;
+    schedule &= ~(LOFGB_GROUPED_TILE_N64 | LOFGB_GROUPED_TILE_N256);
     if (schedule < 0 || schedule > 2) return set_error(LOFGB_ERR_UNSUPPORTED, "schedule %d", schedule);
     for (int i = 0; i < ntasks; ++i) {
         const int st = check_task(tasks[i], i);
@@ -1366,7 +1375,8 @@ int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* w
         const int nchunks = (g.Kp[i] / 16 + r.chunk16 - 1) / r.chunk16;
         const int64_t cost = 4 * (int64_t)nchunks + g.Kp[i] / SK;
         for (int mt = 0; mt < g.Mp[i] / TBM; ++mt)
-            for (int nt = 0; nt < g.Np[i] / tile_n; ++nt) cands.push_back({i, mt * TBM, nt * tile_n, cost});
+            for (int nt = 0; nt < (g.Np[i] + tile_n - 1) / tile_n; ++nt)
+                cands.push_back({i, mt * TBM, nt * tile_n, cost});
     }
     if (schedule >= 1)
         std::stable_sort(cands.begin(), cands.end(),

@@ -36,7 +36,8 @@ def _reference(t):
 
 
 @pytest.mark.parametrize("schedule", ["task", "lpt", "lpt_snake", "128x64/task", "128x64/lpt",
-                                      "128x64/lpt_snake"])
+                                      "128x64/lpt_snake", "128x256/task", "128x256/lpt",
+                                      "128x256/lpt_snake"])
 def test_grouped_matches_single(schedule):
     tasks = _tasks(10, 1)
     gg = lg.GroupedGemm(tasks, schedule=schedule)
@@ -48,7 +49,7 @@ def test_grouped_matches_single(schedule):
         assert torch.equal(t["D"], _reference(t)), i
 
 
-@pytest.mark.parametrize("schedule", ["lpt_snake", "128x64/lpt_snake"])
+@pytest.mark.parametrize("schedule", ["lpt_snake", "128x64/lpt_snake", "128x256/lpt_snake"])
 def test_grouped_ragged_and_graph(schedule):
     tasks = _tasks(7, 2, dims=(1, 300), ragged=True)
     gg = lg.GroupedGemm(tasks, schedule=schedule, grid=37)
