@@ -326,6 +326,13 @@ int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* w
                                size_t table_bytes, int64_t* num_tiles, int64_t* split_items);
 int lofgb_gemm_grouped_launch(const void* device_table, int64_t num_tiles, int64_t split_items,
                               int grid, void* stream);
+/* lofgb_gemm_grouped_launch for a table prepared with tile width `tile_n`
+ * (64, 128 or 256 output columns; the LOFGB_GROUPED_TILE_* flag given to
+ * prepare): launches the kernel compiled for that width alone. A table
+ * prepared for another width is refused on the device (status word
+ * LOFGB_ERR_UNSUPPORTED, nothing computed). */
+int lofgb_gemm_grouped_launch_w(const void* device_table, int64_t num_tiles, int64_t split_items,
+                                int grid, int tile_n, void* stream);
 
 /* ---- grouped rounding: many tensors, each with its own format, one launch --
  * Batched form of lofgb_round_f32 (the reference rounds one tensor per call,

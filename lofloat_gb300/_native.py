@@ -87,6 +87,7 @@ SIGNATURES = [
     ("lofgb_gemm_grouped_prepare", _i32, [C.POINTER(LofgbGemmTask), _i32, _vp, _sz, _i32, _i32, _vp,
                                           _sz, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("lofgb_gemm_grouped_launch", _i32, [_vp, _i64, _i64, _i32, _vp]),
+    ("lofgb_gemm_grouped_launch_w", _i32, [_vp, _i64, _i64, _i32, _i32, _vp]),
     ("lofgb_round_grouped_table_size", _sz, [_i32]),
     ("lofgb_round_grouped_prepare", _i32, [C.POINTER(LofgbRoundTask), _i32, _vp, _sz,
                                            C.POINTER(C.c_int64)]),

@@ -33,6 +33,7 @@ from .binding import _stream
 
 SCHEDULES = {"task": 0, "lpt": 1, "lpt_snake": 2}
 TILES = {"128x128": 0, "128x64": 16, "128x256": 32}   # LOFGB_GROUPED_TILE_N64 / _N256
+TILE_N = {"128x128": 128, "128x64": 64, "128x256": 256}
 CHOICES = [f"{t}/{s}" for t in TILES for s in SCHEDULES]
 
 
@@ -141,6 +142,7 @@ class GroupedGemm:
                                                C.byref(nt), C.byref(si)), "gemm_grouped_prepare")
         self.table = torch.from_numpy(host).to(self.device)
         self.num_tiles, self.split_items = int(nt.value), int(si.value)
+        self.tile_n = TILE_N[schedule.rpartition("/")[0] or "128x128"]
         self.graph = None
 
     def _tune(self, reps: int):
@@ -163,9 +165,9 @@ class GroupedGemm:
 
     def __call__(self):
         with torch.cuda.device(self.device):
-            check(_native.lib().lofgb_gemm_grouped_launch(self.table.data_ptr(), self.num_tiles,
-                                                          self.split_items, self.grid,
-                                                          _stream(self.table)), "gemm_grouped_launch")
+            check(_native.lib().lofgb_gemm_grouped_launch_w(self.table.data_ptr(), self.num_tiles,
+                                                            self.split_items, self.grid, self.tile_n,
+                                                            _stream(self.table)), "gemm_grouped_launch")
 
     def status(self) -> int:
         """Device status word (0, or LOFGB_ERR_TIMEOUT); synchronises."""

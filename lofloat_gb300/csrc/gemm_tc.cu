@@ -832,6 +832,28 @@ gemm_tc_grouped_kernel(const GroupHeader* __restrict__ h) {
     else grouped_body<128>(h, smem_raw);
 }
 
+// The same for a tile width the host names at launch; a table prepared for
+// another width is refused on the device (status LOFGB_ERR_UNSUPPORTED,
+// nothing computed). The 64- and 128-column bodies are inlined here (on the
+// config-5 mix 14.69 / 11.56 ms against 16.27 / 12.17 through the call);
+// the 256-column body measured faster through its own function (11.51
+// against 11.67 ms inlined) and is called.
+template <int BN>
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+gemm_tc_grouped_w_kernel(const GroupHeader* __restrict__ h) {
+    extern __shared__ uint8_t smem_raw[];
+    if (h->tile_n != BN) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(h->status, (int)LOFGB_ERR_UNSUPPORTED);
+        return;
+    }
+    if constexpr (BN == 256) {
+        grouped_body<256>(h, smem_raw);
+    } else {
+        GroupedSrc src{h};
+        tc_body<0, BN>(src, h->status, smem_raw, const_cast<uint32_t*>(h->range), true, WaitCfg{});
+    }
+}
+
 // ---- operand split: FP32 -> K-major BF16 hi/lo, zero padded -----------------
 // One 32-row x 64-k tile of an operand. Output rows [0, R) x cols [0, Kp)
 // (bf16). Source element (r, k) is src[r*ld + k] when kmajor, else
@@ -1400,8 +1422,12 @@ int lofgb_gemm_grouped_prepare(const lofgb_gemm_task* tasks, int ntasks, void* w
     return LOFGB_OK;
 }
 
-int lofgb_gemm_grouped_launch(const void* device_table, int64_t num_tiles, int64_t split_items,
-                              int grid, void* stream) {
+}  // extern "C"
+
+namespace lofgb {
+namespace {
+int grouped_launch(const void* kernel, int ki, const void* device_table, int64_t num_tiles,
+                   int64_t split_items, int grid, void* stream) {
     if (!device_table) return set_error(LOFGB_ERR_NULL, "NULL device table");
     if ((reinterpret_cast<uintptr_t>(device_table) & 255) != 0)
         return set_error(LOFGB_ERR_WORKSPACE, "device table must be 256-byte aligned");
@@ -1418,17 +1444,42 @@ int lofgb_gemm_grouped_launch(const void* device_table, int64_t num_tiles, int64
     if (num_tiles == 0) return LOFGB_OK;
     int dev = 0;
     cudaGetDevice(&dev);
-    static bool attr_set[64] = {false};
-    if (dev < 0 || dev >= 64 || !attr_set[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(gemm_tc_grouped_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
+    static bool attr_set[4][64] = {};
+    if (dev < 0 || dev >= 64 || !attr_set[ki][dev]) {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES);
         if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "smem attribute: %s", cudaGetErrorString(e));
-        if (dev >= 0 && dev < 64) attr_set[dev] = true;
+        if (dev >= 0 && dev < 64) attr_set[ki][dev] = true;
     }
     if (grid <= 0) grid = sm_count();
     if (grid > num_tiles) grid = (int)num_tiles;
-    gemm_tc_grouped_kernel<<<grid, NUM_THREADS, SMEM_BYTES, st>>>(h);
-    return check_launch("gemm_tc_grouped_kernel");
+    void* args[] = {const_cast<void*>(static_cast<const void*>(&h))};
+    cudaError_t e = cudaLaunchKernel(kernel, dim3(grid), dim3(NUM_THREADS), args, SMEM_BYTES, st);
+    if (e != cudaSuccess) return set_error(LOFGB_ERR_CUDA, "gemm_tc_grouped_kernel: %s", cudaGetErrorString(e));
+    return LOFGB_OK;
+}
+}  // namespace
+}  // namespace lofgb
+
+extern "C" {
+
+int lofgb_gemm_grouped_launch(const void* device_table, int64_t num_tiles, int64_t split_items,
+                              int grid, void* stream) {
+    return grouped_launch((const void*)gemm_tc_grouped_kernel, 0, device_table, num_tiles, split_items,
+                          grid, stream);
+}
+
+int lofgb_gemm_grouped_launch_w(const void* device_table, int64_t num_tiles, int64_t split_items,
+                                int grid, int tile_n, void* stream) {
+    if (tile_n == 64)
+        return grouped_launch((const void*)gemm_tc_grouped_w_kernel<64>, 1, device_table, num_tiles,
+                              split_items, grid, stream);
+    if (tile_n == 128)
+        return grouped_launch((const void*)gemm_tc_grouped_w_kernel<128>, 2, device_table, num_tiles,
+                              split_items, grid, stream);
+    if (tile_n == 256)
+        return grouped_launch((const void*)gemm_tc_grouped_w_kernel<256>, 3, device_table, num_tiles,
+                              split_items, grid, stream);
+    return set_error(LOFGB_ERR_UNSUPPORTED, "tile width %d (64, 128 or 256)", tile_n);
 }
 
 }  // extern "C"

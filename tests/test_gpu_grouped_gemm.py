@@ -76,3 +76,32 @@ def test_autotuner_caches(tmp_path, monkeypatch):
     torch.cuda.synchronize()
     for i, t in enumerate(tasks):
         assert torch.equal(t["D"], _reference(t)), i
+
+
+@pytest.mark.parametrize("schedule", ["lpt_snake", "128x64/lpt_snake", "128x256/lpt_snake"])
+def test_generic_launch_matches_width_launch(schedule):
+    """lofgb_gemm_grouped_launch (tile width read from the table on the
+    device) gives the bits of lofgb_gemm_grouped_launch_w (the kernel built
+    for the width); a width other than the table's is refused on the device."""
+    tasks = _tasks(5, 4)
+    gg = lg.GroupedGemm(tasks, schedule=schedule)
+    gg()
+    torch.cuda.synchronize()
+    want = [t["D"].clone() for t in tasks]
+    for t in tasks:
+        t["D"].zero_()
+    L = lg._native.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    assert L.lofgb_gemm_grouped_launch(gg.table.data_ptr(), gg.num_tiles, gg.split_items, gg.grid,
+                                       stream) == 0
+    torch.cuda.synchronize()
+    assert gg.status() == 0
+    for t, w in zip(tasks, want):
+        assert torch.equal(t["D"], w)
+    other = 128 if gg.tile_n != 128 else 256
+    assert L.lofgb_gemm_grouped_launch_w(gg.table.data_ptr(), gg.num_tiles, gg.split_items, gg.grid,
+                                         other, stream) == 0
+    torch.cuda.synchronize()
+    assert gg.status() == -7   # LOFGB_ERR_UNSUPPORTED
+    assert L.lofgb_gemm_grouped_launch_w(gg.table.data_ptr(), gg.num_tiles, gg.split_items, gg.grid,
+                                         96, stream) == -7
