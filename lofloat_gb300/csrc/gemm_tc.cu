@@ -20,11 +20,12 @@
 // an operand whose lo parts are all zero, and its lo tiles are then neither
 // loaded nor multiplied (MX operands: one MMA per k-step, half the bytes).
 //
-// Kernel layout (one CTA per SM, persistent over 128 x 128 output tiles):
+// Kernel layout (one CTA per SM, persistent over 128 x BN output tiles,
+// BN = 128 here; the 64- and 256-column shapes are described at TileShape):
 //   warp 0      TMA producer: up to 4 tiles (A hi/lo, B hi/lo) of 64 k per
 //               stage, 3 to 6 stages in 192 KiB (more when lo tiles are
 //               left out), 128-byte swizzle, one mbarrier per stage;
-//   warp 1      TMEM owner and MMA issuer (one elected lane):
+//   warp 1      TMEM owner and MMA issuer (one lane):
 //               tcgen05.mma.cta_group::1.kind::f16, M=128 N=128 K=16,
 //               chunk sums in four 128-column TMEM buffers (all 512
 //               columns), so the MMAs run up to three chunks ahead;
@@ -68,9 +69,12 @@ constexpr int PIPE_BYTES = 192 * 1024;         // shared memory of the stage rin
 //             32 KiB without lo tiles); four 128-column TMEM chunk buffers;
 //             16 epilogue warps of 32 columns;
 //   BN = 64:  stages of 48 KiB, 4 stages (8 without lo tiles); eight
-//             64-column chunk buffers; 8
-//             epilogue warps of 32 columns (the grouped kernel's narrow tile,
-//             more tiles for load balance across uneven GEMMs).
+//             64-column chunk buffers; 8 epilogue warps of 32 columns (the
+//             grouped kernel's narrow tile, more tiles for load balance
+//             across uneven GEMMs);
+//   BN = 256: stages of 96 KiB, 2 stages (4 without lo tiles); two
+//             256-column chunk buffers; 16 epilogue warps of 64 columns in
+//             8-column pieces (one MMA covers 256 columns).
 template <int BN>
 struct TileShape {
     static constexpr int TILE_B = BN * SK * 2;
