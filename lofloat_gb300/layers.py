@@ -152,6 +152,26 @@ def _lof_linear(x, weight, bias, accum_mant_bits, gemm_round_mode, stochastic_ro
     return out
 
 
+_TILED8 = {}
+
+
+def _tiled8_order(c: int, rs: int, device) -> torch.Tensor:
+    """The implicit-GEMM conv kernel's reduction order (csrc/conv.cu decode_t,
+    LOFGB_CONV_TILED8: 8-channel tiles outer, then the kernel position r*S + s,
+    then the channel within the tile; steps of channels past C skipped) as
+    indices into the im2col reduction axis c * RS + rs."""
+    key = (c, rs, str(device))
+    if key not in _TILED8:
+        perm = []
+        for t in range((c + 7) // 8 * 8 * rs):
+            ct, rem = divmod(t, 8 * rs)
+            ch = ct * 8 + (rem & 7)
+            if ch < c:
+                perm.append(ch * rs + (rem >> 3))
+        _TILED8[key] = torch.tensor(perm, dtype=torch.long, device=device)
+    return _TILED8[key]
+
+
 def _fwht(x: torch.Tensor, block_size=None) -> torch.Tensor:
     """Orthonormal Walsh–Hadamard transform along the last dim, optionally
     blockwise (same contract as LoFloat/layers.py:173-209)."""
@@ -397,11 +417,6 @@ class LoF_Conv2d(nn.Module):
             raise ValueError(f"scaling must be 'per_tensor' or 'mx', got {scaling!r}")
         if backend not in ("im2col", "cutlass"):
             raise ValueError(f"backend must be 'im2col' or 'cutlass', got {backend!r}")
-        if backend == "cutlass":
-            if scaling == "mx":
-                raise NotImplementedError("backend='cutlass' does not yet support scaling='mx'")
-            if groups != 1:
-                raise NotImplementedError("backend='cutlass' currently supports groups=1 only")
         self.backend = backend
         self.in_channels = in_channels
         self.out_channels = out_channels
@@ -424,8 +439,6 @@ class LoF_Conv2d(nn.Module):
         self.scale_format = scale_format if scale_format is not None else create_e8m0_params()
         if scaling == "mx":
             kh, kw = self.kernel_size
-            if groups != 1:
-                raise NotImplementedError("scaling='mx' for LoF_Conv2d currently supports groups=1 only")
             if (in_channels // groups) * kh * kw % mx_block_size != 0:
                 raise ValueError(
                     f"mx scaling needs the im2col K=(C_in/groups)*kH*kW="
@@ -521,38 +534,61 @@ class LoF_Conv2d(nn.Module):
                 x = _fwht(x, block_size=self.hadamard_block_size)
                 x = x.movedim(-1, 2).contiguous().view(b, c, h, w)
 
+        cin, cout = self.in_channels // self.groups, self.out_channels // self.groups
+
+        if self.scaling == "mx":
+            # MX blocks along each group's im2col reduction (C_in/groups * kH * kW),
+            # as the reference's im2col path defines them; one batched GEMM per
+            # group. backend="cutlass" sums the same rounded values in the
+            # implicit-GEMM kernel's reduction order (8-channel tiles, then
+            # (r, s), then the channel in the tile), by permuting the reduction
+            # axis before a sequential GEMM.
+            b = x.shape[0]
+            ho, wo = self._out_hw(x.shape[2], x.shape[3])
+            outs = []
+            for g in range(self.groups):
+                xg = x if self.groups == 1 else x[:, g * cin:(g + 1) * cin]
+                x_col = torch.nn.functional.unfold(xg, kernel_size=self.kernel_size,
+                                                   dilation=self.dilation, padding=self.padding,
+                                                   stride=self.stride)           # (B, K, L)
+                x_lk = STEMXRound.apply(x_col.transpose(1, 2).contiguous(), self.act_params,
+                                        self.scale_format, self.mx_block_size,
+                                        self.rounding_mode)                      # (B, L, K)
+                wg = self.weight if self.groups == 1 else self.weight[g * cout:(g + 1) * cout]
+                w_col = STEMXRound.apply(wg.reshape(cout, -1), self.weight_params,
+                                         self.scale_format, self.mx_block_size, self.rounding_mode)
+                if self.backend == "cutlass":
+                    perm = _tiled8_order(cin, self.kernel_size[0] * self.kernel_size[1], x.device)
+                    x_lk = x_lk.index_select(2, perm).contiguous()
+                    w_col = w_col.index_select(1, perm).contiguous()
+                outs.append(lof.gemm(w_col, x_lk, self.accum_mant_bits, trans_b=True,
+                                     variant=self.gemm_variant, chunk=self.chunk))   # (B, cout, L)
+            out = outs[0] if self.groups == 1 else torch.cat(outs, dim=1)
+            return self._bias(out.view(b, self.out_channels, ho, wo), scaled=False)
+
         if self.backend == "cutlass":
             x_q = STERound.apply(x, self.act_params, self.rounding_mode, self.act_scale_factor)
             w_q = STERound.apply(self.weight, self.weight_params, self.rounding_mode,
                                  self.w_scale_factor)
-            if self.gemm_variant == "plain":
-                out = lof.lof_conv2d(x_q, w_q, self.padding[0], self.padding[1], self.stride[0],
-                                     self.stride[1], self.dilation[0], self.dilation[1],
-                                     self.accum_mant_bits, self.gemm_round_mode,
-                                     self.stochastic_rounding_bits, float(self.w_scale_factor),
-                                     float(self.act_scale_factor))
-            else:
-                out = lof.conv2d(x_q, w_q, self.accum_mant_bits, stride=self.stride,
-                                 padding=self.padding, dilation=self.dilation,
-                                 alpha=lof.conv2d_alpha(self.w_scale_factor, self.act_scale_factor),
-                                 order="tiled8", variant=self.gemm_variant, chunk=self.chunk)
-            return self._bias(out)
 
-        if self.scaling == "mx":
-            b = x.shape[0]
-            ho, wo = self._out_hw(x.shape[2], x.shape[3])
-            x_col = torch.nn.functional.unfold(x, kernel_size=self.kernel_size,
-                                               dilation=self.dilation, padding=self.padding,
-                                               stride=self.stride)               # (B, K, L)
-            x_lk = STEMXRound.apply(x_col.transpose(1, 2).contiguous(), self.act_params,
-                                    self.scale_format, self.mx_block_size,
-                                    self.rounding_mode)                          # (B, L, K)
-            w_col = STEMXRound.apply(self.weight.reshape(self.out_channels, -1),
-                                     self.weight_params, self.scale_format, self.mx_block_size,
-                                     self.rounding_mode)
-            out = torch.stack([lof.gemm(w_col, x_lk[i], self.accum_mant_bits, trans_b=True)
-                               for i in range(b)])
-            return self._bias(out.view(b, self.out_channels, ho, wo), scaled=False)
+            def run(xx, ww):
+                if self.gemm_variant == "plain":
+                    return lof.lof_conv2d(xx, ww, self.padding[0], self.padding[1], self.stride[0],
+                                          self.stride[1], self.dilation[0], self.dilation[1],
+                                          self.accum_mant_bits, self.gemm_round_mode,
+                                          self.stochastic_rounding_bits, float(self.w_scale_factor),
+                                          float(self.act_scale_factor))
+                return lof.conv2d(xx, ww, self.accum_mant_bits, stride=self.stride,
+                                  padding=self.padding, dilation=self.dilation,
+                                  alpha=lof.conv2d_alpha(self.w_scale_factor, self.act_scale_factor),
+                                  order="tiled8", variant=self.gemm_variant, chunk=self.chunk)
+            if self.groups == 1:
+                out = run(x_q, w_q)
+            else:   # each group is an independent convolution over its channels
+                out = torch.cat([run(x_q[:, g * cin:(g + 1) * cin].contiguous(),
+                                     w_q[g * cout:(g + 1) * cout].contiguous())
+                                 for g in range(self.groups)], dim=1)
+            return self._bias(out)
 
         x_q = STERound.apply(x, self.act_params, self.rounding_mode, self.act_scale_factor)
         w_q = STERound.apply(self.weight, self.weight_params, self.rounding_mode, self.w_scale_factor)
@@ -565,7 +601,6 @@ class LoF_Conv2d(nn.Module):
         if self.groups == 1:
             out = conv(x_q, w_q)
         else:
-            cin, cout = x_q.shape[1] // self.groups, self.out_channels // self.groups
             out = torch.cat([conv(x_q[:, g * cin:(g + 1) * cin].contiguous(),
                                   w_q[g * cout:(g + 1) * cout].contiguous())
                              for g in range(self.groups)], dim=1)

@@ -102,10 +102,12 @@ def test_layer_constructor_validation():
     e4m3 = lg.create_p3109_params(8, 4)
     with pytest.raises(ValueError):
         lg.LoF_Conv2d(3, 4, 3, act_params=e4m3, weight_params=e4m3, scaling="mx", mx_block_size=32)
-    with pytest.raises(NotImplementedError):
-        lg.LoF_Conv2d(32, 4, 1, act_params=e4m3, weight_params=e4m3, scaling="mx", backend="cutlass")
-    with pytest.raises(NotImplementedError):
-        lg.LoF_Conv2d(4, 4, 3, groups=2, act_params=e4m3, weight_params=e4m3, backend="cutlass")
+    # every backend takes groups and MX scaling
+    lg.LoF_Conv2d(32, 4, 1, act_params=e4m3, weight_params=e4m3, scaling="mx", backend="cutlass")
+    lg.LoF_Conv2d(4, 4, 3, groups=2, act_params=e4m3, weight_params=e4m3, backend="cutlass")
+    lg.LoF_Conv2d(64, 4, 1, groups=2, act_params=e4m3, weight_params=e4m3, scaling="mx")
+    with pytest.raises(ValueError):   # the group's reduction 16 * 1 * 1 is not a whole MX block
+        lg.LoF_Conv2d(32, 4, 1, groups=2, act_params=e4m3, weight_params=e4m3, scaling="mx")
     with pytest.raises(ValueError):
         lg.LoF_Conv2d(6, 4, 3, act_params=e4m3, weight_params=e4m3, hadamard_transform=True)
     with pytest.raises(ValueError):
@@ -131,3 +133,21 @@ def test_format_accumulator_oracle_reduces_to_mantissa_rounding():
     for m in (7, 10, 12):
         fmt = O.fmt(9 + m, m, 127, saturating=False)
         assert same_bits(O.gemm_accfmt(A, B, fmt, alpha=0.25), O.gemm(A, B, m, alpha=0.25))
+
+
+@pytest.mark.parametrize("c", [3, 8, 10, 17])
+def test_tiled8_order_is_the_conv_kernels_reduction_order(c):
+    """The implicit-GEMM conv's 8-channel-tile reduction order, as the layer's
+    permutation of the im2col reduction axis: a sequential emulated GEMM over
+    the permuted columns gives the conv oracle's tiled-order bits."""
+    from lofloat_gb300.layers import _tiled8_order
+    rng = np.random.default_rng(c)
+    x = rng.standard_normal((2, c, 6, 5)).astype(np.float32)
+    w = rng.standard_normal((4, c, 3, 3)).astype(np.float32)
+    want = O.conv2d(x, w, 9, padding=(1, 1), order="tiled8")
+    perm = _tiled8_order(c, 9, "cpu").numpy()
+    cols = F.unfold(torch.from_numpy(x), kernel_size=3, padding=1).numpy()     # (N, C*9, L)
+    wc = np.ascontiguousarray(w.reshape(4, -1)[:, perm])
+    for n in range(2):
+        got = O.gemm(wc, np.ascontiguousarray(cols[n][perm]), 9)
+        assert same_bits(got, want[n].reshape(4, -1)), n

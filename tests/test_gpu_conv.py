@@ -226,3 +226,55 @@ def test_layer_mx_scaling():
         ref = torch.stack([lg.lof_gemm(wq, xq[b].contiguous(), 10) for b in range(2)])
     assert got.shape == (2, 16, 8, 8)
     assert same_bits(from_gpu(got).reshape(2, 16, -1), from_gpu(ref))
+
+
+def test_layer_cutlass_backend_with_groups():
+    """backend="cutlass" with groups: each group an independent implicit-GEMM
+    convolution over its channels, in the kernel's tiled reduction order."""
+    torch.manual_seed(3)
+    layer = lg.LoF_Conv2d(12, 6, 3, padding=1, groups=3, act_params=_p3109(8, 4),
+                          weight_params=_p3109(8, 4), bias=False, accum_mant_bits=10,
+                          backend="cutlass").cuda()
+    x = torch.randn(2, 12, 7, 6, device="cuda")
+    with torch.no_grad():
+        got = from_gpu(layer(x))
+        xq = from_gpu(lg.virtual_round(x, layer.act_params))
+        wq = from_gpu(lg.virtual_round(layer.weight, layer.weight_params))
+    want = np.concatenate([O.conv2d(np.ascontiguousarray(xq[:, 4 * g:4 * g + 4]),
+                                    np.ascontiguousarray(wq[2 * g:2 * g + 2]), 10, padding=(1, 1),
+                                    order="tiled8") for g in range(3)], axis=1)
+    assert same_bits(got, want)
+
+
+def _mx_cols(x, layer, g, cin, cout):
+    e8 = lg.create_e8m0_params()
+    cols = F.unfold(x[:, g * cin:(g + 1) * cin], kernel_size=3, padding=1)
+    xq = lg.virtual_mx_round(cols.transpose(1, 2).contiguous(), 32, layer.act_params, e8)
+    wq = lg.virtual_mx_round(layer.weight[g * cout:(g + 1) * cout].reshape(cout, -1), 32,
+                             layer.weight_params, e8)
+    return from_gpu(xq), from_gpu(wq)          # (N, L, K), (cout, K)
+
+
+@pytest.mark.parametrize("backend", ["im2col", "cutlass"])
+def test_layer_mx_scaling_with_groups(backend):
+    """scaling="mx" with groups: MX blocks along each group's im2col reduction;
+    im2col sums it in order, cutlass in the implicit-GEMM kernel's tiled order
+    (the same rounded values, the reduction axis permuted)."""
+    from lofloat_gb300.layers import _tiled8_order
+    torch.manual_seed(4)
+    G, cin, cout = 2, 32, 3
+    layer = lg.LoF_Conv2d(G * cin, G * cout, 3, padding=1, groups=G, act_params=_p3109(8, 4),
+                          weight_params=_p3109(8, 4), bias=False, accum_mant_bits=10,
+                          scaling="mx", mx_block_size=32, backend=backend).cuda()
+    x = torch.randn(2, G * cin, 5, 6, device="cuda")
+    with torch.no_grad():
+        got = from_gpu(layer(x)).reshape(2, G * cout, -1)
+        parts = []
+        for g in range(G):
+            xq, wq = _mx_cols(x, layer, g, cin, cout)
+            if backend == "cutlass":
+                perm = _tiled8_order(cin, 9, "cpu").numpy()
+                xq, wq = xq[..., perm], wq[:, perm]
+            parts.append(np.stack([O.gemm(np.ascontiguousarray(wq), np.ascontiguousarray(xq[n].T), 10)
+                                   for n in range(2)]))
+    assert same_bits(got, np.concatenate(parts, axis=1))
