@@ -26,16 +26,19 @@ namespace lofgb {
 
 namespace {
 
-// One 128 x 128 output tile of one GEMM of the batch.
-template <int ACC>
+// One 128 x 128 output tile of one GEMM of the batch (HALF: a 64-row tile,
+// blockIdx.y counting 64-row steps).
+template <int ACC, bool HALF>
 __device__ __forceinline__ void plain_tile(float (*As)[BK][BM + PAD], float (*Bs)[BK][BN + PAD],
                                            const float* __restrict__ A, int64_t lda, int ta,
                                            const float* __restrict__ B, int64_t ldb, int tb,
                                            float* __restrict__ D, int64_t ldd, int M, int N,
                                            int K, const AccRound& r, float alpha) {
+    constexpr int ROWS = HALF ? BM / 2 : BM;   // A rows staged per k-tile
+    constexpr int RI = HALF ? 4 : 8;           // accumulator rows per thread
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int m0 = blockIdx.y * ROWS, n0 = blockIdx.x * BN;
 
     float acc[8][8];
 #pragma unroll
@@ -50,12 +53,14 @@ __device__ __forceinline__ void plain_tile(float (*As)[BK][BM + PAD], float (*Bs
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int idx = tid + q * NT;
-            int m, k;
-            if (ta) { k = idx / BM; m = idx % BM; } else { m = idx / BK; k = idx % BK; }
-            const int gm = m0 + m, gk = k0 + k;
-            const bool va = gm < M && gk < K;
-            const float* src = va ? (ta ? A + (int64_t)gk * lda + gm : A + (int64_t)gm * lda + gk) : A;
-            cp_async4(smem_addr(&As[buf][k][m]), src, va);
+            if (q < ROWS * BK / NT) {
+                int m, k;
+                if (ta) { k = idx / ROWS; m = idx % ROWS; } else { m = idx / BK; k = idx % BK; }
+                const int gm = m0 + m, gk = k0 + k;
+                const bool va = gm < M && gk < K;
+                const float* src = va ? (ta ? A + (int64_t)gk * lda + gm : A + (int64_t)gm * lda + gk) : A;
+                cp_async4(smem_addr(&As[buf][k][m]), src, va);
+            }
             int n, kb;
             if (tb) { n = idx / BK; kb = idx % BK; } else { kb = idx / BN; n = idx % BN; }
             const int gn = n0 + n, gkb = k0 + kb;
@@ -77,12 +82,12 @@ __device__ __forceinline__ void plain_tile(float (*As)[BK][BM + PAD], float (*Bs
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
         __syncthreads();
-        mac_ktile<ACC>(As[buf], Bs[buf], acc, min(BK, K - kt * BK), tx, ty, r);
+        mac_ktile<ACC, RI>(As[buf], Bs[buf], acc, min(BK, K - kt * BK), tx, ty, r);
         __syncthreads();  // buffer `buf` is refilled by the next iteration's issue()
     }
 
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < RI; ++i) {
         const int gm = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
         if (gm >= M) continue;
 #pragma unroll
@@ -94,7 +99,7 @@ __device__ __forceinline__ void plain_tile(float (*As)[BK][BM + PAD], float (*Bs
 }
 
 // blockIdx.z walks the batch (strided-batched GEMM; batch 1 for a single one).
-template <int ACC>
+template <int ACC, bool HALF>
 __global__ void __launch_bounds__(NT, 2)
 gemm_plain_kernel(const float* __restrict__ A, int64_t lda, int64_t sa, int ta,
                   const float* __restrict__ B, int64_t ldb, int64_t sb, int tb,
@@ -103,8 +108,8 @@ gemm_plain_kernel(const float* __restrict__ A, int64_t lda, int64_t sa, int ta,
     __shared__ __align__(16) float As[2][BK][BM + PAD];
     __shared__ __align__(16) float Bs[2][BK][BN + PAD];
     for (int z = blockIdx.z; z < batch; z += gridDim.z) {
-        plain_tile<ACC>(As, Bs, A + (int64_t)z * sa, lda, ta, B + (int64_t)z * sb, ldb, tb,
-                        D + (int64_t)z * sd, ldd, M, N, K, r, alpha);
+        plain_tile<ACC, HALF>(As, Bs, A + (int64_t)z * sa, lda, ta, B + (int64_t)z * sb, ldb, tb,
+                              D + (int64_t)z * sd, ldd, M, N, K, r, alpha);
         __syncthreads();  // the next batch entry refills the shared tiles
     }
 }
@@ -153,11 +158,25 @@ int launch_gemm_plain(const float* A, int64_t lda, int64_t sa, int ta, const flo
                       int N, int K, int batch, int mbits, const RoundPlan* acc_fmt, float alpha,
                       void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch < 65535 ? batch : 65535);
+    // Two CTAs per SM run at once. A single GEMM of fewer 128 x 128 tiles than
+    // that runs as 64-row tiles, twice the CTAs for half the work each
+    // (1024^2: 128 CTAs instead of 64); every output keeps its whole k order,
+    // so the bits do not change.
+    const int64_t tiles = (int64_t)((N + BN - 1) / BN) * ((M + BM - 1) / BM);
+    const bool half = batch == 1 && tiles < 2 * (int64_t)sm_count();
+    dim3 grid((N + BN - 1) / BN, half ? (M + BM / 2 - 1) / (BM / 2) : (M + BM - 1) / BM,
+              batch < 65535 ? batch : 65535);
     if (grid.y > 65535) return set_error(LOFGB_ERR_SIZE, "M too large for the plain GEMM grid");
     AccRound r = acc_mant(mbits);
-#define LOFGB_PLAIN(ACC) \
-    gemm_plain_kernel<ACC><<<grid, NT, 0, st>>>(A, lda, sa, ta, B, ldb, sb, tb, D, ldd, sd, M, N, K, batch, r, alpha)
+#define LOFGB_PLAIN(ACC)                                                                        \
+    do {                                                                                        \
+        if (half)                                                                               \
+            gemm_plain_kernel<ACC, true><<<grid, NT, 0, st>>>(A, lda, sa, ta, B, ldb, sb, tb, D, \
+                                                              ldd, sd, M, N, K, batch, r, alpha); \
+        else                                                                                    \
+            gemm_plain_kernel<ACC, false><<<grid, NT, 0, st>>>(A, lda, sa, ta, B, ldb, sb, tb, D, \
+                                                               ldd, sd, M, N, K, batch, r, alpha); \
+    } while (0)
     if (acc_fmt) {
         r.plan = *acc_fmt;
         if (acc_fmt->uni == 1) LOFGB_PLAIN(ACC_UNI);

@@ -62,7 +62,8 @@ __device__ __forceinline__ void cp_async4(uint32_t dst, const float* src, bool v
 // owns rows {ty*4 .. ty*4+3, 64+ty*4 .. 64+ty*4+3} and the same columns of tx.
 // One 8x8 MAC block per k (640 instructions) stays resident in the
 // instruction cache; unrolling k as well overflows it.
-template <int ACC>
+// RI = 4: only the first four rows (the 64-row half tile of the plain GEMM).
+template <int ACC, int RI = 8>
 __device__ __forceinline__ void mac_ktile(const float (*As)[BM + PAD], const float (*Bs)[BN + PAD],
                                           float (&acc)[8][8], int kmax, int tx, int ty,
                                           const AccRound& r) {
@@ -75,7 +76,7 @@ __device__ __forceinline__ void mac_ktile(const float (*As)[BM + PAD], const flo
         const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
         const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
+        for (int i = 0; i < RI; ++i)
 #pragma unroll
             for (int j = 0; j < 8; ++j) acc[i][j] = emac<ACC>(av[i], bv[j], acc[i][j], r);
     }

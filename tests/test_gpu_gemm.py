@@ -50,6 +50,20 @@ def test_shapes_and_tails(shape):
     assert same_bits(got, want), mismatch_report(got, got, want)
 
 
+@pytest.mark.parametrize("shape", [(2600, 2200, 40), (1000, 700, 64)])
+def test_whole_and_half_tiles(shape):
+    """378 tiles of 128 x 128 (more than one wave: whole tiles) and 48 tiles
+    (fewer than the GPU holds at once: 64-row half tiles), ragged M and N
+    edges in both; every output equals the oracle's bits."""
+    M, N, K = shape
+    rng = np.random.default_rng(11)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.uniform(-1, 1, (K, N)).astype(np.float32)
+    got = from_gpu(lg.gemm(to_gpu(A), to_gpu(B), 10))
+    want = O.gemm(A, B, 10)
+    assert same_bits(got, want), mismatch_report(got, got, want)
+
+
 def test_special_values():
     rng = np.random.default_rng(3)
     A = rng.standard_normal((40, 64)).astype(np.float32)
