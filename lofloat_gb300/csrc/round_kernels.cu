@@ -24,6 +24,7 @@ namespace {
 constexpr int RT = 256;  // threads per CTA
 constexpr int RU = 4;    // 16-byte vectors per thread per iteration
 constexpr int RING = 3;  // cp.async stages per thread (RING - 1 iterations prefetched)
+static_assert(RU % 2 == 0, "SR-A draws are shared over pairs of steps");
 
 
 struct ScaleArg {
@@ -157,15 +158,44 @@ round_vec_kernel(const uint4* vin, uint4* vout, int64_t n,
             if (bp + RT * RU <= nvec) issue(k, bp);
             cp_async_commit();
         }
+        // SR-A with 8-bit random lanes: one 64-bit draw serves 8 elements,
+        // two neighbouring lanes' vectors. With the element offset a multiple
+        // of 8, each lane computes one draw (its pair's, of step u or u + 1)
+        // and the pair shares it by shuffles, half the draws of rng_elem4.
+        constexpr bool SRA = W == 32 && FMT && (UNI == 3 || UNI == 5);
+        const bool pair_draws = SRA && p.rng_lg == 3 && (offset & 7u) == 0;
+        const int lane = threadIdx.x & 31;
         int stage = 0;
         for (; base + RT * RU <= nvec; base += stride, bp += stride) {
             if (bp + RT * RU <= nvec) issue(stage == 0 ? RING - 1 : stage - 1, bp);
             cp_async_commit();
             cp_async_wait<RING - 1>();
+            if (SRA && pair_draws) {
 #pragma unroll
-            for (int u = 0; u < RU; ++u) {
-                const int64_t vi = base + u * RT + threadIdx.x;
-                __stcs(vout + vi, round_vec(ring[stage][u][threadIdx.x], vi, true));
+                for (int u = 0; u < RU; u += 2) {
+                    const int64_t vj = base + (u + (lane & 1)) * RT + (threadIdx.x & ~1);
+                    const uint64_t w = rng64(seed, (offset + (uint64_t)vj * 4) >> 3);
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const uint64_t wu = __shfl_sync(0xFFFFFFFFu, w, h ? (lane | 1) : (lane & ~1));
+                        const uint32_t half = (lane & 1) ? (uint32_t)(wu >> 32) : (uint32_t)wu;
+                        const int64_t vi = base + (u + h) * RT + threadIdx.x;
+                        const uint4 vv = ring[stage][u + h][threadIdx.x];
+                        uint32_t x[4] = {vv.x, vv.y, vv.z, vv.w};
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            if (SCALED) x[q] = __float_as_uint(__fmul_rn(s.f, __uint_as_float(x[q])));
+                            x[q] = vr_uni_sra_f32<UNI == 5>(x[q], p, (uint64_t)(half >> (8 * q)));
+                        }
+                        __stcs(vout + vi, make_uint4(x[0], x[1], x[2], x[3]));
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < RU; ++u) {
+                    const int64_t vi = base + u * RT + threadIdx.x;
+                    __stcs(vout + vi, round_vec(ring[stage][u][threadIdx.x], vi, true));
+                }
             }
             stage = stage == RING - 1 ? 0 : stage + 1;
         }

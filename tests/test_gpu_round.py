@@ -246,3 +246,21 @@ def test_float_grid_modes_at_grid_points(fmt, mode):
     got = from_gpu(lg.virtual_round(to_gpu(x), desc, round_mode=mode))
     want = O.round(x, ofmt(desc), mode, 0)
     assert same_bits(got, want), mismatch_report(x, got, want)
+
+
+@pytest.mark.parametrize("fmt", [(8, 3, 7, True, True), (8, 2, 15, False, True)])
+@pytest.mark.parametrize("ln", [5, 8])
+@pytest.mark.parametrize("offset", [0, 8, 4096, 4, 12, 3])
+@pytest.mark.parametrize("scale", [1.0, 0.37])
+def test_sr_a_draw_sharing(fmt, ln, offset, scale):
+    """SR-A with 8-bit random lanes: with the element offset a multiple of 8
+    neighbouring lanes share one 64-bit draw (each lane computes one, the
+    pair exchanges them); other offsets draw per vector. Both against the
+    oracle fed the same counter stream, saturating and non-saturating
+    formats, with and without the fused scale."""
+    desc = _desc(fmt)
+    x = _wide_f32(300_007, seed=offset + ln)
+    got = from_gpu(lg.virtual_round(to_gpu(x), desc, round_mode=3, stoch_len=ln, seed=21,
+                                    offset=offset, scale=scale))
+    want = O.round(x, ofmt(desc), 3, ln, seed=21, offset=offset, scale=scale)
+    assert same_bits(got, want), mismatch_report(x, got, want)
