@@ -473,6 +473,14 @@ def codec_workloads(torch, lg, dev, peaks):
         nbytes = xm.numel() * (4 + fmt.total_bits / 8 + 1 / 32)
         out[f"mx_encode_{name}_8192^2_GBs"] = round(nbytes / (ms * 1e-3) / 1e9, 1)
         out[f"mx_encode_{name}_8192^2_frac_hbm"] = round(nbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)
+        # and back: element codes times block scales, one kernel
+        codes, scales = fn()
+        dec = lambda: lg.mx_decode(codes, scales, xm.numel(), fmt, e8)  # noqa: E731
+        for _ in range(3):
+            dec()
+        ms = time_batched(torch, dec, stream)
+        out[f"mx_decode_{name}_8192^2_GBs"] = round(nbytes / (ms * 1e-3) / 1e9, 1)
+        out[f"mx_decode_{name}_8192^2_frac_hbm"] = round(nbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)
     return out
 
 

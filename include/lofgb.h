@@ -542,6 +542,17 @@ int lofgb_mx_encode_f32(const float* src, uint8_t* codes, uint8_t* scales, int64
                         const lofgb_codec_format* scale_fmt, int mode, int scale_mode,
                         int sat_mode, int stoch_len, uint64_t seed, uint64_t offset, void* stream);
 
+/* Values of MX storage in one pass: dst[i] = decode(element code i) *
+ * decode(scale code of block i / 32) in FP32 (round to nearest), the
+ * composition of lofgb_decode_f32 on both streams and the product. Blocks of
+ * 32; element codes of 4, 6 or 8 bits (forward groups, as lofgb_mx_encode_f32
+ * writes them), 8-bit scale codes. `codes` 4-byte aligned, `dst` 16-byte
+ * aligned (LOFGB_ERR_SIZE otherwise), no overlap between output and inputs.
+ * No counterpart in the reference. */
+int lofgb_mx_decode_f32(const uint8_t* codes, const uint8_t* scales, float* dst, int64_t count,
+                        int block_size, const lofgb_codec_format* elem_fmt,
+                        const lofgb_codec_format* scale_fmt, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

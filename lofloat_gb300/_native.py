@@ -116,6 +116,8 @@ SIGNATURES = [
     ("lofgb_mx_encode_f32", _i32, [_vp, _vp, _vp, _i64, _i32, C.POINTER(LofgbCodecFormat),
                                    C.POINTER(LofgbCodecFormat), _i32, _i32, _i32, _i32, _u64, _u64,
                                    _vp]),
+    ("lofgb_mx_decode_f32", _i32, [_vp, _vp, _vp, _i64, _i32, C.POINTER(LofgbCodecFormat),
+                                   C.POINTER(LofgbCodecFormat), _vp]),
 ]
 
 

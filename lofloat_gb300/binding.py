@@ -716,7 +716,24 @@ def mx_decode(codes: torch.Tensor, scales: torch.Tensor, count: int,
               element_format: FloatFormatDescriptor, scale_format: FloatFormatDescriptor, *,
               block_size: int = 32) -> torch.Tensor:
     """Values of MX storage: decoded element codes times their block's decoded
-    scale (a float32 tensor of `count` values)."""
+    scale (a float32 tensor of `count` values); one kernel
+    (lofgb_mx_decode_f32) for blocks of 32, 4/6/8-bit element codes and
+    8-bit scale codes, else the two codec decodes and the product."""
+    if (block_size == 32 and element_format.total_bits in (4, 6, 8) and scale_format.total_bits == 8
+            and codes.dtype == torch.uint8 and scales.dtype == torch.uint8 and codes.is_cuda
+            and scales.is_cuda and codes.device == scales.device and count >= 0
+            and codes.is_contiguous() and scales.is_contiguous() and codes.data_ptr() % 4 == 0):
+        if codes.numel() < packed_size(element_format.total_bits, count) or scales.numel() < (count + 31) // 32:
+            raise RuntimeError("mx_decode: codes or scales shorter than `count` values need")
+        out = torch.empty(count, dtype=torch.float32, device=codes.device)
+        if count == 0:
+            return out
+        ef, sf = codec_format(element_format), codec_format(scale_format)
+        with torch.cuda.device(codes.device):
+            check(_native.lib().lofgb_mx_decode_f32(codes.data_ptr(), scales.data_ptr(), out.data_ptr(),
+                                                    count, 32, C.byref(ef), C.byref(sf),
+                                                    _stream(codes)), "mx_decode")
+        return out
     q = lof_decode(codes, count, element_format)
     nb = (count + block_size - 1) // block_size
     sc = lof_decode(scales, nb, scale_format)

@@ -1222,6 +1222,68 @@ int launch_mx_encode_n(const float* in, uint8_t* codes, uint8_t* scales, int64_t
     return check_launch("mx_encode_kernel");
 }
 
+// MX storage decode: value i = decode(element code i) * decode(scale code of
+// block i / 32), one FP32 multiply (round to nearest), as the composition of
+// two codec decodes and a product. Every CTA first decodes all 256 scale
+// codes into a shared-memory table; then a lane decodes four values (their 4N
+// bits from the two words that hold them), reads its block's scale code and
+// the table, and writes one float4 (a warp's store is 512 contiguous bytes).
+// nq: quads whose two-word window lies inside the element codes; one thread
+// decodes the rest.
+template <int N, bool FAST>
+__global__ void __launch_bounds__(256)
+mx_decode_kernel(const uint32_t* __restrict__ codes, const uint8_t* __restrict__ scales,
+                 float4* __restrict__ dst, int64_t nq, int64_t count, int64_t code_bytes,
+                 CodecArg ea, CodecArg sa) {
+    static_assert(N == 4 || N == 6 || N == 8, "MX storage codes of 4, 6 or 8 bits");
+    constexpr uint32_t CM = (1u << N) - 1u;
+    __shared__ float slut[256];
+    slut[threadIdx.x] = sa.dec_fast ? codec_decode_fast(threadIdx.x, sa) : codec_decode(threadIdx.x, sa);
+    __syncthreads();
+    pdl_wait();
+    for (int64_t q = (int64_t)blockIdx.x * 256 + threadIdx.x; q < nq; q += (int64_t)gridDim.x * 256) {
+        const int64_t b = 4 * N * q;
+        const int64_t w0 = b >> 5;
+        const uint32_t lo = __ldg(codes + w0), hi = __ldg(codes + w0 + 1);
+        const float sc = slut[__ldg(scales + (q >> 3))];   // block 4q / 32
+        const uint32_t bits = (uint32_t)((((uint64_t)hi << 32) | lo) >> (b & 31));
+        float y[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) y[k] = __fmul_rn(decode_one<FAST>((bits >> (N * k)) & CM, ea), sc);
+        __stcs(dst + q, make_float4(y[0], y[1], y[2], y[3]));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint8_t* s8 = reinterpret_cast<const uint8_t*>(codes);
+        float* d = reinterpret_cast<float*>(dst);
+        for (int64_t i = nq * 4; i < count; ++i) {
+            const int64_t bit = i * N;
+            uint32_t v = 0;
+            for (int k = 0; k < 2; ++k)
+                if ((bit >> 3) + k < code_bytes) v |= (uint32_t)s8[(bit >> 3) + k] << (8 * k);
+            d[i] = __fmul_rn(decode_one<FAST>((v >> (bit & 7)) & CM, ea), slut[scales[i / 32]]);
+        }
+    }
+}
+
+template <int N>
+int launch_mx_decode_n(const uint8_t* codes, const uint8_t* scales, float* dst, int64_t count,
+                       const CodecArg& ea, const CodecArg& sa, cudaStream_t st) {
+    const int64_t cb = packed_bytes(N, count);
+    const int64_t words = cb / 4;
+    const int64_t qlim = words >= 2 ? (8 * (words - 1) + N - 1) / N : 0;
+    const int64_t nq = std::min(count / 4, qlim);
+    const int64_t need = (nq + 255) / 256;
+    const int64_t maxg = (int64_t)sm_count() * 8;
+    const int grid = (int)(need < 1 ? 1 : (need < maxg ? need : maxg));
+    const uint32_t* c32 = reinterpret_cast<const uint32_t*>(codes);
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    if (ea.dec_fast)
+        launch_pdl(mx_decode_kernel<N, true>, grid, 256, 0, st, c32, scales, d4, nq, count, cb, ea, sa);
+    else
+        launch_pdl(mx_decode_kernel<N, false>, grid, 256, 0, st, c32, scales, d4, nq, count, cb, ea, sa);
+    return check_launch("mx_decode_kernel");
+}
+
 int codec_pointers(const void* a, const void* b, int64_t count) {
     if (count < 0) return set_error(LOFGB_ERR_SIZE, "negative count");
     if (count > 0 && (!a || !b)) return set_error(LOFGB_ERR_NULL, "NULL buffer");
@@ -1299,6 +1361,38 @@ int lofgb_mx_encode_f32(const float* src, uint8_t* codes, uint8_t* scales, int64
     if (nb == 4) return launch_mx_encode_n<4>(src, codes, scales, count, pe, ps, inv, ea, sa, seed, offset, cs);
     if (nb == 6) return launch_mx_encode_n<6>(src, codes, scales, count, pe, ps, inv, ea, sa, seed, offset, cs);
     return launch_mx_encode_n<8>(src, codes, scales, count, pe, ps, inv, ea, sa, seed, offset, cs);
+}
+
+int lofgb_mx_decode_f32(const uint8_t* codes, const uint8_t* scales, float* dst, int64_t count,
+                        int block_size, const lofgb_codec_format* elem_fmt,
+                        const lofgb_codec_format* scale_fmt, void* stream) {
+    clear_error();
+    if (block_size != 32) return set_error(LOFGB_ERR_BLOCK, "MX storage blocks are 32 values (got %d)", block_size);
+    if (!elem_fmt || !scale_fmt) return set_error(LOFGB_ERR_NULL, "NULL codec format");
+    const int nb = elem_fmt->fmt.bitwidth;
+    if (nb != 4 && nb != 6 && nb != 8)
+        return set_error(LOFGB_ERR_UNSUPPORTED, "MX storage element codes of %d bits (4, 6 or 8 supported)", nb);
+    if (scale_fmt->fmt.bitwidth != 8)
+        return set_error(LOFGB_ERR_UNSUPPORTED, "MX storage scale codes must be 8 bits");
+    CodecArg ea, sa;
+    int st = make_codec_arg(&ea, elem_fmt, LOFGB_RNE, 0, 0);
+    if (!st) st = make_codec_arg(&sa, scale_fmt, LOFGB_RNE, 0, 0);
+    if (st) return st;
+    if (count < 0) return set_error(LOFGB_ERR_SIZE, "negative count");
+    if (count == 0) return LOFGB_OK;
+    if (!codes || !scales || !dst) return set_error(LOFGB_ERR_NULL, "NULL data pointer");
+    if ((reinterpret_cast<uintptr_t>(codes) & 3) || (reinterpret_cast<uintptr_t>(dst) & 15))
+        return set_error(LOFGB_ERR_SIZE, "codes must be 4-byte and the output 16-byte aligned");
+    const int64_t cbytes = packed_bytes(nb, count), sbytes = (count + 31) / 32;
+    const char* c = reinterpret_cast<const char*>(codes);
+    const char* k = reinterpret_cast<const char*>(scales);
+    const char* d = reinterpret_cast<const char*>(dst);
+    if ((d < c + cbytes && c < d + count * 4) || (d < k + sbytes && k < d + count * 4))
+        return set_error(LOFGB_ERR_ALIAS, "the output must not overlap the codes or scales");
+    cudaStream_t cs = static_cast<cudaStream_t>(stream);
+    if (nb == 4) return launch_mx_decode_n<4>(codes, scales, dst, count, ea, sa, cs);
+    if (nb == 6) return launch_mx_decode_n<6>(codes, scales, dst, count, ea, sa, cs);
+    return launch_mx_decode_n<8>(codes, scales, dst, count, ea, sa, cs);
 }
 
 int lofgb_decode_f32(float* dst, const uint8_t* src, int64_t count, const lofgb_codec_format* fmt,

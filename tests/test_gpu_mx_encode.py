@@ -130,3 +130,45 @@ def test_config2_storage_against_oracle_and_mx_round():
     bd, rd = back[diff], ref[diff]
     assert np.array_equal(np.abs(bd), (top * np.repeat(sc, 32).reshape(-1, 32))[diff])
     assert np.all(np.abs(rd) > np.abs(bd)) and np.all(np.sign(rd) == np.sign(bd))
+
+
+def _composed_decode(codes, scales, n, ef_desc, sf_desc):
+    q = lg.lof_decode(codes, n, ef_desc)
+    sc = lg.lof_decode(scales, (n + 31) // 32, sf_desc)
+    return q.view(-1)[:n] * sc.repeat_interleave(32)[:n]
+
+
+@pytest.mark.parametrize("bits,p,signed", [(4, 2, True), (6, 3, True), (6, 4, True), (8, 4, True),
+                                           (8, 3, True), (8, 4, False), (6, 3, False)])
+@pytest.mark.parametrize("n", [32 * 4096, 32 * 77 + 13, 5, 128 * 3 + 31, 1000])
+def test_mx_decode_kernel_equals_composition(bits, p, signed, n):
+    """lofgb_mx_decode_f32 (one kernel) against the two codec decodes and the
+    FP32 product, bit for bit, on storage with specials and all-zero blocks."""
+    rng = np.random.default_rng(bits * 100 + n)
+    x = (rng.standard_normal(n) * np.exp2(rng.integers(-12, 13, n))).astype(np.float32)
+    if n > 70:
+        x[32:64] = 0.0
+        x[rng.integers(0, n, 3)] = np.array([np.inf, np.nan, -np.inf], np.float32)
+    ef = lg.create_p3109_params(bits, p, signed)
+    e8 = lg.create_e8m0_params()
+    codes, scales = lg.mx_encode(to_gpu(x), ef, e8)
+    got = lg.mx_decode(codes, scales, n, ef, e8)
+    want = _composed_decode(codes, scales, n, ef, e8)
+    assert got.shape == (n,)
+    assert np.array_equal(from_gpu(got).view(np.uint32), from_gpu(want).view(np.uint32)), \
+        int((from_gpu(got).view(np.uint32) != from_gpu(want).view(np.uint32)).sum())
+
+
+def test_mx_decode_argument_checks():
+    L = _native.lib()
+    ef, sf = _native_fmt(O.codec_p3109(8, 4)), _native_fmt(E8M0_O)
+    c = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    s = torch.zeros(2, dtype=torch.uint8, device="cuda")
+    d = torch.zeros(64, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    assert L.lofgb_mx_decode_f32(c.data_ptr(), s.data_ptr(), d.data_ptr(), 64, 16, C.byref(ef),
+                                 C.byref(sf), st) == -5
+    assert L.lofgb_mx_decode_f32(c.data_ptr(), s.data_ptr(), d.data_ptr() + 4, 64, 32, C.byref(ef),
+                                 C.byref(sf), st) == -2
+    assert L.lofgb_mx_decode_f32(c.data_ptr(), s.data_ptr(), d.data_ptr(), 64, 32, C.byref(ef),
+                                 C.byref(sf), st) == 0
