@@ -1037,8 +1037,13 @@ mx_encode_kernel(const float* __restrict__ in, uint8_t* __restrict__ codes,
                  uint8_t* __restrict__ scales, int64_t n, RoundPlan pe, RoundPlan ps,
                  float inv_pmn, CodecArg ea, CodecArg sa, uint64_t seed, uint64_t offset, int vec,
                  int64_t code_bytes) {
-    pdl_wait();
     static_assert(N == 4 || N == 6 || N == 8, "MX storage codes of 4, 6 or 8 bits");
+    // scale codes of the values with a zero mantissa field (+0, the powers
+    // of two, +inf: every E8M0 scale) by exponent field, encoded once per CTA
+    __shared__ uint8_t scode[256];
+    scode[threadIdx.x] = (uint8_t)codec_encode<LOFGB_RNE>(__uint_as_float(threadIdx.x << 23), sa, 0ull);
+    __syncthreads();
+    pdl_wait();
     constexpr int U = 4;  // steps of 128 values per warp iteration, loaded up front
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * 256 + threadIdx.x) >> 5;
@@ -1079,7 +1084,8 @@ mx_encode_kernel(const float* __restrict__ in, uint8_t* __restrict__ codes,
         const BlockScale bsj = block_scale<-1>(aj, ps, inv_pmn, seed, offset + (uint64_t)blkj);
         const uint32_t sbj = __float_as_uint(bsj.scale);
         if (lane < 16 && blkj < n)
-            scales[blkj / 32] = (uint8_t)codec_encode<LOFGB_RNE>(bsj.scale, sa, 0ull);
+            scales[blkj / 32] = (sbj & 0x807FFFFFu) == 0u ? scode[sbj >> 23]
+                                                          : (uint8_t)codec_encode<LOFGB_RNE>(bsj.scale, sa, 0ull);
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int64_t e = (s0 + u) * 128 + lane * 4;
