@@ -14,15 +14,22 @@
 //                          co-resident wave; every CTA reduces its slice of
 //                          one channel to a pair of doubles: sum x, or the
 //                          shifted sums sum (x - K), sum (x - K)^2 (K = the
-//                          channel's first value), or sum |x - mean|, or
-//                          max |x - mean| with the FP32 mean of the previous
-//                          pass, the centring the reference performs in FP32;
+//                          channel's first value), or sum |x - mean| with the
+//                          FP32 mean of the previous pass (the centring the
+//                          reference performs in FP32), or sum x with the
+//                          FP32 max and min of x packed in the second double;
 //                          the channel's last CTA (a ticket per channel)
 //                          combines the splits in double, writes the FP32
 //                          statistic and the running-average update
 //                          r = r (1 - m) + m s.
-// L1 / L-infinity take two statistics passes (mean, then the deviation
-// about it); the variance variants one.
+// L1 takes two statistics passes (mean, then the deviation about it);
+// L-infinity and the variance variants one. L-infinity's max |x - mean| is
+// max(max x - mean, mean - min x) with both differences rounded in FP32:
+// rounding is monotone, so the largest rounded |x - mean| comes from the
+// largest or the smallest x, and the bits equal those of the maximum taken
+// over every centred value. A NaN input makes the sum, the mean and so the
+// deviation NaN; an infinite x makes one difference inf - inf = NaN, as the
+// centred value of that x is.
 //
 // Normalisation (HBM-bound, 4 B read + 4 B written per element): per element
 // in FP32, in the reference's operation order,
@@ -50,7 +57,7 @@ constexpr int TARGET_CTAS = 1216;  // statistics grid: about 8 CTAs per SM
 constexpr int MAX_SPLITS = 1024;
 constexpr int UNR = 4;             // 16-byte vectors in flight per thread
 
-enum { P_SUM = 0, P_SHIFTED = 1, P_ABSDEV = 2, P_MAXDEV = 3 };
+enum { P_SUM = 0, P_SHIFTED = 1, P_ABSDEV = 2, P_SUMRANGE = 3 };
 
 struct BnGeo {
     int64_t n, c, inner;
@@ -94,9 +101,19 @@ __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
     return v;
 }
-__device__ __forceinline__ double warp_max(double v) {
+// The FP32 max and min of a P_SUMRANGE pass travel as the two halves of one
+// double's bits (moved and stored, never used in arithmetic).
+__device__ __forceinline__ double pack_range(float hi, float lo) {
+    return __hiloint2double(__float_as_int(hi), __float_as_int(lo));
+}
+__device__ __forceinline__ float range_hi(double v) { return __int_as_float(__double2hiint(v)); }
+__device__ __forceinline__ float range_lo(double v) { return __int_as_float(__double2loint(v)); }
+__device__ __forceinline__ double range_join(double u, double v) {
+    return pack_range(fmaxf(range_hi(u), range_hi(v)), fminf(range_lo(u), range_lo(v)));
+}
+__device__ __forceinline__ double warp_range(double v) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = range_join(v, __shfl_xor_sync(0xFFFFFFFFu, v, o));
     return v;
 }
 
@@ -105,42 +122,44 @@ __device__ __forceinline__ double warp_max(double v) {
 template <int P>
 struct Acc {
     float a = 0.0f, b = 0.0f;
-    float k = 0.0f;  // shift (P_SHIFTED) or FP32 mean (P_ABSDEV, P_MAXDEV)
+    float k = 0.0f;  // shift (P_SHIFTED) or FP32 mean (P_ABSDEV)
+    float hi = -INFINITY, lo = INFINITY;  // P_SUMRANGE
     __device__ __forceinline__ void add(float x) {
         if constexpr (P == P_SUM) {
             a = __fadd_rn(a, x);
+        } else if constexpr (P == P_SUMRANGE) {
+            a = __fadd_rn(a, x);
+            hi = fmaxf(hi, x);  // NaNs are skipped here and carried by the sum
+            lo = fminf(lo, x);
         } else if constexpr (P == P_SHIFTED) {
             const float d = __fsub_rn(x, k);
             a = __fadd_rn(a, d);
             b = __fmaf_rn(d, d, b);
-        } else if constexpr (P == P_ABSDEV) {
-            a = __fadd_rn(a, fabsf(__fsub_rn(x, k)));
         } else {
-            const float d = fabsf(__fsub_rn(x, k));
-            a = fmaxf(a, d);
-            if (d != d) b = 1.0f;  // NaN: the maximum is NaN, as torch's amax
+            a = __fadd_rn(a, fabsf(__fsub_rn(x, k)));
         }
     }
 };
 
 // Combines a channel's split results in double (one warp) and writes the
 // FP32 statistic. P_SUM writes mean; P_SHIFTED mean and the biased variance
-// (to dev); P_ABSDEV / P_MAXDEV dev. running_mean / running_dev (NULL: not
-// updated) take r (1 - m) + m s for what was written.
+// (to dev); P_ABSDEV dev; P_SUMRANGE mean and max |x - mean| (to
+// dev). running_mean / running_dev (NULL: not updated) take r (1 - m) + m s
+// for what was written.
 template <int P>
 __device__ __forceinline__ void finalize_channel(const double2* part, const BnGeo& g, int64_t ch,
                                                  const float* x, float* mean, float* dev,
                                                  float* running_mean, float* running_dev,
                                                  float momentum) {
     const int lane = threadIdx.x & 31;
-    double a = 0.0, b = 0.0;
+    double a = 0.0, b = P == P_SUMRANGE ? pack_range(-INFINITY, INFINITY) : 0.0;
     for (int s = lane; s < g.splits; s += 32) {
         const double2 p = __ldcg(part + ch * g.splits + s);
-        a = (P == P_MAXDEV) ? fmax(a, p.x) : a + p.x;
-        b += p.y;
+        a += p.x;
+        b = (P == P_SUMRANGE) ? range_join(b, p.y) : b + p.y;
     }
-    a = (P == P_MAXDEV) ? warp_max(a) : warp_sum(a);
-    b = warp_sum(b);
+    a = warp_sum(a);
+    b = (P == P_SUMRANGE) ? warp_range(b) : warp_sum(b);
     if (lane != 0) return;
     const double cnt = (double)g.n * (double)g.inner;
     const float keep = __fsub_rn(1.0f, momentum);
@@ -151,6 +170,14 @@ __device__ __forceinline__ void finalize_channel(const double2* part, const BnGe
         const float m = (float)(a / cnt);
         mean[ch] = m;
         track(running_mean, m);
+    } else if constexpr (P == P_SUMRANGE) {
+        const float m = (float)(a / cnt);
+        const float d1 = __fsub_rn(range_hi(b), m), d2 = __fsub_rn(m, range_lo(b));
+        const float d = (d1 != d1 || d2 != d2) ? __int_as_float(0x7FC00000) : fmaxf(d1, d2);
+        mean[ch] = m;
+        dev[ch] = d;
+        track(running_mean, m);
+        track(running_dev, d);
     } else if constexpr (P == P_SHIFTED) {
         const double k = (double)x[ch * g.inner];
         const double d = a / cnt;
@@ -161,11 +188,8 @@ __device__ __forceinline__ void finalize_channel(const double2* part, const BnGe
         dev[ch] = (float)var;
         track(running_mean, m);
         track(running_dev, (float)var);
-    } else if constexpr (P == P_ABSDEV) {
-        dev[ch] = (float)(a / cnt);
-        track(running_dev, dev[ch]);
     } else {
-        dev[ch] = b > 0.0 ? __int_as_float(0x7FC00000) : (float)a;
+        dev[ch] = (float)(a / cnt);
         track(running_dev, dev[ch]);
     }
 }
@@ -183,7 +207,7 @@ stats_pass_kernel(const float* __restrict__ x, BnGeo g, const float* __restrict_
     const int64_t ch = blockIdx.y;
     Acc<P> acc;
     if constexpr (P == P_SHIFTED) acc.k = x[ch * g.inner];
-    if constexpr (P == P_ABSDEV || P == P_MAXDEV) acc.k = center[ch];
+    if constexpr (P == P_ABSDEV) acc.k = center[ch];
     if (g.flat) {
         const int64_t per_ch = g.n * g.inner;
         const int64_t j0 = (int64_t)s * g.elems_per;
@@ -225,9 +249,9 @@ stats_pass_kernel(const float* __restrict__ x, BnGeo g, const float* __restrict_
     }
     __shared__ double red[2][NT / 32];
     __shared__ int last;
-    double a = acc.a, b = acc.b;
-    a = (P == P_MAXDEV) ? warp_max(a) : warp_sum(a);
-    b = warp_sum(b);
+    double a = acc.a, b = P == P_SUMRANGE ? pack_range(acc.hi, acc.lo) : (double)acc.b;
+    a = warp_sum(a);
+    b = (P == P_SUMRANGE) ? warp_range(b) : warp_sum(b);
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
         red[0][w] = a;
@@ -237,8 +261,8 @@ stats_pass_kernel(const float* __restrict__ x, BnGeo g, const float* __restrict_
     if (threadIdx.x == 0) {
         double ta = red[0][0], tb = red[1][0];
         for (int i = 1; i < NT / 32; ++i) {
-            ta = (P == P_MAXDEV) ? fmax(ta, red[0][i]) : ta + red[0][i];
-            tb += red[1][i];
+            ta += red[0][i];
+            tb = (P == P_SUMRANGE) ? range_join(tb, red[1][i]) : tb + red[1][i];
         }
         part[ch * g.splits + s] = make_double2(ta, tb);
         __threadfence();
@@ -444,13 +468,16 @@ int lofgb_bn_stats_f32(const float* x, int64_t n, int64_t c, int64_t inner, int 
         if ((rc = run_pass<P_SHIFTED>(x, g, nullptr, part, tickets, mean, dev, running_mean, running_dev,
                                       momentum, st)))
             return rc;
+    } else if (stat == LOFGB_BN_MAX_ABS_DEV) {
+        if ((rc = run_pass<P_SUMRANGE>(x, g, nullptr, part, tickets, mean, dev, running_mean, running_dev,
+                                       momentum, st)))
+            return rc;
     } else {
         if ((rc = run_pass<P_SUM>(x, g, nullptr, part, tickets, mean, dev, running_mean, nullptr, momentum, st)))
             return rc;
-        rc = stat == LOFGB_BN_MEAN_ABS_DEV
-                 ? run_pass<P_ABSDEV>(x, g, mean, part, tickets, mean, dev, nullptr, running_dev, momentum, st)
-                 : run_pass<P_MAXDEV>(x, g, mean, part, tickets, mean, dev, nullptr, running_dev, momentum, st);
-        if (rc) return rc;
+        if ((rc = run_pass<P_ABSDEV>(x, g, mean, part, tickets, mean, dev, nullptr, running_dev, momentum,
+                                     st)))
+            return rc;
     }
     return check_launch("BatchNorm statistics");
 }

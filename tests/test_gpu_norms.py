@@ -147,6 +147,33 @@ def test_unaligned_in_place_and_flat_paths():
     assert torch.equal(dev, (x2 - mean).abs().amax(dim=0))
 
 
+@pytest.mark.parametrize("shape", [(32, 256, 56, 56), (16, 64, 9, 13), (5000, 3), (2, 3, 1000)])
+def test_max_deviation_equals_centred_amax(shape):
+    """The single pass's max(max x - mean, mean - min x) has the bits of the
+    maximum over every centred value, taken about the same FP32 mean."""
+    g = torch.Generator(device="cuda").manual_seed(31 + sum(shape))
+    x = torch.randn(*shape, device="cuda", generator=g) * 3 + 1
+    mean, dev = lof.bn_stats(x, lof.BnStat.MAX_ABS_DEV)
+    view = [1, -1] + [1] * (x.dim() - 2)
+    dims = [0] + list(range(2, x.dim()))
+    assert torch.equal(dev, (x - mean.view(view)).abs().amax(dim=dims))
+
+
+def test_max_deviation_with_infinities_and_nan():
+    x = torch.randn(6, 7, 50, device="cuda")
+    x[1, 0, 3] = float("inf")                                   # mean inf: inf - inf
+    x[2, 1, 4] = float("-inf")                                  # mean -inf
+    x[0, 2, 5], x[3, 2, 6] = float("inf"), float("-inf")        # mean NaN
+    x[4, 3, 7] = float("nan")
+    x[:, 4] = 2.5                                               # constant: deviation +0
+    x[:, 5] = 1.0e30                                            # large, equal values
+    mean, dev = lof.bn_stats(x, lof.BnStat.MAX_ABS_DEV)
+    want = (x - mean.view(1, -1, 1)).abs().amax(dim=(0, 2))
+    torch.testing.assert_close(dev, want, rtol=0, atol=0, equal_nan=True)
+    assert torch.isnan(dev[:4]).all() and not torch.isnan(dev[4:]).any()
+    assert dev[4].item() == 0.0 and not torch.signbit(dev[4])
+
+
 def test_nan_propagates_to_max_deviation():
     x = torch.randn(4, 3, 100, device="cuda")
     x[2, 1, 7] = float("nan")
