@@ -173,7 +173,10 @@ __device__ __forceinline__ void finalize_channel(const double2* part, const BnGe
     } else if constexpr (P == P_SUMRANGE) {
         const float m = (float)(a / cnt);
         const float d1 = __fsub_rn(range_hi(b), m), d2 = __fsub_rn(m, range_lo(b));
-        const float d = (d1 != d1 || d2 != d2) ? __int_as_float(0x7FC00000) : fmaxf(d1, d2);
+        // the larger difference is never below zero; clearing the sign makes
+        // a zero deviation +0 as |x - mean| is (all x -0: -0 - (+0) = -0)
+        const float d = (d1 != d1 || d2 != d2) ? __int_as_float(0x7FC00000)
+                                               : __int_as_float(__float_as_int(fmaxf(d1, d2)) & 0x7FFFFFFF);
         mean[ch] = m;
         dev[ch] = d;
         track(running_mean, m);

@@ -100,3 +100,49 @@ def test_forward_needs_cuda():
 def test_golden_fixture_is_consistent(golden):
     assert golden["bn_nchw_x"].shape == (8, 6, 5, 7)
     assert np.isfinite(golden["bn_nchw_fisr_y_train"]).all()
+
+
+def _max_centred(x, m):
+    """max |x - m| over FP32 differences, NaN if any difference is NaN."""
+    d = np.abs(x - m)
+    return np.float32(np.nan) if np.isnan(d).any() else d.max()
+
+
+def _max_from_range(x, m):
+    """max(max x - m, m - min x) in FP32 with the sign cleared (the larger
+    difference is never below zero, but is -0 for x all -0 about m = +0), NaN
+    if either difference is; NaN inputs are skipped by the range, as fmaxf /
+    fminf do."""
+    hi, lo = np.nanmax(x), np.nanmin(x)
+    d1, d2 = np.float32(hi - m), np.float32(m - lo)
+    return np.float32(np.nan) if np.isnan(d1) or np.isnan(d2) else np.abs(max(d1, d2))
+
+
+def test_max_deviation_identity_in_fp32():
+    """LinfBatchNorm's max |x - mean| from one pass: with FP32 subtraction
+    rounded monotonically, the largest rounded |x - m| comes from max x or
+    min x, for any FP32 m (the mean the kernel computes, or one placed
+    anywhere, ties and signed zeros included); a NaN x makes the mean NaN."""
+    rng = np.random.default_rng(17)
+    with np.errstate(invalid="ignore", over="ignore"):
+        for trial in range(3000):
+            n = int(rng.integers(1, 200))
+            scale = np.float32(10.0 ** rng.integers(-40, 38))
+            x = (rng.standard_normal(n) * scale).astype(np.float32)
+            if trial % 7 == 0:
+                x[rng.integers(0, n)] = np.float32(rng.choice([np.inf, -np.inf, 0.0, -0.0]))
+            if trial % 11 == 0:
+                x[:] = x[0]
+            if trial % 17 == 0:
+                x[:] = np.float32(-0.0)
+            m = np.float32(x.astype(np.float64).mean())
+            if trial % 2 == 0:      # the kernel's sums start at +0
+                m = np.float32(m + np.float32(0.0))
+            if trial % 5 == 0:      # a centre off the mean, inside or outside the range
+                m = np.float32(m + rng.standard_normal() * scale)
+            if trial % 13 == 0:
+                x[rng.integers(0, n)] = np.float32(np.nan)
+                m = np.float32(np.nan)
+            want, got = _max_centred(x, m), _max_from_range(x, m)
+            assert (np.isnan(want) and np.isnan(got)) or \
+                (want == got and np.signbit(want) == np.signbit(got)), (trial, x, m, want, got)

@@ -167,11 +167,13 @@ def test_max_deviation_with_infinities_and_nan():
     x[4, 3, 7] = float("nan")
     x[:, 4] = 2.5                                               # constant: deviation +0
     x[:, 5] = 1.0e30                                            # large, equal values
+    x[:, 6] = -0.0                                              # mean +0, deviation +0
     mean, dev = lof.bn_stats(x, lof.BnStat.MAX_ABS_DEV)
     want = (x - mean.view(1, -1, 1)).abs().amax(dim=(0, 2))
     torch.testing.assert_close(dev, want, rtol=0, atol=0, equal_nan=True)
     assert torch.isnan(dev[:4]).all() and not torch.isnan(dev[4:]).any()
     assert dev[4].item() == 0.0 and not torch.signbit(dev[4])
+    assert dev[6].item() == 0.0 and not torch.signbit(dev[6])
 
 
 def test_nan_propagates_to_max_deviation():
