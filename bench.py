@@ -164,7 +164,7 @@ def whole_job_gbs(world, steps, step_bytes, seconds):
     return world * steps * step_bytes / seconds / 1e9
 
 
-def config2_input(torch, dev):
+def mx_matrix_input(torch, dev):
     g = torch.Generator().manual_seed(2)
     x = torch.randn(MX_ROWS * MX_COLS, generator=g, dtype=torch.float32)
     mask = torch.rand(MX_ROWS * MX_COLS, generator=g) < 0.01
@@ -191,7 +191,7 @@ def run_reference(args, world, rank):
     from oracle import oracle as O
     threads = O.max_threads()
     # the whole 8192 x 8192 matrix per format per step: the same work as our arm
-    sample = config2_input(torch, None).reshape(-1).numpy()
+    sample = mx_matrix_input(torch, None).reshape(-1).numpy()
     sf = O.fmt(8, 0, 127, saturating=False, signed=False)
     efs = [O.fmt(*v) for v in ELEM_FORMATS.values()]
 
@@ -226,7 +226,7 @@ def cpu_baseline_sample():
 
     from oracle import oracle as O
     threads = O.max_threads()
-    x = config2_input(torch, None).reshape(-1).numpy()[: 1 << 22]
+    x = mx_matrix_input(torch, None).reshape(-1).numpy()[: 1 << 22]
     sf = O.fmt(8, 0, 127, saturating=False, signed=False)
     efs = [O.fmt(*v) for v in ELEM_FORMATS.values()]
     O.mx_round(x, MX_BLOCK, efs[1], sf, nthreads=threads)
@@ -274,7 +274,7 @@ def time_batched(torch, fn, stream, per_batch=10, batches=5):
 
 
 def secondary(torch, lg, dev, peaks):
-    """Plain rounding (config-1 workload) and the 4096^3 emulated GEMMs."""
+    """Plain rounding of 2^24 FP32 values to E4M3 and the 4096^3 emulated GEMMs."""
     out = {}
     stream = torch.cuda.current_stream(dev)
     g = torch.Generator().manual_seed(0)
@@ -438,7 +438,7 @@ def graph_of(torch, fn):
 
 
 def codec_workloads(torch, lg, dev, peaks):
-    """Storage codec over 2^26 FP32 values (config-1 distribution): encode to
+    """Storage codec over 2^26 FP32 values (N(0,1) * 2^U{-20..20}): encode to
     packed E4M3 (8-bit) and P3109<6,3> (6-bit) codes and decode back, GB/s at
     4 + n/8 bytes per value."""
     out = {}
@@ -460,10 +460,10 @@ def codec_workloads(torch, lg, dev, peaks):
             gbs = n * (4 + bits / 8) / (ms * 1e-3) / 1e9
             out[f"codec_{tag}_{name}_2^26_GBs"] = round(gbs, 1)
             out[f"codec_{tag}_{name}_2^26_frac_hbm"] = round(gbs / peaks["hbm_gbs"], 4)
-    # MX storage of the config-2 matrix in one pass: E4M3 / FP6 element codes
+    # MX storage of the 8192 x 8192 matrix in one pass: E4M3 / FP6 element codes
     # and E8M0 block scales (4 B read, bits/8 + 1/32 B written per value)
     del x, y
-    xm = config2_input(torch, None).to(dev)
+    xm = mx_matrix_input(torch, None).to(dev)
     e8 = lg.create_e8m0_params()
     for name, fmt in (("e4m3", lg.create_p3109_params(8, 4)), ("p3109_6p3", lg.create_p3109_params(6, 3))):
         fn = lambda: lg.mx_encode(xm, fmt, e8)  # noqa: E731
@@ -531,10 +531,10 @@ def linear_fwd_bwd(torch, lg, dev):
 
 
 def grouped_round_case(torch, lg, dev, item="auto"):
-    """Config-5 part 1: 512 FP32 tensors, each with its own format and mode
+    """Grouped rounding: 512 FP32 tensors, each with its own format and mode
     (seed 5). Returns the grouped launch, the per-tensor specs (exp and
     mantissa bits, saturation, mode, stoch_len, seed) and the two generators,
-    which part 2 continues."""
+    which the grouped GEMMs continue."""
     rng = np.random.default_rng(5)
     g = torch.Generator(device=dev).manual_seed(5)
     ins, outs, fmts, modes, lens, seeds, specs = [], [], [], [], [], [], []
@@ -556,9 +556,9 @@ def grouped_round_case(torch, lg, dev, item="auto"):
 
 
 def grouped_gemm_case(torch, lg, dev, rng, g):
-    """Config-5 part 2: 64 emulated GEMMs, M, N, K in {256..4096 step 256},
+    """Grouped GEMMs: 64 emulated GEMMs, M, N, K in {256..4096 step 256},
     MX-E4M3 operands (B given transposed, blocks along K), accumulator bits
-    7-12, chunk 32; continues part 1's generators."""
+    7-12, chunk 32; continues the grouped rounding's generators."""
     e4m3 = fmt_desc(lg, 8, 3, 7)
     e8 = lg.create_e8m0_params()
     tasks = []
@@ -572,10 +572,10 @@ def grouped_gemm_case(torch, lg, dev, rng, g):
 
 
 def grouped_workloads(torch, lg, dev):
-    """Config-5 workloads. Part 1: 512 FP32 tensors, n ~ 2^U(10,24), values
+    """The grouped workloads. Rounding: 512 FP32 tensors, n ~ 2^U(10,24), values
     N(0,1)*2^U(-10,10), each with its own format (exp 2-8, mant 1-10, bias
     2^(e-1)-1, saturating or not) and mode (RNE/RTZ/RTO/SR-A), seed 5: one
-    grouped launch replayed from a CUDA graph. Part 2: 64 emulated GEMMs,
+    grouped launch replayed from a CUDA graph. GEMMs: 64 emulated GEMMs,
     M,N,K in {256..4096 step 256}, MX-E4M3 operands, accumulator bits 7-12,
     one grouped tensor-core launch with the autotuned schedule, from a graph."""
     out = {}
@@ -706,7 +706,7 @@ def run_ours(args, world, rank, local):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
     peaks, peak_src = measured_peaks()
-    x_host = config2_input(torch, None)
+    x_host = mx_matrix_input(torch, None)
     x = x_host.to(dev)
     y = torch.empty_like(x)
     e8 = lg.create_e8m0_params()
@@ -866,7 +866,7 @@ def run_only(args):
     e4m3 = fmt_desc(lg, 8, 3, 7)
     e8 = lg.create_e8m0_params()
     if args.only == "mx":
-        x = config2_input(torch, None).to(dev)
+        x = mx_matrix_input(torch, None).to(dev)
         y = torch.empty_like(x)
         fn = lambda: lg.virtual_mx_round(x, MX_BLOCK, e4m3, e8, out=y)  # noqa: E731
         work, unit = MX_BYTES, "GB/s"
@@ -903,7 +903,7 @@ def run_only(args):
             (lambda: lg.lof_decode(packed, n, fmt, out=y))  # noqa: E731
         work, unit = n * (4 + bits / 8), "GB/s"
     elif args.only == "mx_encode":
-        x = config2_input(torch, None).to(dev)
+        x = mx_matrix_input(torch, None).to(dev)
         fn = lambda: lg.mx_encode(x, e4m3, e8)  # noqa: E731
         work, unit = x.numel() * (4 + 1 + 1 / 32), "GB/s"
     elif args.only in ("bn_train", "bn_eval"):

@@ -839,7 +839,8 @@ gemm_tc_grouped_kernel(const GroupHeader* __restrict__ h) {
 // The same for a tile width the host names at launch; a table prepared for
 // another width is refused on the device (status LOFGB_ERR_UNSUPPORTED,
 // nothing computed). The 64- and 128-column bodies are inlined here (on the
-// config-5 mix 14.69 / 11.56 ms against 16.27 / 12.17 through the call);
+// mix of 64 GEMMs of 256..4096 14.69 / 11.56 ms against 16.27 / 12.17
+// through the call);
 // the 256-column body measured faster through its own function (11.51
 // against 11.67 ms inlined) and is called.
 template <int BN>

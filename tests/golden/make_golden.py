@@ -86,7 +86,7 @@ def inputs_f32(rng, f, n=512):
     m, to_max, to_min, tiny = consts(f)
     d = 23 - m
     vals = []
-    # config-1 style values N(0,1)*2^U{-20..20}
+    # values of the 2^24-element rounding workload: N(0,1)*2^U{-20..20}
     vals += list((rng.standard_normal(200) * 2.0 ** rng.integers(-20, 21, 200)).astype(np.float32))
     # values across the format's exponent range and just outside it
     lo, hi = max(to_min - m - 3, -149), min(to_max + 3, 127)
@@ -255,7 +255,8 @@ def gen_round(R, rng, out):
 
 MX_CASES = [
     # (block, elem, scale, mode) — the combinations of
-    # test/test_virtual_mx_round_cuda.cu:139-152 plus the config-2 formats
+    # test/test_virtual_mx_round_cuda.cu:139-152 plus the E2M1 / E4M3 / E5M2
+    # formats of the 8192 x 8192 MX rounding workload
     (32, "e4m3", "e8m0", 0), (8, "e4m3", "e8m0", 5), (16, "e5m2", "e8m0", 6),
     (128, "e4m3", "e8m0", 0), (64, "e4m3", "e5m2s", 1), (128, "e5m2", "e8m0", 0),
     (256, "e4m3", "e8m0", 5), (256, "e5m2", "e8m0", 0), (32, "e2m1", "e8m0", 0),
@@ -295,7 +296,8 @@ def gen_mx(R, rng, out):
             # elements where the CPU expression amax / pmn gives a different result
             rec["cpu_formula_diff"] = np.int64(np.sum(ys[0].view(np.uint32) != ys[1].view(np.uint32)))
             out[f"mx_b{bs}_{en}_{sn}_m{mode}_n{n}"] = rec
-    # config-2-like data: N(0,1) with 1% outliers scaled by 2^12, blocks of 32
+    # the 8192 x 8192 workload's distribution: N(0,1) with 1% outliers scaled
+    # by 2^12, blocks of 32, on 16384 values
     x = rng.standard_normal(16384).astype(np.float32)
     x[rng.random(16384) < 0.01] *= 4096.0
     for en in ("e2m1", "e4m3", "e5m2"):
@@ -310,13 +312,13 @@ def gen_mx(R, rng, out):
             ys.append(y)
         rec["y"] = ys[0]
         rec["cpu_formula_diff"] = np.int64(np.sum(ys[0].view(np.uint32) != ys[1].view(np.uint32)))
-        out[f"mx_config2_{en}"] = rec
+        out[f"mx_outliers_{en}"] = rec
 
 
 def gen_gemm(R, rng, out):
     e4m3, e8m0 = O.fmt(8, 3, 7), O.fmt(8, 0, 127, saturating=False, signed=False)
     cases = []
-    # MX-E4M3 operands along K (config-3 scheme), 10-bit accumulator
+    # MX-E4M3 operands along K (the 4096^3 GEMM workload's scheme), 10-bit accumulator
     A = O.mx_round(rng.standard_normal((24, 256)).astype(np.float32), 32, e4m3, e8m0)
     Bt = O.mx_round(rng.standard_normal((20, 256)).astype(np.float32), 32, e4m3, e8m0)
     cases.append(("mx_e4m3_m10", A, np.ascontiguousarray(Bt.T), 10, 1.0))

@@ -28,7 +28,7 @@ def ofmt(d):
                     int(d.signedness), 0)
 
 
-def config1_data(n=1 << 24, seed=0):
+def round_data_2p24(n=1 << 24, seed=0):
     """N(0,1)·2^u, u ~ U{-20..20}, float32 (the plain-rounding workload)."""
     g = torch.Generator().manual_seed(seed)
     x = torch.randn(n, generator=g, dtype=torch.float32)
@@ -36,7 +36,7 @@ def config1_data(n=1 << 24, seed=0):
     return (x * torch.exp2(u.float())).numpy()
 
 
-def config2_data(rows=8192, cols=8192, seed=2):
+def mx_matrix_data(rows=8192, cols=8192, seed=2):
     """N(0,1) with 1% of elements scaled by 2^12, float32 (the MX workload)."""
     g = torch.Generator().manual_seed(seed)
     x = torch.randn(rows * cols, generator=g, dtype=torch.float32)

@@ -1,20 +1,20 @@
 """Parity at the benchmark workloads' own sizes.
 
-  * Config 3 (4096^3 emulated GEMM, MX-E4M3 operands, 10-bit accumulator,
+  * the 4096^3 emulated GEMM (MX-E4M3 operands, 10-bit accumulator,
     CUDA-core form): 256 rows (16 blocks of 16 spread over M) bit-exact
     against the oracle, and the whole output bit-identical to the transposed
     problem D^T = B^T A^T, which reads the operands through the other
     loaders and tiles (every output is the same sequence of products, and
     a*b = b*a exactly);
-  * config 4 (differentiable linear layer, X 8192x4096, W 4096x4096, BF16
+  * the differentiable linear layer (X 8192x4096, W 4096x4096, BF16
     masters, MX-E4M3, FP16-like 5e/10m accumulator in 64-element chunks,
     dY stochastic-rounded to E5M2): output and gradients at full size against
     the FP64 surrogate (autograd through the rounded operands), with stated
     bounds;
-  * config 5 part 1 (512 tensors, each its own format and mode, one grouped
+  * the grouped rounding (512 tensors, each its own format and mode, one grouped
     launch): every tensor against the oracle — whole tensors up to 2^20
     elements, head, tail and 16 random windows of 4096 beyond;
-  * config 5 part 2 (64 GEMMs of 256..4096, one grouped tensor-core launch):
+  * the grouped GEMMs (64 GEMMs of 256..4096, one grouped tensor-core launch):
     sampled rows of every GEMM against the CPU chunked model, within the
     tensor-core tests' bound.
 """
@@ -38,7 +38,7 @@ def _err_units(got, want, Arows, B, mbits):
     return np.abs(got.astype(np.float64) - want.astype(np.float64)) / (np.exp2(-mbits) * np.maximum(S, 1e-30))
 
 
-def test_config3_plain_256_rows_and_transposed_full_output():
+def test_gemm_4096_plain_256_rows_and_transposed_full_output():
     g = torch.Generator().manual_seed(3)
     A = torch.randn(4096, 4096, generator=g).cuda()
     Bt = torch.randn(4096, 4096, generator=g).cuda()
@@ -56,7 +56,7 @@ def test_config3_plain_256_rows_and_transposed_full_output():
         assert same_bits(Dh[r0:r0 + 16], want), f"rows {r0}..{r0 + 15}"
 
 
-def test_config4_linear_full_size_against_fp64():
+def test_linear_8192x4096x4096_against_fp64():
     g = torch.Generator(device="cuda").manual_seed(4)
     X = torch.randn(8192, 4096, device="cuda", generator=g).bfloat16().requires_grad_(True)
     W = (torch.randn(4096, 4096, device="cuda", generator=g) * 0.02).bfloat16().requires_grad_(True)
@@ -85,7 +85,7 @@ def test_config4_linear_full_size_against_fp64():
 
 
 @pytest.fixture(scope="module")
-def config5():
+def grouped_workloads():
     dev = torch.device("cuda", 0)
     gr, specs, rng, g = bench.grouped_round_case(torch, lg, dev, item=1 << 16)
     gr()
@@ -102,8 +102,8 @@ def _windows(n, rng):
     return [(s, s + 4096) for s in starts]
 
 
-def test_config5_grouped_rounding_every_tensor(config5):
-    gr, specs, _, _ = config5
+def test_grouped_rounding_512_tensors_every_tensor(grouped_workloads):
+    gr, specs, _, _ = grouped_workloads
     wrng = np.random.default_rng(55)
     checked = 0
     for i, sp in enumerate(specs):
@@ -119,8 +119,8 @@ def test_config5_grouped_rounding_every_tensor(config5):
     assert len(specs) == 512 and checked > 10_000_000
 
 
-def test_config5_grouped_gemms_every_task(config5):
-    _, _, rng, g = config5
+def test_grouped_gemms_64_every_task(grouped_workloads):
+    _, _, rng, g = grouped_workloads
     dev = torch.device("cuda", 0)
     tasks = bench.grouped_gemm_case(torch, lg, dev, rng, g)
     gg = lg.GroupedGemm(tasks, schedule="lpt_snake")

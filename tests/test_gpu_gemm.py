@@ -100,7 +100,7 @@ def test_alpha_and_dropin_signature():
         lg.lof_gemm(Ag.cpu(), Bg.cpu(), 10)
 
 
-def test_config3_sample_rows():
+def test_gemm_4096_sample_rows():
     """M=N=K=4096, MX-E4M3 operands, 10-bit accumulator: 32 sampled rows of the
     full-size GPU output are bit-exact against the oracle, and the whole
     output agrees with an FP64 GEMM to the accumulator's precision."""

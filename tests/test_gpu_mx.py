@@ -7,7 +7,7 @@ import torch
 
 import lofloat_gb300 as lg
 from golden_io import cases, fmt_tuple, same_bits_nan_class
-from gpu_util import config2_data, from_gpu, mismatch_report, ofmt, to_gpu
+from gpu_util import mx_matrix_data, from_gpu, mismatch_report, ofmt, to_gpu
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -37,10 +37,10 @@ def test_golden_mx(cname, rec):
 
 
 @pytest.mark.parametrize("elem", [E2M1, E4M3, E5M2])
-def test_config2_full_size(elem):
+def test_mx_8192x8192_full_size(elem):
     """8192x8192 N(0,1) with 1% outliers x2^12, blocks of 32 along rows, E8M0
     scale, RNE: bit-exact against the oracle at full size."""
-    x = config2_data()
+    x = mx_matrix_data()
     ef, sf = _desc(elem), _desc(E8M0)
     got = from_gpu(lg.virtual_mx_round(to_gpu(x), 32, ef, sf))
     want = O.mx_round(x, 32, ofmt(ef), ofmt(sf))
@@ -155,7 +155,7 @@ def test_bf16_source_equals_fp32_copy(bs, mode, skew):
     assert torch.equal(got.view(torch.int32), want.view(torch.int32))
 
 
-def test_bf16_source_config4_operands():
+def test_bf16_source_linear_operands():
     """The linear layer's MX-E4M3 rounding of BF16 masters (8192 x 4096) read
     directly equals rounding the FP32 copy."""
     g = torch.Generator(device="cuda").manual_seed(4)

@@ -9,7 +9,7 @@ import pytest
 import torch
 
 import lofloat_gb300 as lg
-from gpu_util import config2_data, from_gpu, to_gpu
+from gpu_util import mx_matrix_data, from_gpu, to_gpu
 from lofloat_gb300 import _native
 from oracle import oracle as O
 
@@ -99,17 +99,17 @@ def test_modes_and_misaligned_buffers(skew, mode, ln):
     assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
 
 
-def test_config2_storage_against_oracle_and_mx_round():
-    """Config-2 data (8192 x 8192, 1 % outliers x 2^12): the GPU's element
+def test_mx_8192x8192_storage_against_oracle_and_mx_round():
+    """The 8192 x 8192 matrix (N(0,1), 1 % outliers x 2^12): the GPU's element
     codes and E8M0 scales equal the oracle's byte for byte over the whole
     matrix; and decode(codes) * scale equals the MX-E4M3 rounding wherever
     the rounding's quotient is an E4M3 value (equal values: P3109 formats
     have no -0, their sign-only code being NaN, so -0 is stored as +0).
-    Elsewhere — about 4 % of config-2 quotients overflow E4M3 and pass
+    Elsewhere — about 4 % of this matrix's quotients overflow E4M3 and pass
     through the rounding unrounded — storage holds the largest finite code
     (SatFinite): the decoded value is that code's value times the block
     scale, with the rounding's sign and a smaller magnitude."""
-    x = config2_data()
+    x = mx_matrix_data()
     xg = to_gpu(x)
     e4m3, e8 = lg.create_p3109_params(8, 4), lg.create_e8m0_params()
     codes, scales = lg.mx_encode(xg, e4m3, e8)

@@ -6,7 +6,7 @@ import torch
 
 import lofloat_gb300 as lg
 from golden_io import cases, fmt_tuple, same_bits
-from gpu_util import config1_data, from_gpu, mismatch_report, ofmt, to_gpu
+from gpu_util import round_data_2p24, from_gpu, mismatch_report, ofmt, to_gpu
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -158,11 +158,11 @@ def test_misaligned_and_inplace():
     assert same_bits(from_gpu(y), O.round(x, ofmt(desc), 0))
 
 
-def test_config1_full_size():
+def test_round_2p24_full_size():
     """2^24 FP32, E4M3 (bias 7, saturating): RNE, then SR-A (stoch_len 8,
     seed 1), bit-exact against the oracle at full size."""
     desc = _desc((8, 3, 7, True, True))
-    x = config1_data()
+    x = round_data_2p24()
     xg = to_gpu(x)
     got = from_gpu(lg.virtual_round(xg, desc, round_mode=0))
     assert same_bits(got, O.round(x, ofmt(desc), 0))

@@ -135,7 +135,7 @@ def test_exact_inputs_match_plain():
     assert np.array_equal(from_gpu(tc), (A.astype(np.float64) @ B).astype(np.float32))
 
 
-def test_config3_error_vs_fp64():
+def test_gemm_4096_error_vs_fp64():
     """M=N=K=4096, MX-E4M3 operands along K, 10-bit accumulator, chunk 32:
     the error against the FP64 oracle is of the accumulator's order and
     close to the bit-exact CUDA-core form's."""
