@@ -263,6 +263,8 @@ def test_grouped_gemm_validation_host_only():
     assert prep(good, ws=0x100010) == -9                     # workspace misaligned
     assert prep(good, tbytes=tb_need - 1) == -9              # table too small
     assert prep(good, sched=5) == -7                         # unknown schedule
+    assert prep(good, sched=1 | 16 | 32) == -7               # two tile widths in one table
+    assert prep(good, sched=3 | 32) == -7                    # unknown schedule, wide tile
 
 
 def test_codec_validation_and_sizes():
