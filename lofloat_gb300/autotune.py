@@ -2,11 +2,13 @@
 
 ``GroupedGemm`` runs many emulated-accumulation GEMMs of different shapes,
 each with its own accumulator width, chunk and alpha, as one operand-split
-launch plus one persistent tcgen05 launch (lofgb_gemm_grouped_launch), and
-can capture both in a CUDA graph.
+launch plus one persistent tcgen05 launch (lofgb_gemm_grouped_launch_w, the
+kernel built for the table's tile width), and can capture both in a CUDA
+graph.
 
-The tile shape (128 x 128, or 128 x 64: twice the tiles, finer load balance
-over uneven GEMMs, more operand traffic per product) and the tile schedule —
+The tile shape (128 x 128; 128 x 64: twice the tiles, finer load balance
+over uneven GEMMs, more operand traffic per product; 128 x 256: half the
+tiles, one MMA per 256 columns) and the tile schedule —
 the order in which the persistent CTAs take the output tiles of all GEMMs —
 decide load balance when the GEMMs differ in size. ``GroupedGemm(...,
 schedule="auto")`` times every (shape, schedule) pair the library offers
